@@ -1,0 +1,410 @@
+"""Benchmark of the matched-filter hot path on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload config4|config1|config2|config0] [--precision ...]
+
+One *step* is one complete search of the workload (every template against
+every channel and output index: preprocessing kernels + correlation
+kernel).  Metric: template*lag*channel multiply-accumulates per second
+(T * n_corr * S * C * L per step, TMAC/s).
+
+  value     device-resident inputs, K steps timed with CUDA events on the
+            launching stream, barrier + synchronize on both sides, max over
+            ranks; inputs (1 GB of data for the full-day search) exceed L2.
+  e2e       the same search through the C ABI (fmf_matched_filter_ex) with
+            pinned host buffers: H2D of every input and D2H of the whole
+            output inside each timed step.
+  roofline  the correlation kernel, event-timed inside the timed region.
+  cpu_baseline  the oracle's C port of the reference CPU algorithm (OpenMP,
+            all host cores) on a bounded sample of the same workload.
+
+--impl reference times that CPU algorithm alone (rank 0; other ranks exit).
+Under torchrun each rank searches its own template set against the same
+data (weak scaling); the only collectives are the barrier and the max of
+the per-rank times.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+METRIC = "template*lag*channel TMAC/s"
+UNIT = "TMAC/s"
+PEAKS_FILE = os.path.join(HERE, "MEASURED_PEAKS.json")
+FALLBACK_PEAKS = {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0,
+                  "sm_max_mhz": 2070.0}
+N_SM = 152
+
+
+def parse_args(argv=None):
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--workload", default="config4")
+    p.add_argument("--precision", default="auto")
+    p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--templates", type=int, default=0, help="override T (smaller runs)")
+    p.add_argument("--samples", type=int, default=0, help="override N (smaller runs)")
+    return p.parse_args(argv)
+
+
+def load_peaks():
+    try:
+        with open(PEAKS_FILE) as f:
+            pk = json.load(f)
+        return pk, "measured"
+    except (OSError, ValueError):
+        return dict(FALLBACK_PEAKS), "fallback"
+
+
+# ---------------------------------------------------------------- workload
+def make_workload(name, rank=0, templates=0, samples=0):
+    from fast_matched_filter_gb300 import synthetic
+    kw = {}
+    if templates:
+        kw["n_templates"] = templates
+    if samples:
+        kw["n_samples"] = samples
+    gen = {"config0": synthetic.config0, "config1": synthetic.config1,
+           "config2": synthetic.config2, "config4": synthetic.config4}[name]
+    if name == "config0":
+        cfg = gen(seed=100 + 1000 * rank)
+    else:
+        cfg = gen(seed={"config1": 101, "config2": 102, "config4": 104}[name] + 1000 * rank, **kw)
+    tp = cfg["templates"]
+    cfg["sst"] = np.sum(tp ** 2, axis=-1).astype(np.float32)
+    cfg["macs"] = synthetic.macs(tp.shape, cfg["data"].shape[-1], cfg["step"])
+    cfg["n_corr"] = (cfg["data"].shape[-1] - tp.shape[-1]) // cfg["step"] + 1
+    return cfg
+
+
+def describe(cfg, extra=None):
+    T, S, C, L = cfg["templates"].shape
+    d = {"workload": cfg["name"], "templates": T, "stations": S, "components": C,
+         "template_length": L, "samples": int(cfg["data"].shape[-1]), "step": cfg["step"],
+         "normalize": cfg["normalize"], "network_sum": cfg["network_sum"],
+         "n_corr": int(cfg["n_corr"]),
+         "l2": "inputs larger than L2 (data %.2f GB > 129 MB); no flush"
+               % (cfg["data"].nbytes / 1e9)}
+    if extra:
+        d.update(extra)
+    return d
+
+
+# ---------------------------------------------------------------- clocks
+class ClockSampler:
+    """nvidia-smi sampling of SM clock and throttle reasons while running."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index):
+        self.dev = device_index
+        self.proc = None
+        self.path = os.path.join(HERE, "gpurun_out", "clocks_bench_%d.csv" % device_index)
+
+    def __enter__(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.dev), "--query-gpu=" + self.Q,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self):
+        if self.proc is None:
+            return None
+        rows = []
+        with open(self.path) as f:
+            for line in f:
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) < 9:
+                    continue
+                try:
+                    rows.append((float(parts[1]), float(parts[2]), float(parts[3]), parts[5:9]))
+                except ValueError:
+                    continue
+        if not rows:
+            return None
+        loaded = [r for r in rows if r[2] > 200.0] or rows
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in loaded for i, v in enumerate(r[3]) if v == "Active"})
+        return {"sm_mhz": statistics.median(r[0] for r in loaded),
+                "sm_max_mhz": max(r[1] for r in rows), "reasons": reasons,
+                "samples": len(loaded), "power_w_max": max(r[2] for r in rows)}
+
+
+# ---------------------------------------------------------------- distributed
+def dist_info():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def dist_max(value, world):
+    """Max of a float over ranks (the only cross-rank reduction of the bench)."""
+    if world <= 1:
+        return value
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([value], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+# ---------------------------------------------------------------- CPU baseline
+def cpu_sample(cfg, n_templates=1):
+    """Bounded sample of the workload for the CPU algorithm: the first
+    template(s) against the whole trace."""
+    sub = dict(cfg)
+    sub["templates"] = cfg["templates"][:n_templates]
+    sub["moveouts"] = cfg["moveouts"][:n_templates]
+    sub["weights"] = cfg["weights"][:n_templates]
+    from fast_matched_filter_gb300 import synthetic
+    sub["macs"] = synthetic.macs(sub["templates"].shape, cfg["data"].shape[-1], cfg["step"])
+    return sub
+
+
+def run_cpu_once(sub, threads):
+    from oracle import cpu
+    arch = "cpu" if sub["normalize"] == "short" else "precise"
+    t0 = time.perf_counter()
+    cpu.run_oracle(sub["templates"], sub["moveouts"], sub["weights"], sub["data"], sub["step"],
+                   arch, sub["normalize"], sub["network_sum"], n_threads=threads)
+    return time.perf_counter() - t0
+
+
+def cpu_baseline(cfg, reps=1):
+    """The CPU algorithm on a bounded sample: the reference library compiled
+    from its own source (oracle/_ref) where it exists, else the oracle port."""
+    from oracle import cpu
+    if not os.path.exists(cpu.ORACLE_SO):
+        cpu.build()
+    threads = os.cpu_count() or 1
+    sub = cpu_sample(cfg)
+    kind = "reference" if cpu.reference_available() else "port"
+    if kind == "reference":
+        os.environ["OMP_NUM_THREADS"] = str(threads)
+        arch = "cpu" if sub["normalize"] == "short" else "precise"
+        t0 = time.perf_counter()
+        cpu.run_reference(sub["templates"], sub["moveouts"], sub["weights"], sub["data"],
+                          sub["step"], arch, sub["normalize"], sub["network_sum"])
+        secs = time.perf_counter() - t0
+    else:
+        secs = min(run_cpu_once(sub, threads) for _ in range(reps))
+    what = ("reference CPU library compiled from its source" if kind == "reference"
+            else "oracle C port of the reference CPU algorithm")
+    return {"value": sub["macs"] / secs / 1e12, "unit": UNIT, "cores": threads, "kind": kind,
+            "sample": "%d of %d templates x full trace (%d samples), %.3g MAC in %.2f s; "
+                      "%s (OpenMP %d threads)"
+                      % (sub["templates"].shape[0], cfg["templates"].shape[0],
+                         cfg["data"].shape[-1], sub["macs"], secs, what, threads),
+            "seconds": secs}
+
+
+def run_reference_arm(args):
+    world, rank, local = dist_info()
+    if rank != 0:
+        return 0
+    cfg = make_workload(args.workload, 0, args.templates, args.samples)
+    from oracle import cpu
+    cpu.build()
+    threads = os.cpu_count() or 1
+    sub = cpu_sample(cfg)
+    for _ in range(args.warmup):
+        run_cpu_once(sub, threads)
+    times = [run_cpu_once(sub, threads) for _ in range(args.steps)]
+    tot = sum(times)
+    value = sub["macs"] * args.steps / tot / 1e12
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic", "impl": "reference",
+            "config": describe(cfg, {"sample": "first template x full trace per step"}),
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": "1 of %d templates x full trace, %.3g MAC per step"
+                                       % (cfg["templates"].shape[0], sub["macs"])},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+# ---------------------------------------------------------------- our arm
+def run_ours(args):
+    import torch
+
+    world, rank, local = dist_info()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", init_method="env://")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    import fast_matched_filter_gb300 as fmf
+    from fast_matched_filter_gb300 import _lib
+    lib = _lib.load()
+
+    cfg = make_workload(args.workload, rank, args.templates, args.samples)
+    precision = args.precision
+    if precision == "auto":
+        precision = "fp32"
+    T, S, C, L = cfg["templates"].shape
+    n_corr = cfg["n_corr"]
+    out_shape = (T, n_corr) if cfg["network_sum"] else (T, n_corr, S, C)
+
+    g = {k: torch.from_numpy(np.ascontiguousarray(cfg[k])).to(dev)
+         for k in ("templates", "sst", "moveouts", "weights", "data")}
+    out = torch.empty(out_shape, dtype=torch.float32, device=dev)
+    stream = torch.cuda.current_stream()
+
+    def step():
+        return fmf.matched_filter_device(g["templates"], g["sst"], g["moveouts"], g["weights"],
+                                         g["data"], cfg["step"], out, cfg["normalize"],
+                                         cfg["network_sum"], precision, stream)
+
+    for _ in range(max(args.warmup, 0)):
+        step()
+    torch.cuda.synchronize()
+    barrier(world)
+    torch.cuda.synchronize()
+    launches = 0
+    with ClockSampler(local) as clocks:
+        lib.fmf_timing_begin()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            launches += step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        import ctypes as ct
+        prep_ms, kern_ms, ncalls = ct.c_double(), ct.c_double(), ct.c_int()
+        lib.fmf_timing_end(ct.byref(prep_ms), ct.byref(kern_ms), ct.byref(ncalls))
+    barrier(world)
+    torch.cuda.synchronize()
+    elapsed_ms = e0.elapsed_time(e1)
+    t_max = dist_max(elapsed_ms, world)
+    total_macs = cfg["macs"] * args.steps * world
+    value = total_macs / (t_max / 1e3) / 1e12
+    clock = clocks.summary()
+
+    # roofline of the correlation kernel
+    peaks, src = load_peaks()
+    kern_avg_ms = kern_ms.value / max(ncalls.value, 1)
+    algo_tflops = 2.0 * cfg["macs"] / (kern_avg_ms / 1e3) / 1e12
+    if precision == "fp32":
+        mhz = float(peaks.get("sm_max_mhz", 2070.0))
+        peak = N_SM * 128 * 2 * mhz * 1e6 / 1e12
+        roof = {"bound": "fp32_fma", "achieved": algo_tflops, "peak": peak, "unit": "TFLOP/s",
+                "frac": algo_tflops / peak, "traffic": None,
+                "kernel": "plain_kernel",
+                "peak_source": "nominal FP32 FMA: 152 SMs x 128 lanes x %.0f MHz (%s clock)"
+                               % (mhz, src)}
+    else:
+        peak = float(peaks["bf16_tflops"])
+        roof = {"bound": "tensor", "achieved": algo_tflops, "peak": peak, "unit": "TFLOP/s",
+                "frac": algo_tflops / peak, "traffic": None, "kernel": "tc_kernel",
+                "peak_source": "%s bf16_tflops" % src}
+    roof["kernel_ms_avg"] = kern_avg_ms
+    roof["prep_ms_avg"] = prep_ms.value / max(ncalls.value, 1)
+
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_max / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": {"fp32": "f32", "split_bf16": "bf16x3", "bf16": "bf16"}[precision],
+            "data": "synthetic",
+            "config": describe(cfg, {"precision": precision,
+                                     "parallelism": "template sets per rank" if world > 1
+                                     else "single GPU"}),
+            "roofline": roof, "gpu_launches": launches, "clocks": clock}
+
+    # end to end through the C ABI with pinned host buffers
+    del g
+    if not args.no_e2e:
+        line["e2e"] = run_e2e(cfg, out, precision, args, world, lib)
+    del out
+    torch.cuda.empty_cache()
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(cfg)
+    if rank == 0:
+        print(json.dumps(line))
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return 0
+
+
+def run_e2e(cfg, dev_out, precision, args, world, lib):
+    import torch
+    from fast_matched_filter_gb300 import _lib
+    pinned = {k: torch.from_numpy(np.ascontiguousarray(cfg[k])).pin_memory()
+              for k in ("templates", "sst", "moveouts", "weights", "data")}
+    host_out = torch.empty(tuple(dev_out.shape), dtype=torch.float32).pin_memory()
+    T, S, C, L = cfg["templates"].shape
+    N = cfg["data"].shape[-1]
+    prec = _lib.PRECISIONS[precision]
+
+    def call():
+        st = lib.fmf_matched_filter_ex(
+            pinned["templates"].data_ptr(), pinned["sst"].data_ptr(),
+            pinned["moveouts"].data_ptr(), pinned["data"].data_ptr(),
+            pinned["weights"].data_ptr(), cfg["step"], L, N, T, S, C, cfg["n_corr"],
+            host_out.data_ptr(), 1 if cfg["normalize"] == "full" else 0,
+            int(cfg["network_sum"]), prec, 0, None)
+        _lib.check(st, lib)
+
+    call()  # warm-up (pool growth)
+    barrier(world)
+    n = max(1, min(args.steps, 3))
+    t0 = time.perf_counter()
+    for _ in range(n):
+        call()
+    secs = dist_max(time.perf_counter() - t0, world)
+    h2d = sum(int(v.numel() * v.element_size()) for v in pinned.values())
+    d2h = int(host_out.numel() * 4)
+    return {"value": cfg["macs"] * n * world / secs / 1e12, "unit": UNIT,
+            "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "steps": n,
+            "api": "fmf_matched_filter_ex (C ABI, host pointers, pinned)"}
+
+
+def main(argv=None):
+    args = parse_args(argv)
+    if args.impl == "reference":
+        return run_reference_arm(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

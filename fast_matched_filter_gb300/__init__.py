@@ -1,0 +1,18 @@
+"""GB300-native matched filter with the interface of fast_matched_filter.
+
+    from fast_matched_filter_gb300 import matched_filter
+    cc_sums = matched_filter(templates, moveouts, weights, data, step, arch="gpu")
+
+The exported names mirror the reference package's
+(fast_matched_filter/__init__.py:11-16).
+"""
+from .fast_matched_filter import (  # noqa: F401
+    CPU_LOADED,
+    GPU_LOADED,
+    matched_filter,
+    matched_filter_device,
+    test_matched_filter,
+)
+from ._lib import FMFError  # noqa: F401
+
+__version__ = "0.1.0"

@@ -1,0 +1,456 @@
+// fmf_api.cu -- C ABI and host driver of the GB300 matched-filter library.
+//
+// Replaces the reference GPU host driver (matched_filter.cu:171-399): one
+// process drives its current device; inputs are copied (or used in place
+// when the caller passes device pointers), the per-call preprocessing kernels
+// run once, and one kernel launch covers every template and every output
+// index -- no lag chunks, no per-chunk memset/sync/copy round trips.
+// Errors are returned as FMF_* status codes with a message for
+// fmf_last_error(); nothing here terminates the process.
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <climits>
+
+#include "fmf_common.cuh"
+
+#define FMF_VERSION_STRING "fmf_gb300 0.1.0 sm_103a"
+
+namespace fmf {
+
+// ---------------------------------------------------------------- errors
+static thread_local int g_status = FMF_OK;
+static thread_local char g_msg[512] = "";
+static thread_local int g_launches = 0;
+
+int set_error(int status, const char *fmt, ...)
+{
+    g_status = status;
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_msg, sizeof(g_msg), fmt, ap);
+    va_end(ap);
+    return status;
+}
+
+static int clear_error()
+{
+    g_status = FMF_OK;
+    g_msg[0] = '\0';
+    return FMF_OK;
+}
+
+void count_launch(int n) { g_launches += n; }
+
+// ---------------------------------------------------------------- event timing
+// Opt-in (fmf_timing_begin/end): every call records CUDA events on its stream
+// around the preprocessing kernels and around the correlation kernel.
+struct TimedSpan {
+    cudaEvent_t a, b;
+    int kind;  // 0 preprocessing, 1 correlation kernel
+};
+static thread_local bool g_timing = false;
+static thread_local TimedSpan g_spans[4096];
+static thread_local int g_nspans = 0;
+
+static cudaEvent_t mark(cudaStream_t s)
+{
+    cudaEvent_t e = nullptr;
+    if (!g_timing)
+        return nullptr;
+    if (cudaEventCreate(&e) != cudaSuccess)
+        return nullptr;
+    cudaEventRecord(e, s);
+    return e;
+}
+
+static void span(cudaEvent_t a, cudaEvent_t b, int kind)
+{
+    if (!a || !b)
+        return;
+    if (g_nspans < 4096)
+        g_spans[g_nspans++] = TimedSpan{a, b, kind};
+    else {
+        cudaEventDestroy(a);
+        cudaEventDestroy(b);
+    }
+}
+
+int check_launch(const char *what)
+{
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess)
+        return set_error(FMF_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+    return FMF_OK;
+}
+
+static int cuda_status(cudaError_t e, const char *what)
+{
+    if (e == cudaSuccess)
+        return FMF_OK;
+    if (e == cudaErrorMemoryAllocation)
+        return set_error(FMF_ERR_OOM, "%s: %s", what, cudaGetErrorString(e));
+    return set_error(FMF_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+// ---------------------------------------------------------------- kernels
+__global__ void template_range_kernel(const int *, int, int, int, int, int, int, int *, int *);
+__global__ void template_center_kernel(const float *, int, float *, float *);
+__global__ void channel_mean_kernel(const float *, int, float *);
+__global__ void window_stats_kernel(const float *, int, int, int, const float *, float *,
+                                    float *, float *);
+int launch_plain(const Problem &P, cudaStream_t stream);
+
+// ---------------------------------------------------------------- memory
+// Stream-ordered scratch allocations (cudaMallocAsync from the device's
+// default pool).  The pool keeps freed blocks for reuse by later calls;
+// fmf_release_cache() trims it.
+struct Scratch {
+    cudaStream_t s;
+    void *ptr[16];
+    int n = 0;
+    explicit Scratch(cudaStream_t st) : s(st) {}
+    template <class T>
+    int get(T **out, size_t count, const char *what)
+    {
+        void *p = nullptr;
+        cudaError_t e = cudaMallocAsync(&p, count * sizeof(T) + 16, s);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            return set_error(e == cudaErrorMemoryAllocation ? FMF_ERR_OOM : FMF_ERR_CUDA,
+                             "allocating %zu bytes for %s: %s", count * sizeof(T), what,
+                             cudaGetErrorString(e));
+        }
+        ptr[n++] = p;
+        *out = static_cast<T *>(p);
+        return FMF_OK;
+    }
+    ~Scratch()
+    {
+        for (int i = 0; i < n; i++)
+            cudaFreeAsync(ptr[i], s);
+    }
+};
+
+static void keep_pool_cached()
+{
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess)
+        return;
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+        unsigned long long thr = ULLONG_MAX;
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+    }
+}
+
+// ---------------------------------------------------------------- validation
+struct Args {
+    const float *tpl, *sst, *data, *w;
+    const int *mo;
+    float *out;
+    size_t step, L, N, T, S, C, n_corr;
+    int normalize, sum_mode, precision, flags;
+};
+
+static int validate(const Args &a)
+{
+    if (!a.tpl || !a.sst || !a.mo || !a.data || !a.w || !a.out)
+        return set_error(FMF_ERR_ARG, "null array argument");
+    if (a.step < 1 || a.L < 1 || a.T < 1 || a.S < 1 || a.C < 1 || a.n_corr < 1)
+        return set_error(FMF_ERR_ARG,
+                         "sizes must be positive (step=%zu L=%zu T=%zu S=%zu C=%zu n_corr=%zu)",
+                         a.step, a.L, a.T, a.S, a.C, a.n_corr);
+    if (a.N < a.L)
+        return set_error(FMF_ERR_ARG, "data length %zu is shorter than the template length %zu", a.N,
+                         a.L);
+    if (a.N > (size_t)INT_MAX / 2 || a.n_corr > (size_t)INT_MAX || a.S * a.C > (size_t)INT_MAX ||
+        a.T > (size_t)INT_MAX || a.step > (size_t)INT_MAX / 2)
+        return set_error(FMF_ERR_ARG, "sizes exceed the 32-bit index range of this build");
+    if (a.n_corr > (a.N - a.L) / a.step + 1)
+        return set_error(FMF_ERR_ARG, "n_corr=%zu exceeds (N-L)/step+1=%zu", a.n_corr,
+                         (a.N - a.L) / a.step + 1);
+    if (a.normalize != 0 && a.normalize != 1)
+        return set_error(FMF_ERR_ARG, "normalize must be 0 (short) or 1 (full), got %d", a.normalize);
+    if (a.precision < FMF_PREC_FP32 || a.precision > FMF_PREC_BF16)
+        return set_error(FMF_ERR_ARG, "unknown precision %d", a.precision);
+    return FMF_OK;
+}
+
+constexpr int kStatBlock = 4096;
+
+// ---------------------------------------------------------------- core (device pointers)
+static int run_device(const Args &a, cudaStream_t s)
+{
+    int rc;
+    const int T = (int)a.T, SC = (int)(a.S * a.C), L = (int)a.L, N = (int)a.N;
+    const bool full = a.normalize == 1;
+    size_t stat_smem = (size_t)(kStatBlock + L + 1) * sizeof(double) * (full ? 2 : 1);
+    if (stat_smem > 227 * 1024)
+        return set_error(FMF_ERR_SMEM, "template length %d too long for the window-statistics kernel", L);
+
+    Scratch ws(s);
+    int *k_lo, *k_hi;
+    float *stat_e, *stat_m = nullptr, *mu = nullptr, *dcen = nullptr, *tcen = nullptr, *tsum = nullptr;
+    if ((rc = ws.get(&k_lo, 2 * (size_t)T, "template ranges")))
+        return rc;
+    k_hi = k_lo + T;
+    if ((rc = ws.get(&stat_e, (size_t)SC * N, "window energies")))
+        return rc;
+    if (full) {
+        if ((rc = ws.get(&stat_m, (size_t)SC * N, "window means")) ||
+            (rc = ws.get(&mu, (size_t)SC, "channel means")) ||
+            (rc = ws.get(&dcen, (size_t)SC * N, "centred data")) ||
+            (rc = ws.get(&tcen, (size_t)T * SC * L, "centred templates")) ||
+            (rc = ws.get(&tsum, (size_t)T * SC, "template sums")))
+            return rc;
+    }
+
+    cudaEvent_t ev_prep0 = mark(s);
+    template_range_kernel<<<(T + 127) / 128, 128, 0, s>>>(a.mo, T, SC, L, N, (int)a.step,
+                                                            (int)a.n_corr, k_lo, k_hi);
+    count_launch();
+    if (full) {
+        template_center_kernel<<<(unsigned)((size_t)T * SC), 128, 0, s>>>(a.tpl, L, tcen, tsum);
+        channel_mean_kernel<<<SC, 256, 0, s>>>(a.data, N, mu);
+        count_launch(2);
+    }
+    cudaFuncSetAttribute(window_stats_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         227 * 1024);
+    dim3 sgrid((N + kStatBlock - 1) / kStatBlock, SC);
+    window_stats_kernel<<<sgrid, 256, stat_smem, s>>>(a.data, N, L, kStatBlock, mu, dcen, stat_e,
+                                                      stat_m);
+    count_launch();
+    if ((rc = check_launch("preprocessing kernels")))
+        return rc;
+    cudaEvent_t ev_prep1 = mark(s);
+    span(ev_prep0, ev_prep1, 0);
+
+    Problem P;
+    P.tpl = full ? tcen : a.tpl;
+    P.sst = a.sst;
+    P.tsum = tsum;
+    P.mo = a.mo;
+    P.w = a.w;
+    P.data = full ? dcen : a.data;
+    P.stat_e = stat_e;
+    P.stat_m = stat_m;
+    P.k_lo = k_lo;
+    P.k_hi = k_hi;
+    P.out = a.out;
+    P.T = T;
+    P.SC = SC;
+    P.L = L;
+    P.N = N;
+    P.step = (int)a.step;
+    P.n_corr = (int)a.n_corr;
+    P.normalize = a.normalize;
+    P.network_sum = a.sum_mode != 0;
+
+    if (!P.network_sum) {
+        size_t bytes = (size_t)T * a.n_corr * SC * sizeof(float);
+        if ((rc = cuda_status(cudaMemsetAsync(a.out, 0, bytes, s), "clearing the output")))
+            return rc;
+    }
+    if (a.precision != FMF_PREC_FP32)
+        return set_error(FMF_ERR_UNSUPPORTED, "tensor-core precision not built yet");
+    // grid.y carries the template index: launch in slices of 65535 templates
+    cudaEvent_t ev_main0 = mark(s);
+    for (int t0 = 0; t0 < T; t0 += 65535) {
+        Problem Q = P;
+        int nt = T - t0 < 65535 ? T - t0 : 65535;
+        size_t o = (size_t)t0 * SC;
+        Q.tpl += o * L;
+        Q.sst += o;
+        if (Q.tsum)
+            Q.tsum += o;
+        Q.mo += o;
+        Q.w += o;
+        Q.k_lo += t0;
+        Q.k_hi += t0;
+        Q.out += (size_t)t0 * a.n_corr * (P.network_sum ? 1 : SC);
+        Q.T = nt;
+        if ((rc = launch_plain(Q, s)))
+            return rc;
+    }
+    span(ev_main0, mark(s), 1);
+    return FMF_OK;
+}
+
+// ---------------------------------------------------------------- host-pointer path
+static int run_host(const Args &a, cudaStream_t s)
+{
+    int rc;
+    const size_t SC = a.S * a.C;
+    const size_t n_tsc = a.T * SC;
+    const size_t out_n = a.T * a.n_corr * (a.sum_mode ? 1 : SC);
+    const size_t n[6] = {n_tsc * a.L, n_tsc, n_tsc, SC * a.N, n_tsc, out_n};
+    float *buf[6];
+    {
+        Scratch io(s);  // device copies of the arguments, freed in stream order
+        for (int i = 0; i < 6; i++)
+            if ((rc = io.get(&buf[i], n[i], "input/output copies")))
+                return rc;
+        const void *src[5] = {a.tpl, a.sst, a.mo, a.data, a.w};
+        for (int i = 0; i < 5; i++)
+            if ((rc = cuda_status(cudaMemcpyAsync(buf[i], src[i], n[i] * 4, cudaMemcpyHostToDevice, s),
+                                  "copying inputs to the device")))
+                return rc;
+        Args d = a;
+        d.tpl = buf[0];
+        d.sst = buf[1];
+        d.mo = reinterpret_cast<const int *>(buf[2]);
+        d.data = buf[3];
+        d.w = buf[4];
+        d.out = buf[5];
+        if ((rc = run_device(d, s)))
+            return rc;
+        if ((rc = cuda_status(cudaMemcpyAsync(a.out, d.out, n[5] * 4, cudaMemcpyDeviceToHost, s),
+                              "copying the result to the host")))
+            return rc;
+    }
+    return cuda_status(cudaStreamSynchronize(s), "matched filter");
+}
+
+static int entry(const Args &a, void *stream)
+{
+    clear_error();
+    g_launches = 0;
+    int rc = validate(a);
+    if (rc)
+        return rc;
+    keep_pool_cached();
+    cudaStream_t s = (cudaStream_t)stream;
+    if (a.flags & FMF_FLAG_DEVICE_POINTERS)
+        return run_device(a, s);
+    return run_host(a, s);
+}
+
+}  // namespace fmf
+
+// ---------------------------------------------------------------- C ABI
+extern "C" {
+
+int fmf_matched_filter_ex(const float *templates, const float *sum_square_templates,
+                          const int *moveouts, const float *data, const float *weights,
+                          size_t step, size_t n_samples_template, size_t n_samples_data,
+                          size_t n_templates, size_t n_stations, size_t n_components,
+                          size_t n_corr, float *cc_out, int normalize, int sum_cc_mode,
+                          int precision, int flags, void *stream)
+{
+    fmf::Args a;
+    a.tpl = templates;
+    a.sst = sum_square_templates;
+    a.mo = moveouts;
+    a.data = data;
+    a.w = weights;
+    a.out = cc_out;
+    a.step = step;
+    a.L = n_samples_template;
+    a.N = n_samples_data;
+    a.T = n_templates;
+    a.S = n_stations;
+    a.C = n_components;
+    a.n_corr = n_corr;
+    a.normalize = normalize;
+    a.sum_mode = sum_cc_mode;
+    a.precision = precision;
+    a.flags = flags;
+    return fmf::entry(a, stream);
+}
+
+int fmf_matched_filter(const float *templates, const float *sum_square_templates,
+                       const int *moveouts, const float *data, const float *weights,
+                       size_t step, size_t n_samples_template, size_t n_samples_data,
+                       size_t n_templates, size_t n_stations, size_t n_components,
+                       size_t n_corr, float *cc_out, int normalize, int sum_cc_mode)
+{
+    return fmf_matched_filter_ex(templates, sum_square_templates, moveouts, data, weights, step,
+                                 n_samples_template, n_samples_data, n_templates, n_stations,
+                                 n_components, n_corr, cc_out, normalize, sum_cc_mode,
+                                 FMF_PREC_FP32, 0, nullptr);
+}
+
+int matched_filter(const float *templates, const float *sum_square_templates, const int *moveouts,
+                   const float *data, const float *weights, size_t step, size_t n_samples_template,
+                   size_t n_samples_data, size_t n_templates, size_t n_stations,
+                   size_t n_components, size_t n_corr, float *cc_out, int normalize,
+                   int sum_cc_mode)
+{
+    int rc = fmf_matched_filter(templates, sum_square_templates, moveouts, data, weights, step,
+                                n_samples_template, n_samples_data, n_templates, n_stations,
+                                n_components, n_corr, cc_out, normalize, sum_cc_mode);
+    if (rc != FMF_OK)
+        fprintf(stderr, "fmf_gb300 matched_filter failed (status %d): %s\n", rc, fmf::g_msg);
+    return rc;
+}
+
+int fmf_last_error(char *buf, size_t len)
+{
+    if (buf && len) {
+        strncpy(buf, fmf::g_msg, len - 1);
+        buf[len - 1] = '\0';
+    }
+    return fmf::g_status;
+}
+
+const char *fmf_version(void) { return FMF_VERSION_STRING; }
+
+int fmf_last_launch_count(void) { return fmf::g_launches; }
+
+int fmf_timing_begin(void)
+{
+    for (int i = 0; i < fmf::g_nspans; i++) {
+        cudaEventDestroy(fmf::g_spans[i].a);
+        cudaEventDestroy(fmf::g_spans[i].b);
+    }
+    fmf::g_nspans = 0;
+    fmf::g_timing = true;
+    return FMF_OK;
+}
+
+int fmf_timing_end(double *prep_ms, double *kernel_ms, int *n_calls)
+{
+    double acc[2] = {0.0, 0.0};
+    int calls = 0, rc = FMF_OK;
+    for (int i = 0; i < fmf::g_nspans; i++) {
+        fmf::TimedSpan &sp = fmf::g_spans[i];
+        float ms = 0.0f;
+        cudaError_t e = cudaEventSynchronize(sp.b);
+        if (e == cudaSuccess)
+            e = cudaEventElapsedTime(&ms, sp.a, sp.b);
+        if (e != cudaSuccess)
+            rc = fmf::cuda_status(e, "fmf_timing_end");
+        acc[sp.kind] += ms;
+        calls += sp.kind == 1;
+        cudaEventDestroy(sp.a);
+        if (i + 1 >= fmf::g_nspans || fmf::g_spans[i + 1].a != sp.b)
+            cudaEventDestroy(sp.b);
+    }
+    fmf::g_nspans = 0;
+    fmf::g_timing = false;
+    if (prep_ms)
+        *prep_ms = acc[0];
+    if (kernel_ms)
+        *kernel_ms = acc[1];
+    if (n_calls)
+        *n_calls = calls;
+    return rc;
+}
+
+int fmf_release_cache(void)
+{
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess)
+        return fmf::cuda_status(e, "fmf_release_cache");
+    cudaMemPool_t pool;
+    e = cudaDeviceGetDefaultMemPool(&pool, dev);
+    if (e == cudaSuccess)
+        e = cudaDeviceSynchronize();
+    if (e == cudaSuccess)
+        e = cudaMemPoolTrimTo(pool, 0);
+    return fmf::cuda_status(e, "fmf_release_cache");
+}
+
+}  // extern "C"

@@ -1,0 +1,49 @@
+// fmf_common.cuh -- shared definitions of the GB300 matched-filter library.
+//
+// Terminology follows the reference (fast_matched_filter): a *template* t has
+// one waveform per *channel* ch = station * C + component; the *moveout*
+// mo[t][ch] shifts that channel's waveform in the continuous *data*; output
+// index k ("lag") correlates template t against data samples
+// k*step + mo[t][ch] + [0, L) of every channel.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdint.h>
+
+#include "../../include/fmf_gb300.h"
+
+namespace fmf {
+
+// Stability threshold of the reference (matched_filter.cu:22, matched_filter.c:17):
+// a channel contributes only when sst * (window energy) exceeds it.
+constexpr float kThreshold = 0.000001f;
+
+// Device view of one matched-filter problem.  Channel-major arrays are
+// indexed [t][ch] (T x SC) or [ch][sample] (SC x N).
+struct Problem {
+    const float *tpl;     // (T, SC, L) templates; centred per channel for "full"
+    const float *sst;     // (T, SC) caller-supplied sum of squares (raw templates)
+    const float *tsum;    // (T, SC) sum of the centred template ("full"), else null
+    const int *mo;        // (T, SC) moveouts
+    const float *w;       // (T, SC) weights
+    const float *data;    // (SC, N) data; centred per channel for "full"
+    const float *stat_e;  // (SC, N) window energy (short) / centred ssd (full), window starts at the index
+    const float *stat_m;  // (SC, N) centred window mean ("full"), else null
+    const int *k_lo;      // (T) first valid output index
+    const int *k_hi;      // (T) one past the last valid output index (<= n_corr)
+    float *out;           // (T, n_corr) or (T, n_corr, SC)
+    int T, SC, L, N, step, n_corr;
+    int normalize;        // 0 short, 1 full
+    int network_sum;      // 1 weighted sum over channels, 0 per channel
+};
+
+}  // namespace fmf
+
+// ---------------------------------------------------------------------------
+// Host-side helpers shared by the translation units (defined in fmf_api.cu).
+namespace fmf {
+int set_error(int status, const char *fmt, ...);
+void count_launch(int n = 1);
+int check_launch(const char *what);
+}  // namespace fmf

@@ -1,0 +1,229 @@
+// fmf_plain.cu -- plain FP32 CUDA-core matched filter (drop-in form).
+//
+// Replaces the reference kernels network_corr + sum_cc
+// (matched_filter.cu:42-168) and the per-lag loop of the CPU library
+// (matched_filter.c:78-92, 416-455, 611-657).
+//
+// One CTA = one template x one tile of 4096 consecutive output indices; it
+// walks the template's channels in station-major / component-minor order,
+// skipping channels of weight 0, and keeps the weighted network sum of its
+// 4096 outputs on chip for the whole walk.  Each thread owns 16 consecutive
+// outputs.
+//
+// step > 1 is handled polyphase: taps j = step*q + phi see the data stream
+// d[step*(k + q) + mo + phi], so every phase phi is a unit-step correlation of
+// ceil((L - phi)/step) taps against a decimated data window.  Per (channel,
+// phase) one *stage* is staged in shared memory with cp.async (zero-filled
+// outside [0, N)): the decimated data window (4096 + taps samples, stored with
+// 4 padding floats every 32 so that the 16-byte loads of consecutive threads,
+// 64 bytes apart, fall into distinct banks) and the phase's template taps.
+// Two stage buffers are in flight.
+//
+// Inner loop: a 20-register sliding window of data per thread; per 4 taps one
+// 16-byte data load, one 16-byte broadcast template load and 64 FMAs.
+//
+// Epilogue per channel (fused): numerator of "full" minus m*sum(t'),
+// den = sst * E (E and m from the FP64 window statistics), threshold 1e-6 on
+// den, cc = num / sqrt(den), network sum acc = fma(cc, w, acc) in channel
+// order (the reference's accumulation, matched_filter.c:450).  Outputs
+// outside [k_lo, k_hi) are written as 0.
+#include "fmf_common.cuh"
+
+namespace fmf {
+
+constexpr int PL_THREADS = 256;
+constexpr int PL_R = 16;                       // outputs per thread
+constexpr int PL_TILE = PL_THREADS * PL_R;     // outputs per CTA
+constexpr int PL_U = 20;                       // taps per unrolled iteration
+
+__host__ __device__ __forceinline__ int padx(int x) { return x + ((x >> 5) << 2); }
+
+struct PlainGeom {
+    int lq_pad;       // taps per phase, padded to a multiple of PL_U
+    int dw;           // data window length (logical floats)
+    int data_floats;  // padded data floats
+    int stage_floats; // data + template floats, multiple of 4
+    size_t smem;      // dynamic shared memory bytes
+};
+
+inline PlainGeom plain_geom(int L, int step)
+{
+    PlainGeom g;
+    int lq = (L + step - 1) / step;
+    g.lq_pad = (lq + PL_U - 1) / PL_U * PL_U;
+    g.dw = PL_TILE + g.lq_pad;
+    g.data_floats = padx(g.dw) + 4;
+    g.stage_floats = (g.data_floats + g.lq_pad + 3) & ~3;
+    g.smem = (size_t)(2 * g.stage_floats + PL_R * PL_THREADS) * sizeof(float);
+    return g;
+}
+
+__device__ __forceinline__ void cp_async4(float *smem, const float *gmem, bool valid)
+{
+    unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    int n = valid ? 4 : 0;
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(s), "l"(gmem), "r"(n)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
+
+__device__ __forceinline__ int next_active(const float *w, int ch, int SC)
+{
+    while (ch < SC && w[ch] == 0.0f)
+        ch++;
+    return ch;
+}
+
+__device__ __forceinline__ void load_stage(float *buf, const Problem &P, const PlainGeom &g,
+                                           int t, int ch, int phi, long long k0, int mo)
+{
+    const float *dch = P.data + (size_t)ch * P.N;
+    const long long base = (long long)P.step * k0 + mo + phi;
+    for (int x = threadIdx.x; x < g.dw; x += PL_THREADS) {
+        long long src = base + (long long)P.step * x;
+        bool ok = src >= 0 && src < P.N;
+        cp_async4(buf + padx(x), ok ? dch + src : dch, ok);
+    }
+    float *tb = buf + g.data_floats;
+    const float *tc = P.tpl + ((size_t)t * P.SC + ch) * P.L;
+    for (int q = threadIdx.x; q < g.lq_pad; q += PL_THREADS) {
+        int j = P.step * q + phi;
+        bool ok = j < P.L;
+        cp_async4(tb + q, ok ? tc + j : tc, ok);
+    }
+}
+
+__device__ __forceinline__ void compute_phase(const float *buf, const PlainGeom &g, float acc[PL_R])
+{
+    const float *tb = buf + g.data_floats;
+    const int x0 = threadIdx.x * PL_R;
+    float win[PL_U];
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        float4 v = *reinterpret_cast<const float4 *>(buf + padx(x0 + 4 * i));
+        win[4 * i + 0] = v.x;
+        win[4 * i + 1] = v.y;
+        win[4 * i + 2] = v.z;
+        win[4 * i + 3] = v.w;
+    }
+    for (int q = 0; q < g.lq_pad; q += PL_U) {
+#pragma unroll
+        for (int s = 0; s < 5; s++) {
+            float4 v = *reinterpret_cast<const float4 *>(buf + padx(x0 + q + 16 + 4 * s));
+            win[(16 + 4 * s + 0) % PL_U] = v.x;
+            win[(16 + 4 * s + 1) % PL_U] = v.y;
+            win[(16 + 4 * s + 2) % PL_U] = v.z;
+            win[(16 + 4 * s + 3) % PL_U] = v.w;
+            float4 tv4 = *reinterpret_cast<const float4 *>(tb + q + 4 * s);
+            float tv[4] = {tv4.x, tv4.y, tv4.z, tv4.w};
+#pragma unroll
+            for (int jj = 0; jj < 4; jj++)
+#pragma unroll
+                for (int r = 0; r < PL_R; r++)
+                    acc[r] = fmaf(tv[jj], win[(4 * s + r + jj) % PL_U], acc[r]);
+        }
+    }
+}
+
+__global__ void __launch_bounds__(PL_THREADS, 2)
+plain_kernel(const Problem P, const PlainGeom g)
+{
+    extern __shared__ __align__(16) float smem[];
+    float *net = smem + 2 * g.stage_floats;  // [PL_R][PL_THREADS]
+
+    const int t = blockIdx.y;
+    const long long k0 = (long long)blockIdx.x * PL_TILE;
+    const int klo = P.k_lo[t], khi = P.k_hi[t];
+    const int tid = threadIdx.x;
+    const float *w = P.w + (size_t)t * P.SC;
+    const int *mo = P.mo + (size_t)t * P.SC;
+
+#pragma unroll
+    for (int r = 0; r < PL_R; r++)
+        net[r * PL_THREADS + tid] = 0.0f;
+
+    const bool busy = k0 < khi && k0 + PL_TILE > klo;
+    if (busy) {
+        float acc[PL_R];
+#pragma unroll
+        for (int r = 0; r < PL_R; r++)
+            acc[r] = 0.0f;
+        int ch = next_active(w, 0, P.SC), phi = 0, b = 0;
+        if (ch < P.SC)
+            load_stage(smem, P, g, t, ch, 0, k0, mo[ch]);
+        cp_async_commit();
+        while (ch < P.SC) {
+            int nch = ch, nphi = phi + 1;
+            if (nphi == P.step) {
+                nphi = 0;
+                nch = next_active(w, ch + 1, P.SC);
+            }
+            if (nch < P.SC)
+                load_stage(smem + (b ^ 1) * g.stage_floats, P, g, t, nch, nphi, k0, mo[nch]);
+            cp_async_commit();
+            cp_async_wait1();
+            __syncthreads();
+            compute_phase(smem + b * g.stage_floats, g, acc);
+            if (phi == P.step - 1) {
+                // fused epilogue of channel ch
+                const size_t row = (size_t)t * P.SC + ch;
+                const float sst = P.sst[row], wc = w[ch];
+                const float ts = P.normalize ? P.tsum[row] : 0.0f;
+                const float *se = P.stat_e + (size_t)ch * P.N;
+                const float *sm = P.normalize ? P.stat_m + (size_t)ch * P.N : nullptr;
+#pragma unroll
+                for (int r = 0; r < PL_R; r++) {
+                    long long k = k0 + tid * PL_R + r;
+                    if (k >= klo && k < khi) {
+                        long long u = k * P.step + mo[ch];
+                        float num = acc[r];
+                        if (P.normalize)
+                            num = fmaf(-sm[u], ts, num);
+                        float den = sst * se[u];
+                        float cc = den > kThreshold ? num / sqrtf(den) : 0.0f;
+                        if (P.network_sum)
+                            net[r * PL_THREADS + tid] = fmaf(cc, wc, net[r * PL_THREADS + tid]);
+                        else
+                            P.out[((size_t)t * P.n_corr + k) * P.SC + ch] = cc;
+                    }
+                    acc[r] = 0.0f;
+                }
+            }
+            __syncthreads();
+            b ^= 1;
+            ch = nch;
+            phi = nphi;
+        }
+    }
+    if (P.network_sum) {
+        float *o = P.out + (size_t)t * P.n_corr;
+#pragma unroll
+        for (int r = 0; r < PL_R; r++) {
+            long long k = k0 + tid * PL_R + r;
+            if (k < P.n_corr)
+                o[k] = net[r * PL_THREADS + tid];
+        }
+    }
+}
+
+// Host launcher.  Returns FMF status.
+int launch_plain(const Problem &P, cudaStream_t stream)
+{
+    PlainGeom g = plain_geom(P.L, P.step);
+    if (g.smem > 227 * 1024)
+        return set_error(FMF_ERR_SMEM,
+                         "template length %d with step %d needs %zu bytes of shared memory (max 232448)",
+                         P.L, P.step, g.smem);
+    static bool attr_done = false;  // per process; attribute is per function
+    if (!attr_done) {
+        cudaFuncSetAttribute(plain_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+        attr_done = true;
+    }
+    dim3 grid((unsigned)((P.n_corr + PL_TILE - 1) / PL_TILE), (unsigned)P.T);
+    plain_kernel<<<grid, PL_THREADS, g.smem, stream>>>(P, g);
+    count_launch();
+    return check_launch("plain_kernel");
+}
+
+}  // namespace fmf

@@ -1,0 +1,197 @@
+// fmf_prep.cu -- per-call preprocessing kernels.
+//
+//  * template_range_kernel : valid output range [k_lo, k_hi) of each template
+//    (reference: matched_filter.c:53-76 start/stop, matched_filter.cu:302-308
+//    n_corr_t).
+//  * template_center_kernel: "full" only -- template minus its FP64 mean and
+//    the FP64 sum of the centred values.  sum(t*(d-m)) equals
+//    sum((t-tbar)*(d-m)) exactly, so centring changes no result; it removes
+//    the template's DC term from the products the numerator sums.
+//  * channel_mean_kernel   : "full" only -- FP64 mean of each data channel,
+//    rounded to float; d - mu is exact in FP32 wherever mu/2 <= d <= 2 mu.
+//  * window_stats_kernel   : FP64 sliding-window statistics of every channel
+//    for windows of L samples starting at each sample index:
+//      short: E = sum d^2                      (matched_filter.c:622)
+//      full : m = sum d'/L, V = sum d'^2 - (sum d')^2/L   (d' = d - mu)
+//    computed from an FP64 prefix sum local to each block of windows, so the
+//    differenced values are of the size of the block's energy, not of the
+//    whole trace's.
+#include "fmf_common.cuh"
+
+namespace fmf {
+
+__global__ void template_range_kernel(const int *__restrict__ mo, int T, int SC,
+                                      int L, int N, int step, int n_corr,
+                                      int *__restrict__ k_lo, int *__restrict__ k_hi)
+{
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= T)
+        return;
+    int lo = 0, hi = 0;
+    const int *m = mo + (size_t)t * SC;
+    for (int ch = 0; ch < SC; ch++) {
+        lo = min(lo, m[ch]);
+        hi = max(hi, m[ch]);
+    }
+    long long first = lo < 0 ? ((long long)(-lo) + step - 1) / step : 0;
+    long long last = (long long)N - L - hi;
+    long long a = 0, b = 0;
+    if (last >= 0) {
+        b = last / step + 1;
+        if (b > n_corr)
+            b = n_corr;
+        a = first < b ? first : b;
+    }
+    k_lo[t] = (int)a;
+    k_hi[t] = (int)b;
+}
+
+__device__ __forceinline__ double block_sum_f64(double v, double *red)
+{
+    for (int o = 16; o > 0; o >>= 1)
+        v += __shfl_down_sync(0xffffffffu, v, o);
+    int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0)
+        red[wid] = v;
+    __syncthreads();
+    double s = 0.0;
+    if (threadIdx.x == 0) {
+        for (int i = 0; i < (int)(blockDim.x >> 5); i++)
+            s += red[i];
+        red[32] = s;
+    }
+    __syncthreads();
+    return red[32];
+}
+
+// grid = T*SC blocks of 128 threads
+__global__ void template_center_kernel(const float *__restrict__ tpl, int L,
+                                       float *__restrict__ tcen,
+                                       float *__restrict__ tsum)
+{
+    __shared__ double red[33];
+    size_t row = blockIdx.x;
+    const float *src = tpl + row * L;
+    float *dst = tcen + row * L;
+    double s = 0.0;
+    for (int j = threadIdx.x; j < L; j += blockDim.x)
+        s += (double)src[j];
+    double mean = block_sum_f64(s, red) / (double)L;
+    float mf = (float)mean;
+    double s2 = 0.0;
+    for (int j = threadIdx.x; j < L; j += blockDim.x) {
+        float v = src[j] - mf;
+        dst[j] = v;
+        s2 += (double)v;
+    }
+    double tot = block_sum_f64(s2, red);
+    if (threadIdx.x == 0)
+        tsum[row] = (float)tot;
+}
+
+// grid = SC blocks of 256 threads
+__global__ void channel_mean_kernel(const float *__restrict__ data, int N,
+                                    float *__restrict__ mu)
+{
+    __shared__ double red[33];
+    const float *src = data + (size_t)blockIdx.x * N;
+    double s = 0.0;
+    for (int i = threadIdx.x; i < N; i += blockDim.x)
+        s += (double)src[i];
+    double tot = block_sum_f64(s, red);
+    if (threadIdx.x == 0)
+        mu[blockIdx.x] = (float)(tot / (double)N);
+}
+
+// Inclusive block scan of a[1..len] (a[0] = 0) held in shared memory.
+// Each thread scans a contiguous segment serially; segment totals are
+// combined with a warp-level exclusive scan.
+__device__ void block_scan_f64(double *a, int len, double *part)
+{
+    const int nt = blockDim.x;
+    const int seg = (len + nt - 1) / nt;
+    const int b = 1 + threadIdx.x * seg;
+    const int e = min(len + 1, b + seg);
+    double s = 0.0;
+    for (int i = b; i < e; i++) {
+        s += a[i];
+        a[i] = s;
+    }
+    // exclusive scan of per-thread totals
+    int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    double x = s;
+    for (int o = 1; o < 32; o <<= 1) {
+        double y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o)
+            x += y;
+    }
+    if (lane == 31)
+        part[wid] = x;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double run = 0.0;
+        for (int i = 0; i < (nt >> 5); i++) {
+            double v = part[i];
+            part[i] = run;
+            run += v;
+        }
+    }
+    __syncthreads();
+    double off = part[wid] + (x - s);
+    for (int i = b; i < e; i++)
+        a[i] += off;
+    __syncthreads();
+}
+
+// grid = (ceil(N / B), SC), block 256, dynamic smem = (B + L + 1) * 8 * (full ? 2 : 1)
+__global__ void window_stats_kernel(const float *__restrict__ data, int N, int L,
+                                    int B, const float *__restrict__ mu,
+                                    float *__restrict__ dcen,
+                                    float *__restrict__ stat_e,
+                                    float *__restrict__ stat_m)
+{
+    extern __shared__ double sh[];
+    __shared__ double part[33];
+    const int ch = blockIdx.y;
+    const long long c0 = (long long)blockIdx.x * B;
+    const int len = (int)min((long long)B + L, (long long)N - c0);
+    const bool full = mu != nullptr;
+    double *P2 = sh;
+    double *P1 = sh + (B + L + 1);
+    const float *src = data + (size_t)ch * N + c0;
+    const float m = full ? mu[ch] : 0.0f;
+    for (int i = threadIdx.x; i < len; i += blockDim.x) {
+        float v = src[i] - m;
+        if (full && i < B)
+            dcen[(size_t)ch * N + c0 + i] = v;
+        P2[i + 1] = (double)v * (double)v;
+        if (full)
+            P1[i + 1] = (double)v;
+    }
+    if (threadIdx.x == 0) {
+        P2[0] = 0.0;
+        if (full)
+            P1[0] = 0.0;
+    }
+    __syncthreads();
+    block_scan_f64(P2, len, part);
+    if (full)
+        block_scan_f64(P1, len, part);
+    const int nwin = min(B, len - L + 1);
+    const double invL = 1.0 / (double)L;
+    for (int u = threadIdx.x; u < nwin; u += blockDim.x) {
+        double e2 = P2[u + L] - P2[u];
+        size_t o = (size_t)ch * N + c0 + u;
+        if (full) {
+            double e1 = P1[u + L] - P1[u];
+            double v = e2 - e1 * e1 * invL;
+            stat_e[o] = (float)(v > 0.0 ? v : 0.0);
+            stat_m[o] = (float)(e1 * invL);
+        } else {
+            stat_e[o] = (float)e2;
+        }
+    }
+}
+
+}  // namespace fmf

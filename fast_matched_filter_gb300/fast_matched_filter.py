@@ -1,0 +1,280 @@
+"""Python interface of the GB300 matched filter.
+
+``matched_filter`` keeps the reference call
+(fast_matched_filter/fast_matched_filter.py:66-362): same arguments, same
+input formats (4-D templates, single template, "traces"), the same moveout /
+weight broadcasting, n_corr, template energies, output layout and
+``check_zeros`` report.  ``arch='gpu'`` runs this package's CUDA library; the
+reference's CPU architectures are not part of this package, which reports
+them as not loaded exactly as the reference wrapper does when its CPU
+library is missing (fast_matched_filter.py:164-177).
+
+One keyword is added: ``precision`` -- 'fp32' (plain FP32 CUDA-core form,
+the default and the drop-in), 'split_bf16' (tensor cores, bf16 hi+lo with
+three products) or 'bf16' (single bf16 product).
+
+``matched_filter_device`` runs the same computation on arrays already
+resident on the GPU (torch CUDA tensors), asynchronously on a stream.
+"""
+import ctypes as ct
+
+import numpy as np
+
+from . import _lib
+
+CPU_LOADED = False
+_LIB, _LIB_ERROR = _lib.try_load()
+GPU_LOADED = _LIB is not None
+
+
+def _require_lib():
+    if _LIB is None:
+        raise RuntimeError(
+            "fast_matched_filter_gb300: libfmf_gb300.so is not loadable (%s); "
+            "build it with `python -m fast_matched_filter_gb300.build`" % _LIB_ERROR)
+    return _LIB
+
+
+def _broadcast(arr, T, S, C, what):
+    """(T,S,C) broadcast rule of fast_matched_filter.py:235-251."""
+    arr = np.asarray(arr)
+    if arr.shape == (T, S, C):
+        return arr
+    ratio = (T * S * C) / arr.size
+    if ratio == C:
+        return np.repeat(arr, C).reshape(T, S, C)
+    if ratio == 1.0:
+        return arr.reshape(T, S, C)
+    raise ValueError("%s of shape %s cannot be broadcast to (%d, %d, %d)"
+                     % (what, arr.shape, T, S, C))
+
+
+def _infer_dims(templates, data):
+    """Input-format inference of fast_matched_filter.py:179-214.
+    Returns (T, S, C) or None for incompatible dimensions."""
+    if templates.ndim > data.ndim:
+        T = int(templates.shape[0])
+        assert templates.shape[1] == data.shape[0]
+        S = int(templates.shape[1])
+        if templates.ndim == 4:
+            assert templates.shape[2] == data.shape[1]
+            return T, S, int(templates.shape[2])
+        if templates.ndim == 3:
+            return T, S, 1
+        return None
+    if templates.ndim == data.ndim:
+        assert templates.shape[0] == data.shape[0]
+        S = int(templates.shape[0])
+        if templates.ndim == 3:
+            assert templates.shape[1] == data.shape[1]
+            return 1, S, int(templates.shape[1])
+        if templates.ndim == 2:
+            return 1, S, 1
+        return None
+    return None
+
+
+def _zero_report(cc, moveouts_flat, weights_flat, n_templates, n_corr, step,
+                 network_sum, check_zeros):
+    """The check_zeros diagnostic of fast_matched_filter.py:322-361, including
+    its slicing of the last axis in the per-channel layout."""
+    if (check_zeros is not False) and (check_zeros != "first") and (check_zeros != "all"):
+        print("check_zeros should be False, 'first', or 'all'. Set it to "
+              "the default value: 'first'")
+        check_zeros = "first"
+    if not check_zeros:
+        return None
+    stop = int(n_corr - moveouts_flat.max() / step)
+    if check_zeros == "first":
+        if network_sum:
+            zeros = np.sum(cc[0:1, :stop] == 0.0, axis=-1)
+        else:
+            zeros = np.sum(cc[0:1, :, :, :stop] == 0.0, axis=(1, 2, 3))
+    else:
+        zeros = np.sum(cc[..., :stop].reshape(n_templates, -1) == 0.0, axis=-1)
+    threshold = 10
+    if not network_sum:
+        threshold *= np.sum(weights_flat[0, ...] > 0.0)
+    for t in range(zeros.shape[0]):
+        if zeros[t] > threshold:
+            print("{} correlation computations were skipped on the {:d}-th "
+                  "template. Can be caused by zeros in data, or too low "
+                  "amplitudes (try to increase the gain).".format(zeros[t], t))
+    return zeros
+
+
+def prepare(templates, moveouts, weights, data, step, normalize="short"):
+    """Shape handling of the reference wrapper: returns the flat float32/int32
+    buffers and sizes (fast_matched_filter.py:179-268), or None for
+    incompatible dimensions."""
+    dims = _infer_dims(templates, data)
+    if dims is None:
+        return None
+    T, S, C = dims
+    L = templates.shape[-1]
+    if templates.shape != (T, S, C, L):
+        templates = templates.reshape(T, S, C, L)
+    N = data.shape[-1]
+    if data.shape != (S, C, N):
+        data = data.reshape(S, C, N)
+    assert np.asarray(moveouts).shape == np.asarray(weights).shape
+    moveouts = _broadcast(moveouts, T, S, C, "moveouts")
+    weights = _broadcast(weights, T, S, C, "weights")
+    step = int(step)
+    if step < 1:
+        raise ValueError("step must be a positive integer, got %d" % step)
+    if N < L:
+        raise ValueError("data (%d samples) shorter than the templates (%d)" % (N, L))
+    n_corr = int((N - L) / step + 1)
+    sst = np.sum(templates ** 2, axis=-1)
+    return dict(
+        templates=np.ascontiguousarray(templates.flatten(), dtype=np.float32),
+        sst=np.ascontiguousarray(sst.flatten(), dtype=np.float32),
+        moveouts=np.ascontiguousarray(moveouts.flatten(), dtype=np.int32),
+        weights=np.ascontiguousarray(weights.flatten(), dtype=np.float32),
+        data=np.ascontiguousarray(data.flatten(), dtype=np.float32),
+        T=T, S=S, C=C, L=int(L), N=int(N), step=step, n_corr=n_corr,
+        normalize=1 if normalize == "full" else 0)
+
+
+def _ptr(a, typ):
+    return a.ctypes.data_as(ct.POINTER(typ))
+
+
+def matched_filter(templates, moveouts, weights, data, step,
+                   n_samples_template=None, arch="gpu", check_zeros="first",
+                   normalize="short", network_sum=True, precision="fp32"):
+    """Correlation coefficients between ``templates`` and ``data``
+    (reference: fast_matched_filter.py:66-362).
+
+    templates : (T, S, C, L), (T, traces, L) or single-template (S, C, L) /
+        (traces, L) float array.
+    moveouts, weights : (T, S, C) or (T, S) arrays (broadcast over C).
+    data : (S, C, N) or (traces, N).
+    step : output decimation, in samples.
+    arch : 'gpu' (this package); 'cpu', 'precise' and 'variable_precise' are
+        the reference's CPU libraries and are reported as not loaded.
+    normalize : 'short' or 'full' (window mean removed).
+    network_sum : True -> (T, n_corr) weighted sums; False -> (T, n_corr, S, C).
+    precision : 'fp32' | 'split_bf16' | 'bf16' (numerator arithmetic).
+    """
+    assert normalize in ("short", "full"), "Only know short or full normalization methods"
+    if normalize == "full":
+        assert arch != "cpu", "Full normalization not supported with cpu arch - try arch=precise"
+    if arch.lower() != "gpu":
+        print("Compiled library for {} not loaded; exiting!".format(arch))
+        return None
+    if n_samples_template is not None:
+        raise NotImplementedError(
+            "per-channel template lengths (arch='variable_precise') are not "
+            "implemented by the GPU library")
+    if precision not in _lib.PRECISIONS:
+        raise ValueError("precision must be one of %s" % sorted(_lib.PRECISIONS))
+    lib = _require_lib()
+    pp = prepare(templates, moveouts, weights, data, step, normalize)
+    if pp is None:
+        print("Template and data dimensions are not compatible!")
+        return None
+    T, S, C, n_corr = pp["T"], pp["S"], pp["C"], pp["n_corr"]
+    n_out = T * n_corr * (1 if network_sum else S * C)
+    cc = np.zeros(n_out, dtype=np.float32)
+    args = (_ptr(pp["templates"], ct.c_float), _ptr(pp["sst"], ct.c_float),
+            _ptr(pp["moveouts"], ct.c_int), _ptr(pp["data"], ct.c_float),
+            _ptr(pp["weights"], ct.c_float), pp["step"], pp["L"], pp["N"], T, S, C,
+            n_corr, _ptr(cc, ct.c_float), pp["normalize"], int(bool(network_sum)))
+    if precision == "fp32":
+        st = lib.fmf_matched_filter(*args)
+    else:
+        st = lib.fmf_matched_filter_ex(
+            pp["templates"].ctypes.data, pp["sst"].ctypes.data, pp["moveouts"].ctypes.data,
+            pp["data"].ctypes.data, pp["weights"].ctypes.data, pp["step"], pp["L"], pp["N"],
+            T, S, C, n_corr, cc.ctypes.data, pp["normalize"], int(bool(network_sum)),
+            _lib.PRECISIONS[precision], 0, None)
+    _lib.check(st, lib)
+    cc = cc.reshape(T, n_corr) if network_sum else cc.reshape(T, n_corr, S, C)
+    _zero_report(cc, pp["moveouts"], pp["weights"], T, n_corr, pp["step"],
+                 network_sum, check_zeros)
+    return cc
+
+
+def matched_filter_device(templates, sum_square_templates, moveouts, weights, data,
+                          step, out, normalize="short", network_sum=True,
+                          precision="fp32", stream=None):
+    """Run on device-resident, canonical, C-contiguous torch CUDA tensors:
+    templates (T,S,C,L) f32, sum_square_templates (T,S,C) f32, moveouts
+    (T,S,C) int32, weights (T,S,C) f32, data (S,C,N) f32, out (T,n_corr) or
+    (T,n_corr,S,C) f32.  Asynchronous on ``stream`` (a torch.cuda.Stream or
+    raw handle; default: torch's current stream).  Returns the launch count."""
+    import torch  # plumbing only: device memory and streams
+
+    lib = _require_lib()
+    T, S, C, L = templates.shape
+    N = data.shape[-1]
+    n_corr = out.shape[1]
+    for name, t, dt in (("templates", templates, torch.float32),
+                        ("sum_square_templates", sum_square_templates, torch.float32),
+                        ("moveouts", moveouts, torch.int32), ("weights", weights, torch.float32),
+                        ("data", data, torch.float32), ("out", out, torch.float32)):
+        if not (t.is_cuda and t.dtype == dt and t.is_contiguous()):
+            raise ValueError("%s must be a contiguous CUDA tensor of %s" % (name, dt))
+    if stream is None:
+        stream = torch.cuda.current_stream()
+    handle = stream.cuda_stream if hasattr(stream, "cuda_stream") else int(stream)
+    st = lib.fmf_matched_filter_ex(
+        templates.data_ptr(), sum_square_templates.data_ptr(), moveouts.data_ptr(),
+        data.data_ptr(), weights.data_ptr(), int(step), L, N, T, S, C, n_corr,
+        out.data_ptr(), 1 if normalize == "full" else 0, int(bool(network_sum)),
+        _lib.PRECISIONS[precision], _lib.FLAG_DEVICE_POINTERS, handle)
+    _lib.check(st, lib)
+    return lib.fmf_last_launch_count()
+
+
+def test_matched_filter(n_templates=1, n_stations=1, n_components=1,
+                        template_duration=10, data_duration=86400,
+                        sampling_rate=100, step=1, arch="gpu",
+                        check_zeros="first", normalize="short",
+                        network_sum=True, precision="fp32"):
+    """Synthetic self-test of the reference (fast_matched_filter.py:365-569):
+    uniform-noise data (mean removed per channel), templates cut from the data
+    at random times with random moveouts of 0-10 s, unit weights, so that the
+    maximum coefficient of every template is 1.  Returns (templates,
+    moveouts, data, step, cc_sums, run_time)."""
+    from time import time as clock
+
+    starts = np.random.random_sample(n_templates) * (data_duration / 2)
+    if step != 1:
+        starts = np.round(starts / (step / sampling_rate)) * (step / sampling_rate)
+    moveouts = np.zeros((n_templates, n_stations, n_components))
+    for t in range(n_templates):
+        for s in range(n_stations):
+            moveouts[t, s, :] = np.random.random_sample(n_components) * 10.0
+    moveouts = np.int32(np.round(moveouts * sampling_rate))
+    n_data = data_duration * sampling_rate
+    if float(int(n_data)) != float(n_data):
+        print("The data duration times the sampling rate yields a non-integer number of samples !")
+        return None
+    n_data = int(n_data)
+    data = np.random.random_sample((n_stations, n_components, n_data)).astype("float32")
+    data -= data.mean(axis=-1, keepdims=True)
+    n_tp = template_duration * sampling_rate
+    if float(int(n_tp)) != float(n_tp):
+        print("The template duration times the sampling rate yields a non-integer number of samples !")
+        return None
+    n_tp = int(n_tp)
+    templates = np.zeros((n_templates, n_stations, n_components, n_tp), dtype=np.float32)
+    for t in range(n_templates):
+        first = starts[t] * sampling_rate
+        for s in range(n_stations):
+            for c in range(n_components):
+                a = int(first + moveouts[t, s, c])
+                templates[t, s, c, :] = data[s, c, a:a + n_tp]
+    weights = np.ones((n_templates, n_stations, n_components), dtype=np.float32)
+    t0 = clock()
+    cc_sum = matched_filter(templates, moveouts, weights, data, step, arch=arch,
+                            check_zeros=check_zeros, normalize=normalize,
+                            network_sum=network_sum, precision=precision)
+    run_time = clock() - t0
+    print("Matched filter ({}) for {} templates on {} stations/{} components over "
+          "{} samples ({} step) ran in {:.3f}s".format(
+              arch, n_templates, n_stations, n_components, n_data, step, run_time))
+    return templates, moveouts, data, step, cc_sum, run_time

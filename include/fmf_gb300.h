@@ -1,0 +1,127 @@
+/*
+ * fmf_gb300.h -- C ABI of the GB300 matched-filter library (libfmf_gb300.so).
+ *
+ * Array conventions are those of the reference library
+ * (fast_matched_filter/src/matched_filter_GPU.h:1-4, matched_filter.cu:171-176,
+ * argument packing at fast_matched_filter/fast_matched_filter.py:253-316):
+ *
+ *   templates            (T, S, C, L)  float32, C-contiguous
+ *   sum_square_templates (T, S, C)     float32, sum of templates**2 over L
+ *   moveouts             (T, S, C)     int32, samples (may be negative)
+ *   data                 (S, C, N)     float32
+ *   weights              (T, S, C)     float32; weight 0 skips the channel
+ *   cc_out               (T, n_corr)          when sum_cc_mode != 0
+ *                        (T, n_corr, S, C)    when sum_cc_mode == 0
+ *   normalize            0 = "short", 1 = "full" (window mean removed)
+ *
+ * with n_corr = (N - L) / step + 1.  Output index k of template t is valid
+ * when start <= k*step <= N - L - max(0, max moveout of t), start =
+ * ceil(-min(0, min moveout of t) / step) * step; every other output element
+ * is written as 0.  Every entry point returns an FMF_* status and never
+ * terminates the process.  All entry points run on the calling thread's
+ * current CUDA device.
+ */
+#ifndef FMF_GB300_H
+#define FMF_GB300_H
+
+#include <stddef.h>
+
+#if defined(__GNUC__)
+#define FMF_API __attribute__((visibility("default")))
+#else
+#define FMF_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define FMF_OK 0
+#define FMF_ERR_ARG 1         /* invalid sizes, null pointers, bad option */
+#define FMF_ERR_OOM 2         /* device memory allocation failed */
+#define FMF_ERR_SMEM 3        /* problem does not fit the kernel's shared memory */
+#define FMF_ERR_CUDA 4        /* CUDA runtime / launch error */
+#define FMF_ERR_TIMEOUT 5     /* a bounded device-side wait gave up */
+#define FMF_ERR_UNSUPPORTED 6 /* option not available in this build/device */
+
+/* numerator precision */
+#define FMF_PREC_FP32 0       /* plain FP32 CUDA-core form */
+#define FMF_PREC_SPLIT_BF16 1 /* tensor cores, bf16 hi+lo, 3 products, FP32 accumulate */
+#define FMF_PREC_BF16 2       /* tensor cores, single bf16 product (loss demonstration) */
+
+/* flags of fmf_matched_filter_ex */
+#define FMF_FLAG_DEVICE_POINTERS 1 /* all array arguments are device pointers */
+
+/*
+ * Drop-in for the reference GPU entry point
+ *   void matched_filter(float*, float*, int*, float*, float*, size_t step,
+ *                       size_t n_samples_template, size_t n_samples_data,
+ *                       size_t n_templates, size_t n_stations,
+ *                       size_t n_components, size_t n_corr, float* cc_out,
+ *                       int normalize, int sum_cc_mode)
+ * (fast_matched_filter/src/matched_filter_GPU.h:1-4, matched_filter.cu:171-176).
+ * Host pointers; plain FP32 form; synchronous.
+ */
+FMF_API int fmf_matched_filter(const float *templates, const float *sum_square_templates,
+                       const int *moveouts, const float *data, const float *weights,
+                       size_t step, size_t n_samples_template, size_t n_samples_data,
+                       size_t n_templates, size_t n_stations, size_t n_components,
+                       size_t n_corr, float *cc_out, int normalize, int sum_cc_mode);
+
+/*
+ * Same symbol name and argument list as the reference GPU library
+ * (matched_filter.cu:171-176), so that the reference's ctypes wrapper
+ * (fast_matched_filter.py:52-55, 314-316) can load this library in place of
+ * matched_filter_GPU.so.  Identical to fmf_matched_filter.
+ */
+FMF_API int matched_filter(const float *templates, const float *sum_square_templates,
+                   const int *moveouts, const float *data, const float *weights,
+                   size_t step, size_t n_samples_template, size_t n_samples_data,
+                   size_t n_templates, size_t n_stations, size_t n_components,
+                   size_t n_corr, float *cc_out, int normalize, int sum_cc_mode);
+
+/*
+ * Extended form of fmf_matched_filter (no reference counterpart beyond the
+ * arguments above): selects the numerator precision (FMF_PREC_*), accepts
+ * device pointers (FMF_FLAG_DEVICE_POINTERS) and runs on `stream`
+ * (a cudaStream_t, NULL = legacy default stream).  With device pointers the
+ * call is asynchronous with respect to the host; with host pointers it
+ * returns after the result has been copied back.
+ */
+FMF_API int fmf_matched_filter_ex(const float *templates, const float *sum_square_templates,
+                          const int *moveouts, const float *data, const float *weights,
+                          size_t step, size_t n_samples_template, size_t n_samples_data,
+                          size_t n_templates, size_t n_stations, size_t n_components,
+                          size_t n_corr, float *cc_out, int normalize, int sum_cc_mode,
+                          int precision, int flags, void *stream);
+
+/* Copies the calling thread's last error message (NUL-terminated, truncated
+ * to len) and returns its status.  The reference printed and exited instead
+ * (matched_filter.cu:30-39, 236-242, 286-299). */
+FMF_API int fmf_last_error(char *buf, size_t len);
+
+/* Library version string, e.g. "fmf_gb300 0.1.0 sm_103a". */
+FMF_API const char *fmf_version(void);
+
+/* Number of kernel launches issued by this thread's last entry-point call
+ * (all kernels of the library; copies and memsets are not counted). */
+FMF_API int fmf_last_launch_count(void);
+
+/* Event timing (no reference counterpart; used by the benchmark).
+ * fmf_timing_begin() makes every later call on this thread record CUDA
+ * events on its stream around its preprocessing kernels and around its
+ * correlation kernel; fmf_timing_end() waits for those events, returns the
+ * summed milliseconds of each class and the number of calls, and stops the
+ * recording. */
+FMF_API int fmf_timing_begin(void);
+FMF_API int fmf_timing_end(double *prep_ms, double *kernel_ms, int *n_calls);
+
+/* Releases device memory cached by the library on the current device. */
+FMF_API int fmf_release_cache(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FMF_GB300_H */

@@ -1,0 +1,88 @@
+"""C-ABI checks that need no GPU: the library loads, exports every symbol
+include/fmf_gb300.h declares, and rejects bad arguments with a status code
+and a message (the reference exits the process instead,
+matched_filter.cu:30-39, 236-242, 286-299)."""
+import ctypes as ct
+import os
+import re
+
+import numpy as np
+import pytest
+
+from fast_matched_filter_gb300 import _lib
+
+HEADER = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))),
+                      "include", "fmf_gb300.h")
+
+
+def declared_functions():
+    src = open(HEADER).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b([A-Za-z_]\w*)\s*\([^;{]*\)\s*;", src)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from fast_matched_filter_gb300 import build
+    build.build()
+    return _lib.load()
+
+
+def test_header_declares_the_reference_entry_point():
+    names = declared_functions()
+    assert "matched_filter" in names and "fmf_matched_filter" in names
+    assert set(_lib.EXPORTS) <= set(names)
+
+
+def test_library_exports_every_declared_symbol(lib):
+    for name in declared_functions():
+        assert hasattr(lib, name), name
+
+
+def test_version(lib):
+    assert lib.fmf_version().decode().startswith("fmf_gb300")
+
+
+def _args(T=2, S=2, C=3, L=16, N=200, step=1):
+    n_corr = (N - L) // step + 1
+    tp = np.ones((T, S, C, L), np.float32)
+    sst = np.full((T, S, C), float(L), np.float32)
+    mo = np.zeros((T, S, C), np.int32)
+    w = np.ones((T, S, C), np.float32)
+    d = np.ones((S, C, N), np.float32)
+    cc = np.zeros(T * n_corr, np.float32)
+    keep = (tp, sst, mo, d, w, cc)
+    f = lambda a, t: a.ctypes.data_as(ct.POINTER(t))  # noqa: E731
+    args = [f(tp, ct.c_float), f(sst, ct.c_float), f(mo, ct.c_int), f(d, ct.c_float),
+            f(w, ct.c_float), step, L, N, T, S, C, n_corr, f(cc, ct.c_float), 0, 1]
+    return args, keep
+
+
+@pytest.mark.parametrize("field,value", [(5, 0), (6, 0), (8, 0), (9, 0), (10, 0), (11, 0),
+                                         (6, 500), (11, 10 ** 6), (13, 2)])
+def test_bad_arguments_return_status(lib, field, value):
+    args, keep = _args()
+    args[field] = value
+    st = lib.fmf_matched_filter(*args)
+    assert st == _lib.FMF_ERR_ARG
+    code, msg = _lib.last_error(lib)
+    assert code == st and msg
+
+
+def test_null_pointer_rejected(lib):
+    args, keep = _args()
+    args[3] = None
+    assert lib.fmf_matched_filter(*args) == _lib.FMF_ERR_ARG
+
+
+def test_unknown_precision_rejected(lib):
+    args, keep = _args()
+    ex = [a if not hasattr(a, "contents") else ct.cast(a, ct.c_void_p).value for a in args]
+    st = lib.fmf_matched_filter_ex(*ex, 7, 0, None)
+    assert st == _lib.FMF_ERR_ARG
+
+
+def test_python_layer_raises_on_status(lib):
+    with pytest.raises(_lib.FMFError) as e:
+        _lib.check(_lib.FMF_ERR_ARG, lib)
+    assert "BAD_ARG" in str(e.value)

@@ -1,0 +1,178 @@
+"""GPU parity of the plain FP32 form against the oracle (needs a GB300).
+
+Bar: max |cc_gpu - cc_oracle| <= 1e-5 (TOL) for every output element, with
+the 'cpu' oracle for short normalisation and the 'precise' oracle for full
+(the reference's own routing, fast_matched_filter.py:297-306); the integer
+structure (which outputs are exactly zero) must match exactly.
+"""
+import ctypes as ct
+
+import numpy as np
+import pytest
+
+import fast_matched_filter_gb300 as fmf
+from fast_matched_filter_gb300 import _lib, synthetic
+from tests._cases import canonical, golden_names, load_golden, random_search
+
+TOL = 1e-5
+pytestmark = pytest.mark.gpu
+
+
+def oracle_of(oracle_built, tp, mo, w, d, step, normalize, network_sum):
+    arch = "cpu" if normalize == "short" else "precise"
+    return oracle_built.run_oracle(tp, mo, w, d, step, arch, normalize, network_sum)
+
+
+def assert_parity(got, ref, tol=TOL):
+    assert got.shape == ref.shape
+    assert np.all(np.isfinite(got))
+    assert np.array_equal(got == 0.0, ref == 0.0), "zero pattern differs"
+    err = np.abs(got.astype(np.float64) - ref.astype(np.float64)).max()
+    assert err <= tol, "max |diff| %.3g" % err
+
+
+@pytest.mark.parametrize("name", golden_names())
+def test_golden_fixtures(name):
+    inputs, opts, expected = load_golden(name)
+    got = fmf.matched_filter(check_zeros=False, arch="gpu", normalize=opts["normalize"],
+                             network_sum=opts["network_sum"], **inputs)
+    assert_parity(got, expected.reshape(got.shape))
+
+
+@pytest.mark.parametrize("step", [1, 2, 3, 7])
+@pytest.mark.parametrize("L", [1, 6, 33, 257])
+@pytest.mark.parametrize("normalize", ["short", "full"])
+def test_random_searches_network_sum(oracle_built, step, L, normalize):
+    tp, mo, w, d = random_search(1000 * step + L, 3, 3, 2, L, 5000 + 3 * L, -30, 140,
+                                 dc=5.0 if normalize == "full" else 0.0, zero_weights=2)
+    got = fmf.matched_filter(tp, mo, w, d, step, check_zeros=False, normalize=normalize)
+    assert_parity(got, oracle_of(oracle_built, tp, mo, w, d, step, normalize, True))
+
+
+@pytest.mark.parametrize("step", [1, 4])
+@pytest.mark.parametrize("normalize", ["short", "full"])
+def test_random_searches_per_channel(oracle_built, step, normalize):
+    tp, mo, w, d = random_search(77 + step, 2, 4, 3, 90, 6000, -12, 300, dc=1.0, zero_weights=3)
+    got = fmf.matched_filter(tp, mo, w, d, step, check_zeros=False, normalize=normalize,
+                             network_sum=False)
+    assert_parity(got, oracle_of(oracle_built, tp, mo, w, d, step, normalize, False))
+
+
+def test_tile_boundaries_and_long_template(oracle_built):
+    # n_corr straddles several 4096-output tiles; L near the largest batched size
+    tp, mo, w, d = random_search(5, 2, 2, 3, 1200, 14000, 0, 900)
+    got = fmf.matched_filter(tp, mo, w, d, 1, check_zeros=False)
+    assert_parity(got, oracle_of(oracle_built, tp, mo, w, d, 1, "short", True))
+
+
+def test_edge_sizes(oracle_built):
+    # N == L (one output), and a template whose moveouts leave no valid lag
+    tp, mo, w, d = random_search(9, 2, 2, 2, 50, 50, 0, 0, plant=False)
+    got = fmf.matched_filter(tp, mo, w, d, 1, check_zeros=False)
+    assert got.shape == (2, 1)
+    assert_parity(got, oracle_of(oracle_built, tp, mo, w, d, 1, "short", True))
+    tp, mo, w, d = random_search(10, 2, 2, 2, 50, 400, 0, 10, plant=False)
+    mo[1, 0, 0] = 390  # N - L - max_mo < 0: template 1 has no valid output
+    got = fmf.matched_filter(tp, mo, w, d, 1, check_zeros=False)
+    assert np.all(got[1] == 0.0)
+    ref = oracle_of(oracle_built, tp[:1], mo[:1], w[:1], d, 1, "short", True)
+    assert_parity(got[:1], ref)
+
+
+def test_all_weights_zero_gives_zero():
+    tp, mo, w, d = random_search(3, 2, 2, 2, 40, 900)
+    w[:] = 0.0
+    got = fmf.matched_filter(tp, mo, w, d, 1, check_zeros=False)
+    assert np.all(got == 0.0)
+
+
+def test_formats_agree_bit_exact():
+    tp, mo, w, d = random_search(21, 3, 4, 3, 64, 3000)
+    a = fmf.matched_filter(tp, mo, w, d, 1, check_zeros=False)
+    b = fmf.matched_filter(tp.reshape(3, 12, 64), mo.reshape(3, 12), w.reshape(3, 12),
+                           d.reshape(12, 3000), 1, check_zeros=False)
+    c = fmf.matched_filter(tp[1], mo[1], w[1], d, 1, check_zeros=False)
+    assert np.array_equal(a, b)
+    assert np.array_equal(a[1:2], c)
+
+
+def test_config0_full(oracle_built):
+    cfg = synthetic.config0()
+    args = (cfg["templates"], cfg["moveouts"], cfg["weights"], cfg["data"], cfg["step"])
+    got = fmf.matched_filter(*args, check_zeros=False)
+    assert_parity(got, oracle_of(oracle_built, *args, "short", True))
+    # planted copies at amplitude 0.5 are found
+    assert got.max() > 0.3
+
+
+def test_long_trace_crop_consistency(oracle_built):
+    """4.32M-sample channels: outputs of an interior window of lags equal the
+    oracle on the cropped data that window needs."""
+    cfg = synthetic.config4(n_templates=3)
+    tp, mo, w, d = cfg["templates"], cfg["moveouts"], cfg["weights"], cfg["data"]
+    got = fmf.matched_filter(tp, mo, w, d, 1, check_zeros=False)
+    assert got.shape == (3, 4320000 - 600 + 1)
+    for k0 in (0, 2_000_003, 4_300_000):
+        a, b = k0, min(k0 + 8000, got.shape[1])
+        crop = d[:, :, a:b + 600 + 1500]
+        ref = oracle_of(oracle_built, tp, mo, w, crop, 1, "short", True)
+        n = min(b - a, ref.shape[1] - 1500)
+        assert_parity(got[:, a:a + n], ref[:, :n])
+
+
+def test_full_precision_stress_vs_fp64():
+    """DC offset 1e3 and amplitudes 1e-3..1e3 (the precision-stress search),
+    reduced in length: the plain form stays within TOL of FP64."""
+    from oracle import fp64
+    cfg = synthetic.config2(n_templates=2, n_samples=60000)
+    tp, mo, w, d = cfg["templates"], cfg["moveouts"], cfg["weights"], cfg["data"]
+    got = fmf.matched_filter(tp, mo, w, d, 2, check_zeros=False, normalize="full")
+    ref = fp64.fp64_matched_filter(tp, mo, w, d, 2, "full", True)
+    assert np.abs(got - ref).max() <= TOL
+
+
+def test_reference_named_symbol_with_reference_argtypes(oracle_built):
+    """The library answers the reference wrapper's own call
+    (fast_matched_filter.py:19-33, 314-316): symbol `matched_filter`, 13 typed
+    arguments plus two default-converted ints."""
+    lib = ct.CDLL(_lib.LIB_PATH)
+    fp, ip, sz = ct.POINTER(ct.c_float), ct.POINTER(ct.c_int), ct.c_size_t
+    lib.matched_filter.argtypes = [fp, fp, ip, fp, fp, sz, sz, sz, sz, sz, sz, sz, fp]
+    tp, mo, w, d = random_search(31, 2, 3, 3, 48, 2000)
+    T, S, C, L = tp.shape
+    N = d.shape[-1]
+    n_corr = int((N - L) / 1 + 1)
+    sst = np.sum(tp ** 2, axis=-1).astype(np.float32).ravel()
+    cc = np.zeros(T * n_corr, np.float32)
+    p = lambda a, t: np.ascontiguousarray(a).ctypes.data_as(ct.POINTER(t))  # noqa: E731
+    tpf, mof, wf, df = tp.ravel(), mo.ravel(), w.ravel(), d.ravel()
+    lib.matched_filter(p(tpf, ct.c_float), p(sst, ct.c_float), p(mof, ct.c_int),
+                       p(df, ct.c_float), p(wf, ct.c_float), 1, L, N, T, S, C, n_corr,
+                       p(cc, ct.c_float), 0, 1)
+    assert_parity(cc.reshape(T, n_corr), oracle_of(oracle_built, tp, mo, w, d, 1, "short", True))
+
+
+def test_device_pointer_path_matches_host_path():
+    torch = pytest.importorskip("torch")
+    tp, mo, w, d = random_search(41, 4, 3, 3, 100, 20000, 0, 200)
+    host = fmf.matched_filter(tp, mo, w, d, 1, check_zeros=False)
+    dev = torch.device("cuda")
+    sst = torch.from_numpy(np.sum(tp ** 2, axis=-1).astype(np.float32)).to(dev)
+    out = torch.zeros(host.shape, dtype=torch.float32, device=dev)
+    n = fmf.matched_filter_device(torch.from_numpy(tp).to(dev), sst,
+                                  torch.from_numpy(mo).to(dev), torch.from_numpy(w).to(dev),
+                                  torch.from_numpy(d).to(dev), 1, out)
+    torch.cuda.synchronize()
+    assert n >= 2
+    assert np.array_equal(out.cpu().numpy(), host)
+
+
+def test_synthetic_self_test_finds_templates():
+    """The reference's self-test recipe (fast_matched_filter.py:365-569):
+    templates cut from the data correlate to 1 on every channel at their
+    origin, so with unit weights the network sum peaks at S*C."""
+    np.random.seed(7)
+    out = fmf.test_matched_filter(n_templates=3, n_stations=2, n_components=3,
+                                  template_duration=4, data_duration=600, sampling_rate=50)
+    cc = out[4]
+    assert np.all(np.abs(cc.max(axis=1) - 6.0) < 1e-4)
