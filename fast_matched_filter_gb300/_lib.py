@@ -40,7 +40,8 @@ ARGTYPES_EX = [ct.c_void_p] * 5 + [_sz] * 7 + [ct.c_void_p, ct.c_int, ct.c_int,
 # every symbol declared in include/fmf_gb300.h
 EXPORTS = ("fmf_matched_filter", "matched_filter", "fmf_matched_filter_ex",
            "fmf_last_error", "fmf_version", "fmf_last_launch_count",
-           "fmf_release_cache", "fmf_timing_begin", "fmf_timing_end")
+           "fmf_release_cache", "fmf_timing_begin", "fmf_timing_end",
+           "fmf_device_errors")
 
 
 class FMFError(RuntimeError):
@@ -75,6 +76,7 @@ def load(path=None):
     lib.fmf_last_launch_count.restype = ct.c_int
     lib.fmf_release_cache.restype = ct.c_int
     lib.fmf_timing_begin.restype = ct.c_int
+    lib.fmf_device_errors.restype = ct.c_int
     lib.fmf_timing_end.argtypes = [ct.POINTER(ct.c_double), ct.POINTER(ct.c_double),
                                    ct.POINTER(ct.c_int)]
     lib.fmf_timing_end.restype = ct.c_int

@@ -10,6 +10,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <cstdlib>
 #include <climits>
 
 #include "fmf_common.cuh"
@@ -100,37 +101,68 @@ __global__ void channel_mean_kernel(const float *, int, float *);
 __global__ void window_stats_kernel(const float *, int, int, int, const float *, float *,
                                     float *, float *);
 int launch_plain(const Problem &P, cudaStream_t stream);
+int launch_tc(const Problem &P, const float *data_for_tc, int precision, int mo_min, int mo_max,
+              unsigned *err, Scratch &ws, cudaStream_t s, int forced_nb);
 
-// ---------------------------------------------------------------- memory
-// Stream-ordered scratch allocations (cudaMallocAsync from the device's
-// default pool).  The pool keeps freed blocks for reuse by later calls;
-// fmf_release_cache() trims it.
-struct Scratch {
-    cudaStream_t s;
-    void *ptr[16];
-    int n = 0;
-    explicit Scratch(cudaStream_t st) : s(st) {}
-    template <class T>
-    int get(T **out, size_t count, const char *what)
-    {
+// min and max of all moveouts (for the tensor-core stream padding)
+__global__ void moveout_range_kernel(const int *__restrict__ mo, long long n, int *__restrict__ out)
+{
+    int lo = 0x7fffffff, hi = -0x7fffffff - 1;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        lo = min(lo, mo[i]);
+        hi = max(hi, mo[i]);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        lo = min(lo, __shfl_down_sync(0xffffffffu, lo, o));
+        hi = max(hi, __shfl_down_sync(0xffffffffu, hi, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicMin(out, lo);
+        atomicMax(out + 1, hi);
+    }
+}
+
+// ---------------------------------------------------------------- device error word
+// Kernels with bounded waits OR a code into this word when a wait gives up.
+constexpr int kMaxDevices = 64;
+static unsigned *g_err_word[kMaxDevices];
+
+static int device_error_word(unsigned **out)
+{
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess || dev < 0 || dev >= kMaxDevices)
+        return set_error(FMF_ERR_CUDA, "no usable current device");
+    if (!g_err_word[dev]) {
         void *p = nullptr;
-        cudaError_t e = cudaMallocAsync(&p, count * sizeof(T) + 16, s);
-        if (e != cudaSuccess) {
+        if ((e = cudaMalloc(&p, 64)) != cudaSuccess || (e = cudaMemset(p, 0, 64)) != cudaSuccess) {
             cudaGetLastError();
-            return set_error(e == cudaErrorMemoryAllocation ? FMF_ERR_OOM : FMF_ERR_CUDA,
-                             "allocating %zu bytes for %s: %s", count * sizeof(T), what,
-                             cudaGetErrorString(e));
+            return set_error(FMF_ERR_CUDA, "allocating the error word: %s", cudaGetErrorString(e));
         }
-        ptr[n++] = p;
-        *out = static_cast<T *>(p);
-        return FMF_OK;
+        g_err_word[dev] = static_cast<unsigned *>(p);
     }
-    ~Scratch()
-    {
-        for (int i = 0; i < n; i++)
-            cudaFreeAsync(ptr[i], s);
-    }
-};
+    *out = g_err_word[dev];
+    return FMF_OK;
+}
+
+// Reads and clears the error word after the device has finished the work.
+static int collect_device_errors()
+{
+    unsigned *w = nullptr;
+    int rc = device_error_word(&w);
+    if (rc)
+        return rc;
+    unsigned v = 0;
+    cudaError_t e = cudaMemcpy(&v, w, sizeof(v), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && v)
+        e = cudaMemset(w, 0, sizeof(v));
+    if (e != cudaSuccess)
+        return set_error(FMF_ERR_CUDA, "reading the error word: %s", cudaGetErrorString(e));
+    if (v)
+        return set_error(FMF_ERR_TIMEOUT, "a device-side wait gave up (code 0x%x)", v);
+    return FMF_OK;
+}
 
 static void keep_pool_cached()
 {
@@ -252,8 +284,33 @@ static int run_device(const Args &a, cudaStream_t s)
         if ((rc = cuda_status(cudaMemsetAsync(a.out, 0, bytes, s), "clearing the output")))
             return rc;
     }
-    if (a.precision != FMF_PREC_FP32)
-        return set_error(FMF_ERR_UNSUPPORTED, "tensor-core precision not built yet");
+    if (a.precision != FMF_PREC_FP32) {
+        unsigned *err = nullptr;
+        if ((rc = device_error_word(&err)))
+            return rc;
+        int *range_d;
+        if ((rc = ws.get(&range_d, 2, "moveout range")))
+            return rc;
+        const int init[2] = {0x7fffffff, -0x7fffffff - 1};
+        int range[2];
+        if ((rc = cuda_status(cudaMemcpyAsync(range_d, init, sizeof(init), cudaMemcpyHostToDevice, s),
+                              "moveout range")))
+            return rc;
+        const long long n_mo = (long long)T * SC;
+        moveout_range_kernel<<<(unsigned)min((n_mo + 255) / 256, 1024LL), 256, 0, s>>>(a.mo, n_mo,
+                                                                                     range_d);
+        count_launch();
+        if ((rc = cuda_status(cudaMemcpyAsync(range, range_d, sizeof(range), cudaMemcpyDeviceToHost, s),
+                              "moveout range")) ||
+            (rc = cuda_status(cudaStreamSynchronize(s), "moveout range")))
+            return rc;
+        const char *nb_env = getenv("FMF_TC_NB");
+        int forced = nb_env ? atoi(nb_env) : 0;
+        cudaEvent_t ev0 = mark(s);
+        rc = launch_tc(P, full ? dcen : a.data, a.precision, range[0], range[1], err, ws, s, forced);
+        span(ev0, mark(s), 1);
+        return rc;
+    }
     // grid.y carries the template index: launch in slices of 65535 templates
     cudaEvent_t ev_main0 = mark(s);
     for (int t0 = 0; t0 < T; t0 += 65535) {
@@ -309,7 +366,9 @@ static int run_host(const Args &a, cudaStream_t s)
                               "copying the result to the host")))
             return rc;
     }
-    return cuda_status(cudaStreamSynchronize(s), "matched filter");
+    if ((rc = cuda_status(cudaStreamSynchronize(s), "matched filter")))
+        return rc;
+    return a.precision != FMF_PREC_FP32 ? collect_device_errors() : FMF_OK;
 }
 
 static int entry(const Args &a, void *stream)
@@ -397,6 +456,15 @@ int fmf_last_error(char *buf, size_t len)
 const char *fmf_version(void) { return FMF_VERSION_STRING; }
 
 int fmf_last_launch_count(void) { return fmf::g_launches; }
+
+int fmf_device_errors(void)
+{
+    fmf::clear_error();
+    cudaError_t e = cudaDeviceSynchronize();
+    if (e != cudaSuccess)
+        return fmf::cuda_status(e, "fmf_device_errors");
+    return fmf::collect_device_errors();
+}
 
 int fmf_timing_begin(void)
 {

@@ -46,4 +46,37 @@ namespace fmf {
 int set_error(int status, const char *fmt, ...);
 void count_launch(int n = 1);
 int check_launch(const char *what);
+
+// Stream-ordered scratch allocations (cudaMallocAsync from the device's
+// default pool).  The pool keeps freed blocks for reuse by later calls;
+// fmf_release_cache() trims it.  Everything is freed, in stream order, when
+// the Scratch goes out of scope.
+struct Scratch {
+    cudaStream_t s;
+    void *ptr[32];
+    int n = 0;
+    explicit Scratch(cudaStream_t st) : s(st) {}
+    template <class T>
+    int get(T **out, size_t count, const char *what)
+    {
+        void *p = nullptr;
+        if (n >= 32)
+            return set_error(FMF_ERR_OOM, "too many scratch buffers");
+        cudaError_t e = cudaMallocAsync(&p, count * sizeof(T) + 16, s);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            return set_error(e == cudaErrorMemoryAllocation ? FMF_ERR_OOM : FMF_ERR_CUDA,
+                             "allocating %zu bytes for %s: %s", count * sizeof(T), what,
+                             cudaGetErrorString(e));
+        }
+        ptr[n++] = p;
+        *out = static_cast<T *>(p);
+        return FMF_OK;
+    }
+    ~Scratch()
+    {
+        for (int i = 0; i < n; i++)
+            cudaFreeAsync(ptr[i], s);
+    }
+};
 }  // namespace fmf

@@ -28,6 +28,12 @@ GPU_LOADED = _LIB is not None
 
 
 def _require_lib():
+    """The loaded library; retried here when it was built after import.
+    Raises RuntimeError when it cannot be loaded (no CPU fallback)."""
+    global _LIB, _LIB_ERROR, GPU_LOADED
+    if _LIB is None:
+        _LIB, _LIB_ERROR = _lib.try_load()
+        GPU_LOADED = _LIB is not None
     if _LIB is None:
         raise RuntimeError(
             "fast_matched_filter_gb300: libfmf_gb300.so is not loadable (%s); "

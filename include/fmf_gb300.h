@@ -108,6 +108,12 @@ FMF_API const char *fmf_version(void);
  * (all kernels of the library; copies and memsets are not counted). */
 FMF_API int fmf_last_launch_count(void);
 
+/* Waits for the current device and reports FMF_ERR_TIMEOUT if a kernel of
+ * this library gave up a bounded device-side wait since the last check (the
+ * host-pointer entry points check this themselves).  No reference
+ * counterpart. */
+FMF_API int fmf_device_errors(void);
+
 /* Event timing (no reference counterpart; used by the benchmark).
  * fmf_timing_begin() makes every later call on this thread record CUDA
  * events on its stream around its preprocessing kernels and around its

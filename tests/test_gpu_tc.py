@@ -1,0 +1,90 @@
+"""GPU parity of the tensor-core forms (tcgen05 split-BF16 and single BF16).
+
+Split-BF16 must meet the same bar as the plain form: max |cc - oracle|
+<= 1e-5 and the same zero pattern.  The single-BF16 form is checked only
+for the size of its loss (it exists to show that loss).
+"""
+import os
+
+import numpy as np
+import pytest
+
+import fast_matched_filter_gb300 as fmf
+from fast_matched_filter_gb300 import synthetic
+from tests._cases import random_search
+from tests.test_gpu_parity import TOL, assert_parity, oracle_of
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(params=["32", "64", "auto"])
+def tile_lags(request, monkeypatch):
+    """Lag blocks per tile (128 outputs each); 'auto' lets the library choose."""
+    if request.param == "auto":
+        monkeypatch.delenv("FMF_TC_NB", raising=False)
+    else:
+        monkeypatch.setenv("FMF_TC_NB", request.param)
+    return request.param
+
+
+@pytest.mark.parametrize("step", [1, 2, 3])
+@pytest.mark.parametrize("L", [16, 70, 200])
+@pytest.mark.parametrize("normalize", ["short", "full"])
+def test_split_bf16_network_sum(oracle_built, tile_lags, step, L, normalize):
+    tp, mo, w, d = random_search(500 + 10 * step + L, 2, 2, 2, L, 20000 + 7 * L, -40, 300,
+                                 dc=4.0 if normalize == "full" else 0.0, zero_weights=1)
+    got = fmf.matched_filter(tp, mo, w, d, step, check_zeros=False, normalize=normalize,
+                             precision="split_bf16")
+    assert_parity(got, oracle_of(oracle_built, tp, mo, w, d, step, normalize, True))
+
+
+@pytest.mark.parametrize("normalize", ["short", "full"])
+def test_split_bf16_per_channel(oracle_built, tile_lags, normalize):
+    tp, mo, w, d = random_search(8, 2, 3, 2, 90, 9000, -5, 200, dc=2.0, zero_weights=2)
+    got = fmf.matched_filter(tp, mo, w, d, 2, check_zeros=False, normalize=normalize,
+                             network_sum=False, precision="split_bf16")
+    assert_parity(got, oracle_of(oracle_built, tp, mo, w, d, 2, normalize, False))
+
+
+def test_split_bf16_config0(oracle_built):
+    cfg = synthetic.config0()
+    args = (cfg["templates"], cfg["moveouts"], cfg["weights"], cfg["data"], cfg["step"])
+    got = fmf.matched_filter(*args, check_zeros=False, precision="split_bf16")
+    assert_parity(got, oracle_of(oracle_built, *args, "short", True))
+
+
+def test_split_bf16_long_template(oracle_built):
+    tp, mo, w, d = random_search(12, 2, 2, 1, 1200, 40000, 0, 1000)
+    got = fmf.matched_filter(tp, mo, w, d, 1, check_zeros=False, precision="split_bf16")
+    assert_parity(got, oracle_of(oracle_built, tp, mo, w, d, 1, "short", True))
+
+
+def test_split_bf16_matches_plain_on_long_trace():
+    cfg = synthetic.config4(n_templates=2, n_samples=400000)
+    args = (cfg["templates"], cfg["moveouts"], cfg["weights"], cfg["data"], 1)
+    a = fmf.matched_filter(*args, check_zeros=False, precision="fp32")
+    b = fmf.matched_filter(*args, check_zeros=False, precision="split_bf16")
+    assert np.array_equal(a == 0, b == 0)
+    assert np.abs(a - b).max() <= TOL
+
+
+def test_precision_stress_vs_fp64():
+    """DC 1e3, amplitudes 1e-3..1e3, full normalisation, step 2: split-BF16
+    within TOL of FP64; single BF16 visibly worse."""
+    from oracle import fp64
+    cfg = synthetic.config2(n_templates=2, n_samples=80000)
+    tp, mo, w, d = cfg["templates"], cfg["moveouts"], cfg["weights"], cfg["data"]
+    ref = fp64.fp64_matched_filter(tp, mo, w, d, 2, "full", True)
+    split = fmf.matched_filter(tp, mo, w, d, 2, check_zeros=False, normalize="full",
+                               precision="split_bf16")
+    single = fmf.matched_filter(tp, mo, w, d, 2, check_zeros=False, normalize="full",
+                                precision="bf16")
+    e_split = np.abs(split - ref).max()
+    e_single = np.abs(single - ref).max()
+    assert e_split <= TOL, e_split
+    assert e_single > e_split and e_single < 5e-2
+
+
+def test_no_device_errors_after_tc_runs():
+    from fast_matched_filter_gb300 import _lib
+    assert _lib.load().fmf_device_errors() == 0
