@@ -101,27 +101,8 @@ __global__ void channel_mean_kernel(const float *, int, float *);
 __global__ void window_stats_kernel(const float *, int, int, int, const float *, float *,
                                     float *, float *);
 int launch_plain(const Problem &P, cudaStream_t stream);
-int launch_tc(const Problem &P, const float *data_for_tc, int precision, int mo_min, int mo_max,
-              unsigned *err, Scratch &ws, cudaStream_t s, int forced_nb);
-
-// min and max of all moveouts (for the tensor-core stream padding)
-__global__ void moveout_range_kernel(const int *__restrict__ mo, long long n, int *__restrict__ out)
-{
-    int lo = 0x7fffffff, hi = -0x7fffffff - 1;
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-         i += (long long)gridDim.x * blockDim.x) {
-        lo = min(lo, mo[i]);
-        hi = max(hi, mo[i]);
-    }
-    for (int o = 16; o > 0; o >>= 1) {
-        lo = min(lo, __shfl_down_sync(0xffffffffu, lo, o));
-        hi = max(hi, __shfl_down_sync(0xffffffffu, hi, o));
-    }
-    if ((threadIdx.x & 31) == 0) {
-        atomicMin(out, lo);
-        atomicMax(out + 1, hi);
-    }
-}
+int launch_tc(const Problem &P, const float *data_for_tc, int precision, unsigned *err, Scratch &ws,
+              cudaStream_t s, int forced_nb);
 
 // ---------------------------------------------------------------- device error word
 // Kernels with bounded waits OR a code into this word when a wait gives up.
@@ -247,8 +228,11 @@ static int run_device(const Args &a, cudaStream_t s)
         channel_mean_kernel<<<SC, 256, 0, s>>>(a.data, N, mu);
         count_launch(2);
     }
-    cudaFuncSetAttribute(window_stats_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         227 * 1024);
+    if ((rc = cuda_status(cudaFuncSetAttribute(window_stats_kernel,
+                                               cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                               (int)stat_smem),
+                          "window statistics shared memory")))
+        return rc;
     dim3 sgrid((N + kStatBlock - 1) / kStatBlock, SC);
     window_stats_kernel<<<sgrid, 256, stat_smem, s>>>(a.data, N, L, kStatBlock, mu, dcen, stat_e,
                                                       stat_m);
@@ -288,26 +272,10 @@ static int run_device(const Args &a, cudaStream_t s)
         unsigned *err = nullptr;
         if ((rc = device_error_word(&err)))
             return rc;
-        int *range_d;
-        if ((rc = ws.get(&range_d, 2, "moveout range")))
-            return rc;
-        const int init[2] = {0x7fffffff, -0x7fffffff - 1};
-        int range[2];
-        if ((rc = cuda_status(cudaMemcpyAsync(range_d, init, sizeof(init), cudaMemcpyHostToDevice, s),
-                              "moveout range")))
-            return rc;
-        const long long n_mo = (long long)T * SC;
-        moveout_range_kernel<<<(unsigned)min((n_mo + 255) / 256, 1024LL), 256, 0, s>>>(a.mo, n_mo,
-                                                                                     range_d);
-        count_launch();
-        if ((rc = cuda_status(cudaMemcpyAsync(range, range_d, sizeof(range), cudaMemcpyDeviceToHost, s),
-                              "moveout range")) ||
-            (rc = cuda_status(cudaStreamSynchronize(s), "moveout range")))
-            return rc;
         const char *nb_env = getenv("FMF_TC_NB");
         int forced = nb_env ? atoi(nb_env) : 0;
         cudaEvent_t ev0 = mark(s);
-        rc = launch_tc(P, full ? dcen : a.data, a.precision, range[0], range[1], err, ws, s, forced);
+        rc = launch_tc(P, full ? dcen : a.data, a.precision, err, ws, s, forced);
         span(ev0, mark(s), 1);
         return rc;
     }
@@ -379,6 +347,7 @@ static int entry(const Args &a, void *stream)
     if (rc)
         return rc;
     keep_pool_cached();
+    cudaGetLastError();  // this library's runtime state only: start from a clean slate
     cudaStream_t s = (cudaStream_t)stream;
     if (a.flags & FMF_FLAG_DEVICE_POINTERS)
         return run_device(a, s);

@@ -215,11 +215,11 @@ int launch_plain(const Problem &P, cudaStream_t stream)
         return set_error(FMF_ERR_SMEM,
                          "template length %d with step %d needs %zu bytes of shared memory (max 232448)",
                          P.L, P.step, g.smem);
-    static bool attr_done = false;  // per process; attribute is per function
-    if (!attr_done) {
-        cudaFuncSetAttribute(plain_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-        attr_done = true;
-    }
+    cudaError_t e = cudaFuncSetAttribute(plain_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)g.smem);
+    if (e != cudaSuccess)
+        return set_error(FMF_ERR_CUDA, "plain kernel shared memory (%zu bytes): %s", g.smem,
+                         cudaGetErrorString(e));
     dim3 grid((unsigned)((P.n_corr + PL_TILE - 1) / PL_TILE), (unsigned)P.T);
     plain_kernel<<<grid, PL_THREADS, g.smem, stream>>>(P, g);
     count_launch();

@@ -562,8 +562,8 @@ static int choose_nb(int L, int step, int split, int forced)
     return 0;
 }
 
-int launch_tc(const Problem &P, const float *data_for_tc, int precision, int mo_min, int mo_max,
-              unsigned *err, Scratch &ws, cudaStream_t s, int forced_nb)
+int launch_tc(const Problem &P, const float *data_for_tc, int precision, unsigned *err, Scratch &ws,
+              cudaStream_t s, int forced_nb)
 {
     int rc;
     const int split = precision == FMF_PREC_SPLIT_BF16;
@@ -583,13 +583,13 @@ int launch_tc(const Problem &P, const float *data_for_tc, int precision, int mo_
     g.stage_bytes = (g.stage_bytes + 1023) & ~1023;
     g.smem = 2 * (size_t)g.stage_bytes + 128;
     g.n_tiles = (int)((P.n_corr + (long long)TC_Q * NB - 1) / ((long long)TC_Q * NB));
-    // stream-row range touched by any tile: r0 = (I0 + mu - s)/Q + row_front, rows [r0, r0 + R)
-    const long long mu_min = mo_min >= 0 ? mo_min / step : -((-(long long)mo_min + step - 1) / step);
-    const long long mu_max = ((long long)mo_max + step - 1) >= 0 ? ((long long)mo_max + step - 1) / step : 0;
-    g.row_front = (int)((mu_min < 0 ? (-mu_min + TC_Q - 1) / TC_Q : 0) + 1);
-    const long long I0_max = (long long)(g.n_tiles - 1) * TC_Q * NB;
-    g.rows_total = (int)((I0_max + (mu_max > 0 ? mu_max : 0)) / TC_Q + g.row_front + g.R + 1);
-
+    // Stream rows a tile can touch.  A CTA runs only when its tile holds a
+    // valid output k of its template, i.e. k*step + mo >= 0 and
+    // k*step + mo + L <= N for every channel; hence its first row
+    // r0 = (I0 + mu - s)/Q lies in [-(NB + 2), (N/step + 1)/Q + 1] whatever the
+    // moveouts are, and rows [r0, r0 + R) stay inside the padded stream.
+    g.row_front = NB + 3;
+    g.rows_total = g.row_front + (int)(((long long)P.N / step + 2) / TC_Q) + 2 + g.R + 1;
     const size_t g_elems = (size_t)P.SC * step * TC_CB * g.rows_total * 8;
     const size_t w_elems = (size_t)P.T * P.SC * step * g.NW * 64;
     const size_t n_meta = (size_t)P.T * P.SC * step;
@@ -627,20 +627,27 @@ int launch_tc(const Problem &P, const float *data_for_tc, int precision, int mo_
     const long long ctas = (long long)g.n_tiles * P.T;
     if (ctas > 0x7fffffffLL)
         return set_error(FMF_ERR_ARG, "too many tiles for one launch");
+    cudaError_t e;
     switch (NB) {
     case 128:
-        cudaFuncSetAttribute(tc_kernel<128>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)g.smem);
-        tc_kernel<128><<<(unsigned)ctas, TC_THREADS, g.smem, s>>>(A);
+        e = cudaFuncSetAttribute(tc_kernel<128>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)g.smem);
+        if (e == cudaSuccess)
+            tc_kernel<128><<<(unsigned)ctas, TC_THREADS, g.smem, s>>>(A);
         break;
     case 64:
-        cudaFuncSetAttribute(tc_kernel<64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)g.smem);
-        tc_kernel<64><<<(unsigned)ctas, TC_THREADS, g.smem, s>>>(A);
+        e = cudaFuncSetAttribute(tc_kernel<64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)g.smem);
+        if (e == cudaSuccess)
+            tc_kernel<64><<<(unsigned)ctas, TC_THREADS, g.smem, s>>>(A);
         break;
     default:
-        cudaFuncSetAttribute(tc_kernel<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)g.smem);
-        tc_kernel<32><<<(unsigned)ctas, TC_THREADS, g.smem, s>>>(A);
+        e = cudaFuncSetAttribute(tc_kernel<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)g.smem);
+        if (e == cudaSuccess)
+            tc_kernel<32><<<(unsigned)ctas, TC_THREADS, g.smem, s>>>(A);
         break;
     }
+    if (e != cudaSuccess)
+        return set_error(FMF_ERR_CUDA, "tc_kernel shared memory (%zu bytes): %s", g.smem,
+                         cudaGetErrorString(e));
     count_launch();
     return check_launch("tc_kernel");
 }
