@@ -366,8 +366,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1) tc_kernel(const TcArgs A)
     const uint32_t tmem = *tmem_holder;
 
     const int R = g.R, NW = g.NW;
+    // stage layout: [data hi][data lo, split only][template hi][template lo, split only]
     const uint32_t data_bytes = (uint32_t)TC_CB * R * 16;  // one of hi/lo
     const uint32_t wbytes = (uint32_t)NW * 128;
+    const uint32_t w_off = (g.split ? 2u : 1u) * data_bytes;
 
     if (warp == 0) {
         // ---------------------------------------------------------- producer
@@ -397,7 +399,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) tc_kernel(const TcArgs A)
                 }
                 if (lane < (g.split ? 2 : 1)) {
                     const uint16_t *src = (lane ? A.w_lo : A.w_hi) + meta * NW * 64;
-                    bulk_g2s(st + 2 * data_bytes + lane * wbytes, src, wbytes, full0 + 8 * s);
+                    bulk_g2s(st + w_off + lane * wbytes, src, wbytes, full0 + 8 * s);
                 }
             }
         }
@@ -435,8 +437,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) tc_kernel(const TcArgs A)
                     const int k_first = sres & ~15;
                     const int k_end = (sres + lphi + TC_Q - 1 + 15) & ~15;
                     const uint32_t zhi = smem_u32(smem + (size_t)s * g.stage_bytes);
-                    const uint32_t zlo = zhi + data_bytes, whi = zhi + 2 * data_bytes,
-                                   wlo = whi + wbytes;
+                    const uint32_t zlo = zhi + data_bytes, whi = zhi + w_off, wlo = whi + wbytes;
                     for (int k = k_first; k < k_end; k += 16) {
                         const uint32_t wo = (uint32_t)(k >> 3) * 128u;
                         const uint32_t bo = (uint32_t)((k & (TC_Q - 1)) >> 3) * lbo_b +
