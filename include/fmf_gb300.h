@@ -96,6 +96,36 @@ FMF_API int fmf_matched_filter_ex(const float *templates, const float *sum_squar
                           size_t n_corr, float *cc_out, int normalize, int sum_cc_mode,
                           int precision, int flags, void *stream);
 
+/*
+ * Allocation-free entry point.  No counterpart in the reference.
+ *
+ * For callers that cannot allocate device memory while they run -- a
+ * real-time detection loop that reserves its memory at start-up and must not
+ * call cudaMalloc/cudaFree (which can synchronise the device and take
+ * unbounded time) in its processing path, or a host application that owns
+ * the GPU's memory budget (a pre-reserved pool, a per-process cap) in which
+ * allocations by this library would fail or fragment.
+ *
+ * Same arguments as fmf_matched_filter plus a stream; every array argument is
+ * a device pointer; plain FP32 form; asynchronous on `stream`.  It allocates
+ * nothing: its working arrays live in one file-scope device array of
+ * FMF_NOALLOC_SCRATCH_BYTES that every GPU loading this library holds until
+ * the process exits.  The scratch needed is 4*S*C*N + 8*T bytes for
+ * normalize=0 and 12*S*C*N + 4*T*S*C*(L+1) + 4*S*C + 8*T bytes for
+ * normalize=1 (each part rounded up to 256 bytes); larger searches are
+ * rejected with FMF_ERR_ARG.  The first call on a device looks up the array's
+ * device address with that device current: make it before any stream
+ * capture.  All calls share the array, so calls that overlap on the GPU race
+ * and must be serialised by the caller.
+ */
+#define FMF_NOALLOC_SCRATCH_BYTES 33554432u /* 32 MiB */
+FMF_API int fmf_matched_filter_noalloc(const float *templates, const float *sum_square_templates,
+                                       const int *moveouts, const float *data, const float *weights,
+                                       size_t step, size_t n_samples_template, size_t n_samples_data,
+                                       size_t n_templates, size_t n_stations, size_t n_components,
+                                       size_t n_corr, float *cc_out, int normalize, int sum_cc_mode,
+                                       void *stream);
+
 /* Copies the calling thread's last error message (NUL-terminated, truncated
  * to len) and returns its status.  The reference printed and exited instead
  * (matched_filter.cu:30-39, 236-242, 286-299). */
