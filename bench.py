@@ -56,6 +56,8 @@ def parse_args(argv=None):
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-compare", action="store_true",
                    help="skip the plain FP32 comparison run")
+    p.add_argument("--no-precision-report", action="store_true",
+                   help="skip the FP64 error report on a subset")
     p.add_argument("--templates", type=int, default=0, help="override T (smaller runs)")
     p.add_argument("--samples", type=int, default=0, help="override N (smaller runs)")
     return p.parse_args(argv)
@@ -349,6 +351,8 @@ def run_ours(args):
                               "roofline": roofline(cfg, "fp32", plain["kernel_ms_avg"],
                                                    plain["prep_ms_avg"])}
 
+    if rank == 0 and not args.no_precision_report:
+        line["precision_vs_fp64"] = precision_report(cfg)
     # end to end through the C ABI with pinned host buffers
     del g
     if not args.no_e2e:
@@ -441,6 +445,43 @@ def roofline(cfg, precision, kern_ms, prep_ms):
     return roof
 
 
+def precision_report(cfg, n_templates=2, n_lags=50000):
+    """max and p99.9 |cc - FP64| of every form on a bounded subset (the first
+    templates, a window of output indices in the middle of the trace), plus the
+    reference CPU algorithm's own error on the same subset."""
+    import torch
+
+    import fast_matched_filter_gb300 as fmf
+    from oracle import cpu, fp64
+    tp = cfg["templates"][:n_templates]
+    mo, w = cfg["moveouts"][:n_templates], cfg["weights"][:n_templates]
+    d, step = cfg["data"], cfg["step"]
+    L = tp.shape[-1]
+    n_corr = cfg["n_corr"]
+    k0 = max(0, n_corr // 2 - n_lags // 2)
+    k1 = min(n_corr, k0 + n_lags)
+    # data window that outputs [k0, k1) read, re-indexed from 0
+    lo = int(k0 * step + min(0, mo.min()))
+    hi = int((k1 - 1) * step + max(0, mo.max()) + L)
+    lo -= lo % step
+    win = np.ascontiguousarray(d[:, :, lo:hi])
+    ref = fp64.fp64_matched_filter(tp, mo, w, win, step, cfg["normalize"], True)
+    out = {}
+    for prec in ("fp32", "split_bf16", "bf16"):
+        got = fmf.matched_filter(tp, mo, w, win, step, check_zeros=False,
+                                 normalize=cfg["normalize"], precision=prec)
+        err = np.abs(got.astype(np.float64) - ref)
+        out[prec] = {"max": float(err.max()), "p99.9": float(np.quantile(err, 0.999))}
+    arch = "cpu" if cfg["normalize"] == "short" else "precise"
+    r = cpu.run_oracle(tp, mo, w, win, step, arch, cfg["normalize"], True)
+    err = np.abs(r.astype(np.float64) - ref)
+    out["reference_cpu_" + arch] = {"max": float(err.max()), "p99.9": float(np.quantile(err, 0.999))}
+    out["subset"] = "templates 0-%d, %d outputs around the middle of the trace" % (n_templates - 1,
+                                                                                   ref.shape[1])
+    torch.cuda.synchronize()
+    return out
+
+
 def run_e2e(cfg, dev_out, precision, args, world, lib):
     import torch
     from fast_matched_filter_gb300 import _lib
@@ -474,10 +515,84 @@ def run_e2e(cfg, dev_out, precision, args, world, lib):
             "api": "fmf_matched_filter_ex (C ABI, host pointers, pinned)"}
 
 
+def run_batch(args):
+    """Batched uneven searches: one graph (preprocessing + persistent tile-queue
+    launch) vs the same searches as sequential plain FP32 calls and as
+    sequential tensor-core calls."""
+    import torch
+
+    import fast_matched_filter_gb300 as fmf
+    from fast_matched_filter_gb300 import synthetic
+    torch.cuda.set_device(0)
+    shapes = synthetic.config3_shapes(max_templates=args.templates or 100,
+                                      max_samples=args.samples or 400000)
+    probs, total_macs = [], 0
+    for sh in shapes:
+        cfg = synthetic.config3_problem(sh)
+        tp = cfg["templates"]
+        n_corr = (sh["N"] - sh["L"]) // sh["step"] + 1
+        g = [torch.from_numpy(np.ascontiguousarray(x)).cuda() for x in
+             (tp, np.sum(tp ** 2, axis=-1).astype(np.float32), cfg["moveouts"], cfg["weights"],
+              cfg["data"])]
+        out = torch.empty((sh["T"], n_corr), dtype=torch.float32, device="cuda")
+        probs.append((sh, g, out))
+        total_macs += synthetic.macs(tp.shape, sh["N"], sh["step"])
+    batch = fmf.Batch("split_bf16")
+    for sh, g, out in probs:
+        batch.add(*g, sh["step"], out, sh["normalize"], True)
+    stream = torch.cuda.current_stream()
+
+    def timeit(fn, steps, warmup):
+        for _ in range(warmup):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / steps
+
+    def sequential(prec):
+        for sh, g, out in probs:
+            fmf.matched_filter_device(*g, sh["step"], out, sh["normalize"], True, prec, stream)
+
+    with ClockSampler(0) as clocks:
+        ms_batch = timeit(batch.run, args.steps, max(args.warmup, 1))
+    launches = batch.run()
+    ms_seq_tc = timeit(lambda: sequential("split_bf16"), max(1, args.steps // 2), 1)
+    ms_seq_plain = timeit(lambda: sequential("fp32"), max(1, args.steps // 2), 1)
+    lib = fmf.fast_matched_filter._require_lib()
+    from fast_matched_filter_gb300 import _lib
+    _lib.check(lib.fmf_device_errors(), lib)
+    v = total_macs / (ms_batch / 1e3) / 1e12
+    line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_batch, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "bf16x3", "data": "synthetic",
+            "config": {"workload": "config3_64_uneven_searches", "searches": len(shapes),
+                       "templates_max": args.templates or 100,
+                       "samples_max": args.samples or 400000,
+                       "total_macs": total_macs, "shapes_seed": 103,
+                       "form": "one CUDA graph: per-search preprocessing + persistent "
+                               "tile-queue tensor-core launch"},
+            "gpu_launches": launches * args.steps, "clocks": clocks.summary(),
+            "sequential_split_bf16": {"value": total_macs / (ms_seq_tc / 1e3) / 1e12,
+                                      "ms_per_step": ms_seq_tc},
+            "sequential_plain_fp32": {"value": total_macs / (ms_seq_plain / 1e3) / 1e12,
+                                      "ms_per_step": ms_seq_plain,
+                                      "batched_speedup": ms_seq_plain / ms_batch}}
+    batch.close()
+    print(json.dumps(line))
+    return 0
+
+
 def main(argv=None):
     args = parse_args(argv)
     if args.impl == "reference":
         return run_reference_arm(args)
+    if args.workload == "config3":
+        return run_batch(args)
     return run_ours(args)
 
 

@@ -7,6 +7,7 @@ The exported names mirror the reference package's
 (fast_matched_filter/__init__.py:11-16).
 """
 from .fast_matched_filter import (  # noqa: F401
+    Batch,
     CPU_LOADED,
     GPU_LOADED,
     matched_filter,

@@ -29,6 +29,16 @@ PRECISIONS = {"fp32": PREC_FP32, "split_bf16": PREC_SPLIT_BF16, "bf16": PREC_BF1
 
 FLAG_DEVICE_POINTERS = 1
 
+
+def flag_tile(lag_blocks):
+    """FMF_FLAG_TILE: tensor-core lag blocks per tile (0 = library choice)."""
+    return ((int(lag_blocks) // 16) & 0xFF) << 8
+
+
+def flag_template_group(n):
+    """FMF_FLAG_TEMPLATE_GROUP: templates interleaved per group of tile-queue items."""
+    return (int(n) & 0xFF) << 16
+
 _fp = ct.POINTER(ct.c_float)
 _ip = ct.POINTER(ct.c_int)
 _sz = ct.c_size_t
@@ -41,7 +51,9 @@ ARGTYPES_EX = [ct.c_void_p] * 5 + [_sz] * 7 + [ct.c_void_p, ct.c_int, ct.c_int,
 EXPORTS = ("fmf_matched_filter", "matched_filter", "fmf_matched_filter_ex",
            "fmf_last_error", "fmf_version", "fmf_last_launch_count",
            "fmf_release_cache", "fmf_timing_begin", "fmf_timing_end",
-           "fmf_device_errors")
+           "fmf_device_errors", "fmf_matched_filter_noalloc", "fmf_batch_create",
+           "fmf_batch_add", "fmf_batch_set_tiles", "fmf_batch_run", "fmf_batch_launch_count",
+           "fmf_batch_destroy", "fmf_selftest_wait_timeout")
 
 
 class FMFError(RuntimeError):
@@ -77,6 +89,20 @@ def load(path=None):
     lib.fmf_release_cache.restype = ct.c_int
     lib.fmf_timing_begin.restype = ct.c_int
     lib.fmf_device_errors.restype = ct.c_int
+    lib.fmf_selftest_wait_timeout.argtypes = [ct.c_uint]
+    lib.fmf_selftest_wait_timeout.restype = ct.c_int
+    lib.fmf_batch_create.argtypes = [ct.POINTER(ct.c_void_p), ct.c_int]
+    lib.fmf_batch_create.restype = ct.c_int
+    lib.fmf_batch_add.argtypes = [ct.c_void_p] + ARGTYPES_EX[:15]
+    lib.fmf_batch_add.restype = ct.c_int
+    lib.fmf_batch_set_tiles.argtypes = [ct.c_void_p, ct.c_int, ct.c_int]
+    lib.fmf_batch_set_tiles.restype = ct.c_int
+    lib.fmf_batch_run.argtypes = [ct.c_void_p, ct.c_void_p]
+    lib.fmf_batch_run.restype = ct.c_int
+    lib.fmf_batch_launch_count.argtypes = [ct.c_void_p]
+    lib.fmf_batch_launch_count.restype = ct.c_int
+    lib.fmf_batch_destroy.argtypes = [ct.c_void_p]
+    lib.fmf_batch_destroy.restype = ct.c_int
     lib.fmf_timing_end.argtypes = [ct.POINTER(ct.c_double), ct.POINTER(ct.c_double),
                                    ct.POINTER(ct.c_int)]
     lib.fmf_timing_end.restype = ct.c_int

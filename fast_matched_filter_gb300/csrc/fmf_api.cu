@@ -100,16 +100,16 @@ __global__ void template_center_kernel(const float *, int, float *, float *);
 __global__ void channel_mean_kernel(const float *, int, float *);
 __global__ void window_stats_kernel(const float *, int, int, int, const float *, float *,
                                     float *, float *);
-int launch_plain(const Problem &P, cudaStream_t stream);
 int launch_tc(const Problem &P, const float *data_for_tc, int precision, unsigned *err, Scratch &ws,
-              cudaStream_t s, int forced_nb);
+              cudaStream_t s, int forced_nb, int template_group);
+int launch_wait_selftest(unsigned *err, unsigned ms, cudaStream_t s);
 
 // ---------------------------------------------------------------- device error word
 // Kernels with bounded waits OR a code into this word when a wait gives up.
 constexpr int kMaxDevices = 64;
 static unsigned *g_err_word[kMaxDevices];
 
-static int device_error_word(unsigned **out)
+int device_error_word(unsigned **out)
 {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
@@ -158,15 +158,7 @@ static void keep_pool_cached()
 }
 
 // ---------------------------------------------------------------- validation
-struct Args {
-    const float *tpl, *sst, *data, *w;
-    const int *mo;
-    float *out;
-    size_t step, L, N, T, S, C, n_corr;
-    int normalize, sum_mode, precision, flags;
-};
-
-static int validate(const Args &a)
+int validate_args(const Args &a)
 {
     if (!a.tpl || !a.sst || !a.mo || !a.data || !a.w || !a.out)
         return set_error(FMF_ERR_ARG, "null array argument");
@@ -193,7 +185,7 @@ static int validate(const Args &a)
 constexpr int kStatBlock = 4096;
 
 // ---------------------------------------------------------------- core (device pointers)
-static int run_device(const Args &a, cudaStream_t s)
+int prepare_problem(const Args &a, Scratch &ws, cudaStream_t s, Problem *Pout, const float **data_for_tc)
 {
     int rc;
     const int T = (int)a.T, SC = (int)(a.S * a.C), L = (int)a.L, N = (int)a.N;
@@ -202,7 +194,6 @@ static int run_device(const Args &a, cudaStream_t s)
     if (stat_smem > 227 * 1024)
         return set_error(FMF_ERR_SMEM, "template length %d too long for the window-statistics kernel", L);
 
-    Scratch ws(s);
     int *k_lo, *k_hi;
     float *stat_e, *stat_m = nullptr, *mu = nullptr, *dcen = nullptr, *tcen = nullptr, *tsum = nullptr;
     if ((rc = ws.get(&k_lo, 2 * (size_t)T, "template ranges")))
@@ -219,7 +210,6 @@ static int run_device(const Args &a, cudaStream_t s)
             return rc;
     }
 
-    cudaEvent_t ev_prep0 = mark(s);
     template_range_kernel<<<(T + 127) / 128, 128, 0, s>>>(a.mo, T, SC, L, N, (int)a.step,
                                                             (int)a.n_corr, k_lo, k_hi);
     count_launch();
@@ -239,8 +229,6 @@ static int run_device(const Args &a, cudaStream_t s)
     count_launch();
     if ((rc = check_launch("preprocessing kernels")))
         return rc;
-    cudaEvent_t ev_prep1 = mark(s);
-    span(ev_prep0, ev_prep1, 0);
 
     Problem P;
     P.tpl = full ? tcen : a.tpl;
@@ -268,24 +256,21 @@ static int run_device(const Args &a, cudaStream_t s)
         if ((rc = cuda_status(cudaMemsetAsync(a.out, 0, bytes, s), "clearing the output")))
             return rc;
     }
-    if (a.precision != FMF_PREC_FP32) {
-        unsigned *err = nullptr;
-        if ((rc = device_error_word(&err)))
-            return rc;
-        const char *nb_env = getenv("FMF_TC_NB");
-        int forced = nb_env ? atoi(nb_env) : 0;
-        cudaEvent_t ev0 = mark(s);
-        rc = launch_tc(P, full ? dcen : a.data, a.precision, err, ws, s, forced);
-        span(ev0, mark(s), 1);
-        return rc;
-    }
-    // grid.y carries the template index: launch in slices of 65535 templates
-    cudaEvent_t ev_main0 = mark(s);
-    for (int t0 = 0; t0 < T; t0 += 65535) {
+    *Pout = P;
+    *data_for_tc = full ? dcen : a.data;
+    return FMF_OK;
+}
+
+// Plain FP32 form over all templates (grid.y carries the template index:
+// slices of 65535 templates).
+int launch_plain_all(const Problem &P, cudaStream_t s)
+{
+    int rc;
+    for (int t0 = 0; t0 < P.T; t0 += 65535) {
         Problem Q = P;
-        int nt = T - t0 < 65535 ? T - t0 : 65535;
-        size_t o = (size_t)t0 * SC;
-        Q.tpl += o * L;
+        int nt = P.T - t0 < 65535 ? P.T - t0 : 65535;
+        size_t o = (size_t)t0 * P.SC;
+        Q.tpl += o * P.L;
         Q.sst += o;
         if (Q.tsum)
             Q.tsum += o;
@@ -293,13 +278,45 @@ static int run_device(const Args &a, cudaStream_t s)
         Q.w += o;
         Q.k_lo += t0;
         Q.k_hi += t0;
-        Q.out += (size_t)t0 * a.n_corr * (P.network_sum ? 1 : SC);
+        Q.out += (size_t)t0 * P.n_corr * (P.network_sum ? 1 : P.SC);
         Q.T = nt;
         if ((rc = launch_plain(Q, s)))
             return rc;
     }
-    span(ev_main0, mark(s), 1);
     return FMF_OK;
+}
+
+static int run_device(const Args &a, cudaStream_t s)
+{
+    int rc;
+    Scratch ws(s);
+    Problem P;
+    const float *data_for_tc = nullptr;
+    cudaEvent_t ev_prep0 = mark(s);
+    if ((rc = prepare_problem(a, ws, s, &P, &data_for_tc)))
+        return rc;
+    cudaEvent_t ev_prep1 = mark(s);
+    span(ev_prep0, ev_prep1, 0);
+    if (a.precision != FMF_PREC_FP32) {
+        unsigned *err = nullptr;
+        if ((rc = device_error_word(&err)))
+            return rc;
+        const char *nb_env = getenv("FMF_TC_NB");
+        int forced = nb_env ? atoi(nb_env) : 0;
+        if (a.flags & 0xff00)
+            forced = ((a.flags >> 8) & 0xff) * 16;
+        const int group = (a.flags >> 16) & 0xff;
+        if (forced != 0 && forced != 32 && forced != 64 && forced != 128)
+            return set_error(FMF_ERR_ARG, "tensor-core tile of %d lag blocks (32, 64 or 128)", forced);
+        cudaEvent_t ev0 = mark(s);
+        rc = launch_tc(P, data_for_tc, a.precision, err, ws, s, forced, group);
+        span(ev0, mark(s), 1);
+        return rc;
+    }
+    cudaEvent_t ev_main0 = mark(s);
+    rc = launch_plain_all(P, s);
+    span(ev_main0, mark(s), 1);
+    return rc;
 }
 
 // ---------------------------------------------------------------- host-pointer path
@@ -343,7 +360,7 @@ static int entry(const Args &a, void *stream)
 {
     clear_error();
     g_launches = 0;
-    int rc = validate(a);
+    int rc = validate_args(a);
     if (rc)
         return rc;
     keep_pool_cached();
@@ -425,6 +442,25 @@ int fmf_last_error(char *buf, size_t len)
 const char *fmf_version(void) { return FMF_VERSION_STRING; }
 
 int fmf_last_launch_count(void) { return fmf::g_launches; }
+
+int fmf_selftest_wait_timeout(unsigned ms)
+{
+    fmf::clear_error();
+    if (ms < 1 || ms > 5000)
+        return fmf::set_error(FMF_ERR_ARG, "selftest wait limit must be 1..5000 ms");
+    unsigned *err = nullptr;
+    int rc = fmf::device_error_word(&err);
+    if (rc)
+        return rc;
+    cudaError_t e = cudaDeviceSynchronize();
+    if (e != cudaSuccess)
+        return fmf::cuda_status(e, "fmf_selftest_wait_timeout");
+    if ((rc = fmf::collect_device_errors()))  // start from a clear word
+        return rc;
+    if ((rc = fmf::launch_wait_selftest(err, ms, nullptr)))
+        return rc;
+    return fmf_device_errors();
+}
 
 int fmf_device_errors(void)
 {

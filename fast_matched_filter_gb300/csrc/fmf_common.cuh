@@ -11,6 +11,8 @@
 #include <stddef.h>
 #include <stdint.h>
 
+#include <vector>
+
 #include "../../include/fmf_gb300.h"
 
 namespace fmf {
@@ -53,15 +55,14 @@ int check_launch(const char *what);
 // the Scratch goes out of scope.
 struct Scratch {
     cudaStream_t s;
-    void *ptr[32];
-    int n = 0;
+    std::vector<void *> ptr;
     explicit Scratch(cudaStream_t st) : s(st) {}
+    Scratch(const Scratch &) = delete;
+    Scratch &operator=(const Scratch &) = delete;
     template <class T>
     int get(T **out, size_t count, const char *what)
     {
         void *p = nullptr;
-        if (n >= 32)
-            return set_error(FMF_ERR_OOM, "too many scratch buffers");
         cudaError_t e = cudaMallocAsync(&p, count * sizeof(T) + 16, s);
         if (e != cudaSuccess) {
             cudaGetLastError();
@@ -69,14 +70,40 @@ struct Scratch {
                              "allocating %zu bytes for %s: %s", count * sizeof(T), what,
                              cudaGetErrorString(e));
         }
-        ptr[n++] = p;
+        ptr.push_back(p);
         *out = static_cast<T *>(p);
         return FMF_OK;
     }
     ~Scratch()
     {
-        for (int i = 0; i < n; i++)
-            cudaFreeAsync(ptr[i], s);
+        for (void *p : ptr)
+            cudaFreeAsync(p, s);
     }
 };
+
+// Preprocessing shared by every form: per-template lag ranges, 'full'
+// centring, FP64 window statistics (fmf_api.cu).  Fills the epilogue fields of
+// *P and the data the numerator kernels read (centred for 'full').
+struct Args {
+    const float *tpl, *sst, *data, *w;
+    const int *mo;
+    float *out;
+    size_t step, L, N, T, S, C, n_corr;
+    int normalize, sum_mode, precision, flags;
+};
+int validate_args(const Args &a);
+int prepare_problem(const Args &a, Scratch &ws, cudaStream_t s, Problem *P, const float **data_for_tc);
+
+// Tensor-core form (fmf_tc.cu).
+constexpr int TC_MAX_PROBS = 64;
+struct TcProb;
+int tc_choose_nb(int L, int step, int split, int forced);
+int tc_prepare(const Problem &P, const float *data_for_tc, int split, int nb, int tg, Scratch &ws,
+               cudaStream_t s, TcProb *out);
+int tc_run(const TcProb *probs, int n, int split, unsigned long long *queue, unsigned *err,
+           cudaStream_t s);
+size_t tc_prob_size();
+int launch_plain(const Problem &P, cudaStream_t stream);
+int launch_plain_all(const Problem &P, cudaStream_t stream);
+int device_error_word(unsigned **out);
 }  // namespace fmf

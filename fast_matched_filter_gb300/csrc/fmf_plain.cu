@@ -15,8 +15,9 @@
 // ceil((L - phi)/step) taps against a decimated data window.  Per (channel,
 // phase) one *stage* is staged in shared memory with cp.async (zero-filled
 // outside [0, N)): the decimated data window (4096 + taps samples, stored with
-// 4 padding floats every 32 so that the 16-byte loads of consecutive threads,
-// 64 bytes apart, fall into distinct banks) and the phase's template taps.
+// 4 padding floats every 16: the 16-byte load of lane l then falls in bank
+// group 5*l mod 8 whatever the tap offset, so the 8 lanes of each quarter-warp
+// access hit distinct banks) and the phase's template taps.
 // Two stage buffers are in flight.
 //
 // Inner loop: a 20-register sliding window of data per thread; per 4 taps one
@@ -36,7 +37,7 @@ constexpr int PL_R = 16;                       // outputs per thread
 constexpr int PL_TILE = PL_THREADS * PL_R;     // outputs per CTA
 constexpr int PL_U = 20;                       // taps per unrolled iteration
 
-__host__ __device__ __forceinline__ int padx(int x) { return x + ((x >> 5) << 2); }
+__host__ __device__ __forceinline__ int padx(int x) { return x + ((x >> 4) << 2); }
 
 struct PlainGeom {
     int lq_pad;       // taps per phase, padded to a multiple of PL_U

@@ -50,31 +50,37 @@ namespace fmf {
 
 constexpr int TC_Q = 128;
 constexpr int TC_CB = TC_Q / 8;
-constexpr int TC_THREADS = 384;
+constexpr int TC_EPI_WARPS = 8;                    // epilogue warps (2 per TMEM lane quarter)
+constexpr int TC_THREADS = 32 * (4 + TC_EPI_WARPS);  // + producer, MMA and 2 idle warps
 constexpr int TC_TG = 16;  // templates interleaved per group of CTAs (L2 reuse of data rows)
 constexpr unsigned long long TC_WAIT_NS = 2000000000ull;  // 2 s per wait
 
-struct TcGeom {
-    int NB;           // lag blocks per tile (MMA N)
-    int R;            // data rows per stage
-    int NW;           // 128-byte template blocks per (template, channel, phase)
-    int k_span;       // largest K extent (multiple of 16)
-    int rows_total;   // rows per (channel, stream) in G
-    int row_front;    // rows of zero padding before sample 0
-    int stage_bytes;  // bytes of one pipeline stage
-    int split;        // 1: hi/lo, three products; 0: single bf16 product
-    int n_tiles;
-    size_t smem;
-};
 
-struct TcArgs {
-    Problem P;
-    const uint16_t *g_hi, *g_lo;  // bf16 bits, [SC][step][CB][rows_total][8]
-    const uint16_t *w_hi, *w_lo;  // bf16 bits, [T][SC][step][NW][64]
+// One search of a persistent launch (tile-queue items [item_begin, item_begin + n_tiles*T)).
+struct TcProb {
+    Problem P;                    // sizes, epilogue inputs, output
+    const uint16_t *g_hi, *g_lo;  // bf16 bits, data streams [SC][step][CB][rows_total][8]
+    const uint16_t *w_hi, *w_lo;  // bf16 bits, template blocks [T][SC][step][NW][64]
     const int *mu;                // [T][SC][step] moveout of each phase in its stream
     const int *psi;               // [T][SC][step] stream of each phase
+    long long item_begin;         // first tile-queue item of this search
+    int R;                        // data rows per stage
+    int NW;                       // 128-byte template blocks per (template, channel, phase)
+    int rows_total;               // rows per (channel, stream) in the data streams
+    int row_front;                // rows of zero padding before sample 0
+    int n_tiles;                  // output tiles of nb*128 indices
+    int tg;                       // templates interleaved per group of items
+    int nb;                       // lag blocks per tile (MMA N): 32, 64 or 128
+};
+
+struct TcBatch {
+    TcProb prob[TC_MAX_PROBS];
+    int n_probs;
+    int split;                    // 1: hi/lo, three products; 0: single bf16 product
+    int stage_bytes;              // bytes of one pipeline stage (largest search)
+    long long total_items;
+    unsigned long long *queue;    // tile-queue head, zero before the launch
     unsigned *err;                // device error word
-    TcGeom g;
 };
 
 // ------------------------------------------------------------------ PTX helpers
@@ -119,9 +125,11 @@ __device__ __forceinline__ unsigned long long gtimer()
 }
 
 // Bounded wait on an mbarrier phase.  Returns false when the CTA aborted or
-// when this wait gave up (then it raises the error word and the abort flag).
+// when this wait gave up after `limit_ns` (then it raises the error word and
+// the abort flag).
 __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile int *abort_flag,
-                                          unsigned *err, unsigned code)
+                                          unsigned *err, unsigned code,
+                                          unsigned long long limit_ns = TC_WAIT_NS)
 {
     if (mbar_try(bar, parity))
         return true;
@@ -132,7 +140,7 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatil
         if ((it & 63) == 0) {
             if (*abort_flag)
                 return false;
-            if (gtimer() - t0 > TC_WAIT_NS) {
+            if (gtimer() - t0 > limit_ns) {
                 atomicOr(err, code);
                 *abort_flag = 1;
                 return false;
@@ -204,6 +212,61 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float *v)
 }
 
 __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float *v)
+{
+    uint32_t r[8];
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+                   "=r"(r[7])
+                 : "r"(taddr));
+#pragma unroll
+    for (int i = 0; i < 8; i++)
+        v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ void tmem_st16(uint32_t taddr, const float *v)
+{
+    asm volatile(
+        "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+        "%16};" ::"r"(taddr),
+        "r"(__float_as_uint(v[0])), "r"(__float_as_uint(v[1])), "r"(__float_as_uint(v[2])),
+        "r"(__float_as_uint(v[3])), "r"(__float_as_uint(v[4])), "r"(__float_as_uint(v[5])),
+        "r"(__float_as_uint(v[6])), "r"(__float_as_uint(v[7])), "r"(__float_as_uint(v[8])),
+        "r"(__float_as_uint(v[9])), "r"(__float_as_uint(v[10])), "r"(__float_as_uint(v[11])),
+        "r"(__float_as_uint(v[12])), "r"(__float_as_uint(v[13])), "r"(__float_as_uint(v[14])),
+        "r"(__float_as_uint(v[15]))
+        : "memory");
+}
+
+__device__ __forceinline__ void tmem_st8(uint32_t taddr, const float *v)
+{
+    asm volatile("tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};" ::"r"(taddr),
+                 "r"(__float_as_uint(v[0])), "r"(__float_as_uint(v[1])), "r"(__float_as_uint(v[2])),
+                 "r"(__float_as_uint(v[3])), "r"(__float_as_uint(v[4])), "r"(__float_as_uint(v[5])),
+                 "r"(__float_as_uint(v[6])), "r"(__float_as_uint(v[7]))
+                 : "memory");
+}
+
+__device__ __forceinline__ void tmem_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
+
+// CH consecutive accumulator columns of this warp's 32 lanes (CH = 8 or 16)
+template <int CH>
+__device__ __forceinline__ void tmem_ldc(uint32_t taddr, float *v)
+{
+    if constexpr (CH == 16)
+        tmem_ld16(taddr, v);
+    else
+        tmem_ld8(taddr, v);
+}
+template <int CH>
+__device__ __forceinline__ void tmem_stc(uint32_t taddr, const float *v)
+{
+    if constexpr (CH == 16)
+        tmem_st16(taddr, v);
+    else
+        tmem_st8(taddr, v);
+}
 
 // ------------------------------------------------------------------ preprocessing
 __device__ __forceinline__ void split_bf16(float x, uint16_t &hi, uint16_t &lo)
@@ -302,57 +365,63 @@ __global__ void tc_template_kernel(const float *__restrict__ tpl, const int *__r
         reinterpret_cast<uint4 *>(w_lo)[idx] = lv;
 }
 
-// ------------------------------------------------------------------ main kernel
-template <int NB>
-__global__ void __launch_bounds__(TC_THREADS, 1) tc_kernel(const TcArgs A)
+// ------------------------------------------------------------------ persistent kernel
+// Decodes a tile-queue item: search p, output tile, template t.  Items of one
+// search are ordered so that groups of `tg` templates sweep the tiles together.
+__device__ __forceinline__ void decode_item(const TcBatch &B, long long item, int &p, int &tile, int &t)
+{
+    int lo = 0, hi = B.n_probs - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (B.prob[mid].item_begin <= item)
+            lo = mid;
+        else
+            hi = mid - 1;
+    }
+    p = lo;
+    const TcProb &pr = B.prob[p];
+    const long long local = item - pr.item_begin;
+    const long long per_group = (long long)pr.n_tiles * pr.tg;
+    const int grp = (int)(local / per_group);
+    const long long rem = local - (long long)grp * per_group;
+    const int tg0 = grp * pr.tg;
+    const int tgn = min(pr.tg, pr.P.T - tg0);
+    tile = (int)(rem / tgn);
+    t = tg0 + (int)(rem % tgn);
+}
+
+constexpr int TC_NB_MAX = 128;  // largest tile; TMEM columns: D0 [0,128), D1 [128,256), sum [256,384)
+
+__global__ void __launch_bounds__(TC_THREADS, 1) tc_persistent(const __grid_constant__ TcBatch B)
 {
     extern __shared__ __align__(1024) uint8_t smem[];
-    const TcGeom &g = A.g;
-    const Problem &P = A.P;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int split = B.split;
 
-    // tile and template of this CTA (templates interleaved in groups of TC_TG)
-    const int per_group = g.n_tiles * TC_TG;
-    const int grp = blockIdx.x / per_group;
-    const int rem = blockIdx.x - grp * per_group;
-    const int tg0 = grp * TC_TG;
-    const int tgn = min(TC_TG, P.T - tg0);
-    const int tile = rem / tgn;
-    const int t = tg0 + rem % tgn;
-    const long long I0 = (long long)tile * TC_Q * NB;
-    const int klo = P.k_lo[t], khi = P.k_hi[t];
-    const int SC = P.SC, step = P.step;
-    const float *w = P.w + (size_t)t * SC;
-    const int *mo = P.mo + (size_t)t * SC;
-
-    if (!(I0 < khi && I0 + (long long)TC_Q * NB > klo)) {
-        // no valid output in this tile: zeros (network sum); per-channel output is pre-cleared
-        if (P.network_sum)
-            for (int x = threadIdx.x; x < TC_Q * NB; x += TC_THREADS)
-                if (I0 + x < P.n_corr)
-                    P.out[(size_t)t * P.n_corr + I0 + x] = 0.0f;
-        return;
-    }
-
-    uint8_t *bar_base = smem + 2 * g.stage_bytes;
+    uint8_t *bar_base = smem + 2 * (size_t)B.stage_bytes;
     const uint32_t full0 = smem_u32(bar_base), empty0 = full0 + 16, dfull0 = full0 + 32,
-                   dempty0 = full0 + 48, fin = full0 + 64;
-    uint32_t *tmem_holder = reinterpret_cast<uint32_t *>(bar_base + 80);
-    volatile int *abort_flag = reinterpret_cast<volatile int *>(bar_base + 84);
+                   dempty0 = full0 + 48, fin = full0 + 64, ifull0 = full0 + 72, iempty0 = full0 + 104;
+    long long *ring = reinterpret_cast<long long *>(bar_base + 136);  // 4 item slots
+    uint32_t *tmem_holder = reinterpret_cast<uint32_t *>(bar_base + 168);
+    volatile int *abort_flag = reinterpret_cast<volatile int *>(bar_base + 172);
 
     if (threadIdx.x == 0) {
         for (int i = 0; i < 2; i++) {
             mbar_init(full0 + 8 * i, 1);
             mbar_init(empty0 + 8 * i, 1);
             mbar_init(dfull0 + 8 * i, 1);
-            mbar_init(dempty0 + 8 * i, 8);
+            mbar_init(dempty0 + 8 * i, TC_EPI_WARPS);
         }
         mbar_init(fin, 1);
+        for (int i = 0; i < 4; i++) {
+            mbar_init(ifull0 + 8 * i, 1);
+            mbar_init(iempty0 + 8 * i, 1 + TC_EPI_WARPS);  // MMA thread + epilogue warps
+        }
         *abort_flag = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     }
-    constexpr uint32_t TMEM_COLS = NB * 2 <= 32 ? 32 : (NB * 2 <= 64 ? 64 : (NB * 2 <= 128 ? 128 : 256));
+    constexpr uint32_t TMEM_COLS = 512;  // D0, D1, sum at columns 0, 128, 256 (one CTA per SM)
     if (warp == 1) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
                          smem_u32(tmem_holder)),
@@ -364,176 +433,281 @@ __global__ void __launch_bounds__(TC_THREADS, 1) tc_kernel(const TcArgs A)
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = *tmem_holder;
-
-    const int R = g.R, NW = g.NW;
-    // stage layout: [data hi][data lo, split only][template hi][template lo, split only]
-    const uint32_t data_bytes = (uint32_t)TC_CB * R * 16;  // one of hi/lo
-    const uint32_t wbytes = (uint32_t)NW * 128;
-    const uint32_t w_off = (g.split ? 2u : 1u) * data_bytes;
+    const long long total = B.total_items;
 
     if (warp == 0) {
-        // ---------------------------------------------------------- producer
+        // ---------------------------------------------------------- producer + tile queue
         int j = 0;
-        for (int ch = 0; ch < SC; ch++) {
-            if (w[ch] == 0.0f)
+        for (long long q = 0;; q++) {
+            const int slot = (int)(q & 3);
+            long long item = total;
+            if (lane == 0) {
+                bool ok = q < 4 || mbar_wait(iempty0 + 8 * slot, (uint32_t)(((q >> 2) - 1) & 1), abort_flag,
+                                             B.err, 1u);
+                if (ok && !*abort_flag)
+                    item = (long long)atomicAdd(B.queue, 1ull);
+                ring[slot] = item;
+                mbar_arrive(ifull0 + 8 * slot);
+            }
+            item = __shfl_sync(0xffffffffu, item, 0);  // warp-uniform decision
+            if (item >= total)
+                break;
+            int p, tile, t;
+            decode_item(B, item, p, tile, t);
+            const TcProb &pr = B.prob[p];
+            const Problem &P = pr.P;
+            const int nb = pr.nb;
+            const long long I0 = (long long)tile * TC_Q * nb;
+            if (!(I0 < P.k_hi[t] && I0 + (long long)TC_Q * nb > P.k_lo[t]))
                 continue;
-            for (int phi = 0; phi < step; phi++, j++) {
-                const int s = j & 1;
-                if (j >= 2 &&
-                    !mbar_wait_warp(empty0 + 8 * s, ((j >> 1) - 1) & 1, abort_flag, A.err, 2u))
-                    goto producer_done;
-                const long long meta = ((long long)t * SC + ch) * step + phi;
-                const int mu = A.mu[meta], psi = A.psi[meta];
-                const int sres = ((mu % TC_Q) + TC_Q) % TC_Q;
-                const long long r0 = (I0 + mu - sres) / TC_Q + g.row_front;
-                const uint32_t st = smem_u32(smem + (size_t)s * g.stage_bytes);
-                if (lane == 0)
-                    mbar_expect_tx(full0 + 8 * s, (g.split ? 2u : 1u) * (data_bytes + wbytes));
-                __syncwarp();
-                const int cb = lane & 15, hl = lane >> 4;
-                if (hl == 0 || g.split) {
-                    const uint16_t *src = (hl ? A.g_lo : A.g_hi) +
-                                          ((((long long)ch * step + psi) * TC_CB + cb) * g.rows_total + r0) * 8;
-                    bulk_g2s(st + hl * data_bytes + cb * (uint32_t)R * 16, src, (uint32_t)R * 16,
-                             full0 + 8 * s);
-                }
-                if (lane < (g.split ? 2 : 1)) {
-                    const uint16_t *src = (lane ? A.w_lo : A.w_hi) + meta * NW * 64;
-                    bulk_g2s(st + w_off + lane * wbytes, src, wbytes, full0 + 8 * s);
+            const int SC = P.SC, step = P.step, R = pr.R, NW = pr.NW;
+            const uint32_t data_bytes = (uint32_t)TC_CB * R * 16, wbytes = (uint32_t)NW * 128;
+            const uint32_t w_off = (split ? 2u : 1u) * data_bytes;
+            const float *w = P.w + (size_t)t * SC;
+            for (int ch = 0; ch < SC; ch++) {
+                if (w[ch] == 0.0f)
+                    continue;
+                for (int phi = 0; phi < step; phi++, j++) {
+                    const int s = j & 1;
+                    if (j >= 2 &&
+                        !mbar_wait_warp(empty0 + 8 * s, ((j >> 1) - 1) & 1, abort_flag, B.err, 2u))
+                        goto producer_done;
+                    const long long meta = ((long long)t * SC + ch) * step + phi;
+                    const int mu = pr.mu[meta], psi = pr.psi[meta];
+                    const int sres = ((mu % TC_Q) + TC_Q) % TC_Q;
+                    const long long r0 = (I0 + mu - sres) / TC_Q + pr.row_front;
+                    const uint32_t st = smem_u32(smem + (size_t)s * B.stage_bytes);
+                    if (lane == 0)
+                        mbar_expect_tx(full0 + 8 * s, (split ? 2u : 1u) * (data_bytes + wbytes));
+                    __syncwarp();
+                    const int cb = lane & 15, hl = lane >> 4;
+                    if (hl == 0 || split) {
+                        const uint16_t *src = (hl ? pr.g_lo : pr.g_hi) +
+                                              ((((long long)ch * step + psi) * TC_CB + cb) * pr.rows_total + r0) * 8;
+                        bulk_g2s(st + hl * data_bytes + cb * (uint32_t)R * 16, src, (uint32_t)R * 16,
+                                 full0 + 8 * s);
+                    }
+                    if (lane < (split ? 2 : 1)) {
+                        const uint16_t *src = (lane ? pr.w_lo : pr.w_hi) + meta * NW * 64;
+                        bulk_g2s(st + w_off + lane * wbytes, src, wbytes, full0 + 8 * s);
+                    }
                 }
             }
         }
     producer_done:
-        // wait (bounded) until the copies this warp issued have landed
         if (lane == 0)
             for (int k = max(0, j - 2); k < j; k++)
-                mbar_wait(full0 + 8 * (k & 1), (k >> 1) & 1, abort_flag, A.err, 0u);
+                mbar_wait(full0 + 8 * (k & 1), (k >> 1) & 1, abort_flag, B.err, 0u);
         __syncwarp();
     } else if (warp == 1) {
         // ---------------------------------------------------------- MMA issuer
         if (lane == 0) {
-            const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(NB >> 3) << 17) |
-                                   ((uint32_t)(TC_Q >> 4) << 24);
-            const uint32_t lbo_b = (uint32_t)R * 16;
             int j = 0, c = 0;
-            for (int ch = 0; ch < SC; ch++) {
-                if (w[ch] == 0.0f)
-                    continue;
-                const int d = c & 1;
-                if (c >= 2 && !mbar_wait(dempty0 + 8 * d, ((c >> 1) - 1) & 1, abort_flag, A.err, 4u))
+            for (long long q = 0;; q++) {
+                const int slot = (int)(q & 3);
+                if (!mbar_wait(ifull0 + 8 * slot, (uint32_t)((q >> 2) & 1), abort_flag, B.err, 32u))
                     goto mma_done;
-                tc_fence_after();
-                const uint32_t dt = tmem + (uint32_t)(d * NB);
-                uint32_t acc = 0;
-                for (int phi = 0; phi < step; phi++, j++) {
-                    const int s = j & 1;
-                    if (!mbar_wait(full0 + 8 * s, (j >> 1) & 1, abort_flag, A.err, 8u))
+                const long long item = ring[slot];
+                mbar_arrive(iempty0 + 8 * slot);
+                if (item >= total)
+                    break;
+                int p, tile, t;
+                decode_item(B, item, p, tile, t);
+                const TcProb &pr = B.prob[p];
+                const Problem &P = pr.P;
+                const int nb = pr.nb;
+                const long long I0 = (long long)tile * TC_Q * nb;
+                if (!(I0 < P.k_hi[t] && I0 + (long long)TC_Q * nb > P.k_lo[t]))
+                    continue;
+                // kind::f16 descriptor: F32 accumulate, BF16 A and B, K-major, N = nb, M = 128
+                const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(nb >> 3) << 17) |
+                                       ((uint32_t)(TC_Q >> 4) << 24);
+                const int SC = P.SC, step = P.step;
+                const uint32_t data_bytes = (uint32_t)TC_CB * pr.R * 16, wbytes = (uint32_t)pr.NW * 128;
+                const uint32_t w_off = (split ? 2u : 1u) * data_bytes;
+                const uint32_t lbo_b = (uint32_t)pr.R * 16;
+                const float *w = P.w + (size_t)t * SC;
+                for (int ch = 0; ch < SC; ch++) {
+                    if (w[ch] == 0.0f)
+                        continue;
+                    const int d = c & 1;
+                    if (c >= 2 && !mbar_wait(dempty0 + 8 * d, ((c >> 1) - 1) & 1, abort_flag, B.err, 4u))
                         goto mma_done;
                     tc_fence_after();
-                    const long long meta = ((long long)t * SC + ch) * step + phi;
-                    const int mu = A.mu[meta];
-                    const int sres = ((mu % TC_Q) + TC_Q) % TC_Q;
-                    const int lphi = (P.L - phi + step - 1) / step;
-                    const int k_first = sres & ~15;
-                    const int k_end = (sres + lphi + TC_Q - 1 + 15) & ~15;
-                    const uint32_t zhi = smem_u32(smem + (size_t)s * g.stage_bytes);
-                    const uint32_t zlo = zhi + data_bytes, whi = zhi + w_off, wlo = whi + wbytes;
-                    for (int k = k_first; k < k_end; k += 16) {
-                        const uint32_t wo = (uint32_t)(k >> 3) * 128u;
-                        const uint32_t bo = (uint32_t)((k & (TC_Q - 1)) >> 3) * lbo_b +
-                                            (uint32_t)(k / TC_Q) * 16u;
-                        const uint64_t ah = sdesc(whi + wo, 128, 128);
-                        const uint64_t bh = sdesc(zhi + bo, lbo_b, 128);
-                        mma_bf16(dt, ah, bh, idesc, acc);
-                        acc = 1;
-                        if (g.split) {
-                            mma_bf16(dt, ah, sdesc(zlo + bo, lbo_b, 128), idesc, 1);
-                            mma_bf16(dt, sdesc(wlo + wo, 128, 128), bh, idesc, 1);
+                    const uint32_t dt = tmem + (uint32_t)(d * TC_NB_MAX);
+                    uint32_t acc = 0;
+                    for (int phi = 0; phi < step; phi++, j++) {
+                        const int s = j & 1;
+                        if (!mbar_wait(full0 + 8 * s, (j >> 1) & 1, abort_flag, B.err, 8u))
+                            goto mma_done;
+                        tc_fence_after();
+                        const long long meta = ((long long)t * SC + ch) * step + phi;
+                        const int mu = pr.mu[meta];
+                        const int sres = ((mu % TC_Q) + TC_Q) % TC_Q;
+                        const int lphi = (P.L - phi + step - 1) / step;
+                        const int k_first = sres & ~15;
+                        const int k_end = (sres + lphi + TC_Q - 1 + 15) & ~15;
+                        const uint32_t zhi = smem_u32(smem + (size_t)s * B.stage_bytes);
+                        const uint32_t zlo = zhi + data_bytes, whi = zhi + w_off, wlo = whi + wbytes;
+                        for (int k = k_first; k < k_end; k += 16) {
+                            const uint32_t wo = (uint32_t)(k >> 3) * 128u;
+                            const uint32_t bo = (uint32_t)((k & (TC_Q - 1)) >> 3) * lbo_b +
+                                                (uint32_t)(k / TC_Q) * 16u;
+                            const uint64_t ah = sdesc(whi + wo, 128, 128);
+                            const uint64_t bh = sdesc(zhi + bo, lbo_b, 128);
+                            mma_bf16(dt, ah, bh, idesc, acc);
+                            acc = 1;
+                            if (split) {
+                                mma_bf16(dt, ah, sdesc(zlo + bo, lbo_b, 128), idesc, 1);
+                                mma_bf16(dt, sdesc(wlo + wo, 128, 128), bh, idesc, 1);
+                            }
                         }
+                        mma_commit(empty0 + 8 * s);
                     }
-                    mma_commit(empty0 + 8 * s);
+                    mma_commit(dfull0 + 8 * d);
+                    c++;
                 }
-                mma_commit(dfull0 + 8 * d);
-                c++;
             }
         mma_done:
-            // all MMAs issued by this thread complete before TMEM is released
             mma_commit(fin);
-            mbar_wait(fin, 0, abort_flag, A.err, 0u);
+            mbar_wait(fin, 0, abort_flag, B.err, 0u);
         }
         __syncwarp();
     } else if (warp >= 4) {
         // ---------------------------------------------------------- epilogue
-        constexpr int NC = NB / 2;
+        // TC_EPI_WARPS warps: warp w reads TMEM lane quarter w % 4 (rows
+        // 32*(w%4) + lane) and the NC columns [a0, a0 + NC) of the accumulators;
+        // the network sum of its outputs lives in TMEM columns 2*NB + [a0, a0 + NC).
+        constexpr int CH = 16;  // columns per TMEM access and per batch of statistics loads
         const int quarter = warp & 3;
-        const int half = (warp - 4) >> 2;
-        const int m = 32 * quarter + lane;  // accumulator row
-        const int b = TC_Q - 1 - m;         // phase of that row
-        const int a0 = half * NC;           // first lag block of this thread
-        // valid lag blocks: klo <= I0 + Q*a + b < khi
-        const long long kb = I0 + b;
-        const int a_lo = (int)max(0LL, (klo - kb + TC_Q - 1) / TC_Q) - a0;
-        const int a_hi = (int)min((long long)NB, (khi - kb + TC_Q - 1) / TC_Q) - a0;
-        const long long qs = (long long)TC_Q * step;
-        float S[NC];
-#pragma unroll
-        for (int i = 0; i < NC; i++)
-            S[i] = 0.0f;
+        const int cgroup = (warp - 4) >> 2;  // column group of this warp
+        const int m = 32 * quarter + lane;   // accumulator row
+        const int b = TC_Q - 1 - m;          // phase of that row
+        const uint32_t lane_base = tmem + ((uint32_t)(32 * quarter) << 16);
         int c = 0;
-        for (int ch = 0; ch < SC; ch++) {
-            const float wc = w[ch];
-            if (wc == 0.0f)
-                continue;
-            const int d = c & 1;
-            if (!mbar_wait_warp(dfull0 + 8 * d, (c >> 1) & 1, abort_flag, A.err, 16u))
-                break;
-            tc_fence_after();
-            const size_t row = (size_t)t * SC + ch;
-            const float sst = P.sst[row];
-            const float ts = P.normalize ? P.tsum[row] : 0.0f;
-            // statistics of the window of lag block a0 (advanced by qs per block)
-            const long long u0 = (kb + (long long)TC_Q * a0) * step + mo[ch];
-            const float *se = P.stat_e + (size_t)ch * P.N + u0;
-            const float *sm = P.normalize ? P.stat_m + (size_t)ch * P.N + u0 : se;
-            float *oc = P.out + ((size_t)t * P.n_corr + kb + (long long)TC_Q * a0) * SC + ch;
-            const uint32_t tbase = tmem + ((uint32_t)(32 * quarter) << 16) + (uint32_t)(d * NB + a0);
-#pragma unroll
-            for (int c0 = 0; c0 < NC; c0 += 16) {
-                float x[16];
-                tmem_ld16(tbase + c0, x);
-                tmem_wait_ld();
-                if (c0 + 16 >= NC) {
-                    tc_fence_before();
-                    __syncwarp();
-                    if (lane == 0)
-                        mbar_arrive(dempty0 + 8 * d);
+        for (long long q = 0;; q++) {
+            const int slot = (int)(q & 3);
+            long long item = total;
+            if (lane == 0) {
+                if (mbar_wait(ifull0 + 8 * slot, (uint32_t)((q >> 2) & 1), abort_flag, B.err, 64u)) {
+                    item = ring[slot];
+                    mbar_arrive(iempty0 + 8 * slot);
                 }
+            }
+            item = __shfl_sync(0xffffffffu, item, 0);
+            if (item >= total)
+                break;
+            int p, tile, t;
+            decode_item(B, item, p, tile, t);
+            const TcProb &pr = B.prob[p];
+            // per-item fields, once, into registers
+            const int nb = pr.nb;
+            const int NC = nb / (TC_EPI_WARPS / 4);  // columns of this thread (multiple of CH)
+            const int a0 = cgroup * NC;
+            const uint32_t s_cols = lane_base + (uint32_t)(2 * TC_NB_MAX + a0);
+            const int SC = pr.P.SC, step = pr.P.step, n_corr = pr.P.n_corr, N = pr.P.N;
+            const bool full = pr.P.normalize != 0, nsum = pr.P.network_sum != 0;
+            const float *__restrict__ stat_e = pr.P.stat_e;
+            const float *__restrict__ stat_m = pr.P.stat_m;
+            const float *__restrict__ sstp = pr.P.sst;
+            const float *__restrict__ tsump = pr.P.tsum;
+            float *outp = pr.P.out;
+            const long long I0 = (long long)tile * TC_Q * nb;
+            const int klo = pr.P.k_lo[t], khi = pr.P.k_hi[t];
+            const bool busy = I0 < khi && I0 + (long long)TC_Q * nb > klo;
+            // valid lag blocks of this thread: klo <= I0 + Q*a + b < khi
+            const long long kb = I0 + b;
+            const int a_lo = (int)max(0LL, (klo - kb + TC_Q - 1) / TC_Q) - a0;
+            const int a_hi = (int)min((long long)nb, (khi - kb + TC_Q - 1) / TC_Q) - a0;
+            const bool any = busy && a_hi > a_lo;
+            const long long qs = (long long)TC_Q * step;
+            const float *w = pr.P.w + (size_t)t * SC;
+            const int *mo = pr.P.mo + (size_t)t * SC;
+            bool first = true;
+            for (int ch = 0; busy && ch < SC; ch++) {
+                const float wc = w[ch];
+                if (wc == 0.0f)
+                    continue;
+                const int d = c & 1;
+                const size_t row = (size_t)t * SC + ch;
+                const float sst = sstp[row];
+                const float ts = full ? tsump[row] : 0.0f;
+                const long long u0 = (kb + (long long)TC_Q * a0) * step + mo[ch];
+                const float *__restrict__ se = stat_e + (size_t)ch * N + u0;
+                const float *__restrict__ sm = full ? stat_m + (size_t)ch * N + u0 : se;
+                float *oc = outp + ((size_t)t * n_corr + kb + (long long)TC_Q * a0) * SC + ch;
+                // statistics: all loads of a chunk issued together (indices clamped into the
+                // valid range) before any use; the first chunk before waiting for the accumulator
+                float e[CH], mm[CH];
+                auto load_chunk = [&](int c0) {
 #pragma unroll
-                for (int i = 0; i < 16; i++) {
-                    const int a = c0 + i;
-                    if (a >= a_lo && a < a_hi) {
-                        float num = x[i];
-                        if (P.normalize)
-                            num = fmaf(-sm[a * qs], ts, num);
-                        const float den = sst * se[a * qs];
-                        const float cc = den > kThreshold ? num / sqrtf(den) : 0.0f;
-                        if (P.network_sum)
-                            S[a] = fmaf(cc, wc, S[a]);
-                        else
+                    for (int i = 0; i < CH; i++) {
+                        const int ac = min(max(c0 + i, a_lo), a_hi - 1);
+                        e[i] = any ? __ldg(se + ac * qs) : 0.0f;
+                        mm[i] = (any && full) ? __ldg(sm + ac * qs) : 0.0f;
+                    }
+                };
+                load_chunk(0);
+                if (!mbar_wait_warp(dfull0 + 8 * d, (c >> 1) & 1, abort_flag, B.err, 16u))
+                    goto epilogue_done;
+                tc_fence_after();
+                const uint32_t dcols = lane_base + (uint32_t)(d * TC_NB_MAX + a0);
+#pragma unroll 1
+                for (int c0 = 0; c0 < NC; c0 += CH) {
+                    if (c0 > 0)
+                        load_chunk(c0);
+                    float x[CH], sv[CH];
+                    tmem_ldc<CH>(dcols + c0, x);
+                    if (nsum && !first)
+                        tmem_ldc<CH>(s_cols + c0, sv);
+                    tmem_wait_ld();
+                    if (c0 + CH >= NC) {
+                        tc_fence_before();
+                        __syncwarp();
+                        if (lane == 0)
+                            mbar_arrive(dempty0 + 8 * d);
+                    }
+#pragma unroll
+                    for (int i = 0; i < CH; i++) {
+                        const int a = c0 + i;
+                        const float num = full ? fmaf(-mm[i], ts, x[i]) : x[i];
+                        const float den = sst * e[i];
+                        float cc = den > kThreshold ? num * rsqrtf(den) : 0.0f;
+                        if (!(a >= a_lo && a < a_hi))
+                            cc = 0.0f;
+                        if (nsum)
+                            sv[i] = fmaf(cc, wc, first ? 0.0f : sv[i]);
+                        else if (a >= a_lo && a < a_hi)
                             oc[(size_t)a * TC_Q * SC] = cc;
+                    }
+                    if (nsum)
+                        tmem_stc<CH>(s_cols + c0, sv);
+                }
+                if (nsum)
+                    tmem_wait_st();
+                first = false;
+                c++;
+            }
+            if (nsum) {
+                float *o = outp + (size_t)t * n_corr + kb + (long long)TC_Q * a0;
+                const long long lim = n_corr - kb - (long long)TC_Q * a0;
+#pragma unroll 1
+                for (int c0 = 0; c0 < NC; c0 += CH) {
+                    float sv[CH];
+                    if (!first) {
+                        tmem_ldc<CH>(s_cols + c0, sv);
+                        tmem_wait_ld();
+                    }
+#pragma unroll
+                    for (int i = 0; i < CH; i++) {
+                        const int a = c0 + i;
+                        if ((long long)a * TC_Q < lim)
+                            o[(size_t)a * TC_Q] = (!first && a >= a_lo && a < a_hi) ? sv[i] : 0.0f;
                     }
                 }
             }
-            c++;
         }
-        if (P.network_sum) {
-            float *o = P.out + (size_t)t * P.n_corr + kb + (long long)TC_Q * a0;
-            const long long lim = P.n_corr - kb - (long long)TC_Q * a0;
-#pragma unroll
-            for (int a = 0; a < NC; a++)
-                if ((long long)a * TC_Q < lim)
-                    o[(size_t)a * TC_Q] = (a >= a_lo && a < a_hi) ? S[a] : 0.0f;
-        }
+    epilogue_done:;
     }
     tc_fence_before();
     __syncthreads();
@@ -544,54 +718,89 @@ __global__ void __launch_bounds__(TC_THREADS, 1) tc_kernel(const TcArgs A)
     }
 }
 
+// Self-test of the bounded waits: one CTA waits on an mbarrier that nothing
+// ever arrives on; the wait must give up after `limit_ns`, raise code 128 in
+// the error word and return, leaving the context usable.
+__global__ void wait_selftest_kernel(unsigned *err, unsigned long long limit_ns)
+{
+    __shared__ __align__(8) unsigned long long bar;
+    __shared__ int abort_flag;
+    if (threadIdx.x == 0) {
+        mbar_init(smem_u32(&bar), 1);
+        abort_flag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    if (threadIdx.x == 0)
+        mbar_wait(smem_u32(&bar), 0, &abort_flag, err, 128u, limit_ns);
+    __syncthreads();
+}
+
+int launch_wait_selftest(unsigned *err, unsigned ms, cudaStream_t s)
+{
+    wait_selftest_kernel<<<1, 32, 0, s>>>(err, (unsigned long long)ms * 1000000ull);
+    count_launch();
+    return check_launch("wait_selftest_kernel");
+}
+
 // ------------------------------------------------------------------ host side
-static int choose_nb(int L, int step, int split, int forced)
+struct TcShape {
+    int k_span, R, NW;
+    size_t stage;
+};
+
+static TcShape tc_shape(int L, int step, int split, int nb)
+{
+    TcShape g;
+    const int lphi = (L + step - 1) / step;
+    g.k_span = ((2 * TC_Q - 2 + lphi) + 15) & ~15;
+    g.R = nb + (g.k_span - 1) / TC_Q + 1;
+    g.NW = g.k_span / 8 + 16;
+    g.stage = (size_t)(split ? 2 : 1) * ((size_t)TC_CB * g.R * 16 + (size_t)g.NW * 128);
+    g.stage = (g.stage + 1023) & ~(size_t)1023;
+    return g;
+}
+
+constexpr size_t TC_BAR_BYTES = 256;
+
+// Largest tile (lag blocks per CTA tile) whose two pipeline stages fit in shared memory.
+int tc_choose_nb(int L, int step, int split, int forced)
 {
     const int cands[3] = {128, 64, 32};
     for (int i = 0; i < 3; i++) {
-        int nb = cands[i];
-        if (forced && nb != forced)
+        if (forced && cands[i] != forced)
             continue;
-        int lphi = (L + step - 1) / step;
-        int k_span = ((2 * TC_Q - 2 + lphi) + 15) & ~15;
-        int R = nb + (k_span - 1) / TC_Q + 1;
-        int NW = k_span / 8 + 16;
-        size_t stage = (size_t)(split ? 2 : 1) * ((size_t)TC_CB * R * 16 + (size_t)NW * 128);
-        if (2 * stage + 128 <= 227 * 1024)
-            return nb;
+        if (2 * tc_shape(L, step, split, cands[i]).stage + TC_BAR_BYTES <= 227 * 1024)
+            return cands[i];
     }
     return 0;
 }
 
-int launch_tc(const Problem &P, const float *data_for_tc, int precision, unsigned *err, Scratch &ws,
-              cudaStream_t s, int forced_nb)
+// Preprocessing of one search for the tensor-core kernel: bf16 hi/lo data
+// streams and template blocks, in scratch owned by `ws`.  Fills `out`.
+int tc_prepare(const Problem &P, const float *data_for_tc, int split, int nb, int tg, Scratch &ws,
+               cudaStream_t s, TcProb *out)
 {
     int rc;
-    const int split = precision == FMF_PREC_SPLIT_BF16;
     const int step = P.step, L = P.L;
-    const int NB = choose_nb(L, step, split, forced_nb);
-    if (NB == 0)
-        return set_error(FMF_ERR_SMEM, "template length %d, step %d: tensor-core tile does not fit shared memory",
-                         L, step);
-    TcGeom g;
-    g.NB = NB;
-    g.split = split;
-    const int lphi = (L + step - 1) / step;
-    g.k_span = ((2 * TC_Q - 2 + lphi) + 15) & ~15;
-    g.R = NB + (g.k_span - 1) / TC_Q + 1;
-    g.NW = g.k_span / 8 + 16;
-    g.stage_bytes = (int)((size_t)(split ? 2 : 1) * ((size_t)TC_CB * g.R * 16 + (size_t)g.NW * 128));
-    g.stage_bytes = (g.stage_bytes + 1023) & ~1023;
-    g.smem = 2 * (size_t)g.stage_bytes + 128;
-    g.n_tiles = (int)((P.n_corr + (long long)TC_Q * NB - 1) / ((long long)TC_Q * NB));
-    // Stream rows a tile can touch.  A CTA runs only when its tile holds a
-    // valid output k of its template, i.e. k*step + mo >= 0 and
+    const TcShape g = tc_shape(L, step, split, nb);
+    TcProb pr;
+    pr.P = P;
+    pr.R = g.R;
+    pr.NW = g.NW;
+    pr.n_tiles = (int)((P.n_corr + (long long)TC_Q * nb - 1) / ((long long)TC_Q * nb));
+    pr.tg = tg > 0 ? tg : TC_TG;
+    pr.nb = nb;
+    // Stream rows a tile can touch.  An item is processed only when its tile
+    // holds a valid output k of its template, i.e. k*step + mo >= 0 and
     // k*step + mo + L <= N for every channel; hence its first row
     // r0 = (I0 + mu - s)/Q lies in [-(NB + 2), (N/step + 1)/Q + 1] whatever the
     // moveouts are, and rows [r0, r0 + R) stay inside the padded stream.
-    g.row_front = NB + 3;
-    g.rows_total = g.row_front + (int)(((long long)P.N / step + 2) / TC_Q) + 2 + g.R + 1;
-    const size_t g_elems = (size_t)P.SC * step * TC_CB * g.rows_total * 8;
+    pr.row_front = nb + 3;
+    pr.rows_total = pr.row_front + (int)(((long long)P.N / step + 2) / TC_Q) + 2 + g.R + 1;
+    pr.item_begin = 0;
+
+    const size_t g_elems = (size_t)P.SC * step * TC_CB * pr.rows_total * 8;
     const size_t w_elems = (size_t)P.T * P.SC * step * g.NW * 64;
     const size_t n_meta = (size_t)P.T * P.SC * step;
     uint16_t *g_hi, *g_lo = nullptr, *w_hi, *w_lo = nullptr;
@@ -602,55 +811,97 @@ int launch_tc(const Problem &P, const float *data_for_tc, int precision, unsigne
         (split && (rc = ws.get(&w_lo, w_elems, "bf16 template blocks (lo)"))) ||
         (rc = ws.get(&mu, n_meta, "phase moveouts")) || (rc = ws.get(&psi, n_meta, "phase streams")))
         return rc;
+    const long long n = (long long)P.SC * step * TC_CB * pr.rows_total;
+    tc_data_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(data_for_tc, P.N, P.SC, step, pr.rows_total,
+                                                               pr.row_front, g_hi, g_lo);
+    const long long m = (long long)P.T * P.SC * step * g.NW * 8;
+    tc_template_kernel<<<(unsigned)((m + 255) / 256), 256, 0, s>>>(P.tpl, P.mo, P.T, P.SC, L, step, g.NW,
+                                                                   w_hi, w_lo, mu, psi);
+    count_launch(2);
+    if ((rc = check_launch("tensor-core preprocessing")))
+        return rc;
+    pr.g_hi = g_hi;
+    pr.g_lo = g_lo;
+    pr.w_hi = w_hi;
+    pr.w_lo = w_lo;
+    pr.mu = mu;
+    pr.psi = psi;
+    *out = pr;
+    return FMF_OK;
+}
 
-    {
-        long long n = (long long)P.SC * step * TC_CB * g.rows_total;
-        tc_data_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(data_for_tc, P.N, P.SC, step,
-                                                                   g.rows_total, g.row_front, g_hi, g_lo);
-        long long m = (long long)P.T * P.SC * step * g.NW * 8;
-        tc_template_kernel<<<(unsigned)((m + 255) / 256), 256, 0, s>>>(P.tpl, P.mo, P.T, P.SC, L, step,
-                                                                       g.NW, w_hi, w_lo, mu, psi);
-        count_launch(2);
-        if ((rc = check_launch("tensor-core preprocessing")))
-            return rc;
-    }
+static int n_sms()
+{
+    int dev = 0, n = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0)
+        n = 148;
+    cudaGetLastError();
+    return n;
+}
 
-    TcArgs A;
-    A.P = P;
-    A.g_hi = g_hi;
-    A.g_lo = g_lo;
-    A.w_hi = w_hi;
-    A.w_lo = w_lo;
-    A.mu = mu;
-    A.psi = psi;
-    A.err = err;
-    A.g = g;
-    const long long ctas = (long long)g.n_tiles * P.T;
-    if (ctas > 0x7fffffffLL)
-        return set_error(FMF_ERR_ARG, "too many tiles for one launch");
-    cudaError_t e;
-    switch (NB) {
-    case 128:
-        e = cudaFuncSetAttribute(tc_kernel<128>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)g.smem);
-        if (e == cudaSuccess)
-            tc_kernel<128><<<(unsigned)ctas, TC_THREADS, g.smem, s>>>(A);
-        break;
-    case 64:
-        e = cudaFuncSetAttribute(tc_kernel<64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)g.smem);
-        if (e == cudaSuccess)
-            tc_kernel<64><<<(unsigned)ctas, TC_THREADS, g.smem, s>>>(A);
-        break;
-    default:
-        e = cudaFuncSetAttribute(tc_kernel<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)g.smem);
-        if (e == cudaSuccess)
-            tc_kernel<32><<<(unsigned)ctas, TC_THREADS, g.smem, s>>>(A);
-        break;
+// One persistent launch over the tile queue of `n` prepared searches (n <= TC_MAX_PROBS).
+// `queue` is a device counter that this call zeroes on `s` before the launch.
+int tc_run(const TcProb *probs, int n, int split, unsigned long long *queue, unsigned *err, cudaStream_t s)
+{
+    if (n < 1 || n > TC_MAX_PROBS)
+        return set_error(FMF_ERR_ARG, "a persistent launch takes 1..%d searches", TC_MAX_PROBS);
+    static thread_local TcBatch Bh;  // large; built on the host for the launch only
+    TcBatch &B = Bh;
+    long long items = 0;
+    size_t stage = 0;
+    for (int i = 0; i < n; i++) {
+        B.prob[i] = probs[i];
+        B.prob[i].item_begin = items;
+        items += (long long)probs[i].n_tiles * probs[i].P.T;
+        const size_t st = tc_shape(probs[i].P.L, probs[i].P.step, split, probs[i].nb).stage;
+        stage = st > stage ? st : stage;
     }
+    B.n_probs = n;
+    B.split = split;
+    B.stage_bytes = (int)stage;
+    B.total_items = items;
+    B.queue = queue;
+    B.err = err;
+    // more than half of the SM's shared memory: one CTA per SM, so that the
+    // CTA's 512-column TMEM allocation never waits for another CTA
+    size_t smem = 2 * stage + TC_BAR_BYTES;
+    if (smem < 120 * 1024)
+        smem = 120 * 1024;
+    if (smem > 227 * 1024)
+        return set_error(FMF_ERR_SMEM, "tensor-core stages need %zu bytes of shared memory", smem);
+    cudaError_t e = cudaMemsetAsync(queue, 0, sizeof(unsigned long long), s);
     if (e != cudaSuccess)
-        return set_error(FMF_ERR_CUDA, "tc_kernel shared memory (%zu bytes): %s", g.smem,
+        return set_error(FMF_ERR_CUDA, "clearing the tile queue: %s", cudaGetErrorString(e));
+    const unsigned grid = (unsigned)(items < n_sms() ? (items > 0 ? items : 1) : n_sms());
+    e = cudaFuncSetAttribute(tc_persistent, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess)
+        return set_error(FMF_ERR_CUDA, "tc_persistent shared memory (%zu bytes): %s", smem,
                          cudaGetErrorString(e));
+    tc_persistent<<<grid, TC_THREADS, smem, s>>>(B);
     count_launch();
-    return check_launch("tc_kernel");
+    return check_launch("tc_persistent");
+}
+
+size_t tc_prob_size() { return sizeof(TcProb); }
+
+// Single search: preprocessing + one persistent launch.
+int launch_tc(const Problem &P, const float *data_for_tc, int precision, unsigned *err, Scratch &ws,
+              cudaStream_t s, int forced_nb, int template_group)
+{
+    int rc;
+    const int split = precision == FMF_PREC_SPLIT_BF16;
+    const int nb = tc_choose_nb(P.L, P.step, split, forced_nb);
+    if (nb == 0)
+        return set_error(FMF_ERR_SMEM, "template length %d, step %d: tensor-core tile does not fit shared memory",
+                         P.L, P.step);
+    TcProb pr;
+    if ((rc = tc_prepare(P, data_for_tc, split, nb, template_group, ws, s, &pr)))
+        return rc;
+    unsigned long long *queue;
+    if ((rc = ws.get(&queue, 1, "tile queue")))
+        return rc;
+    return tc_run(&pr, 1, split, queue, err, s);
 }
 
 }  // namespace fmf

@@ -20,7 +20,7 @@ import ctypes as ct
 
 import numpy as np
 
-from . import _lib
+from . import _lib, autotune
 
 CPU_LOADED = False
 _LIB, _LIB_ERROR = _lib.try_load()
@@ -191,11 +191,12 @@ def matched_filter(templates, moveouts, weights, data, step,
     if precision == "fp32":
         st = lib.fmf_matched_filter(*args)
     else:
+        flags = autotune.flags_for(pp["L"], pp["step"], S * C, normalize, precision)
         st = lib.fmf_matched_filter_ex(
             pp["templates"].ctypes.data, pp["sst"].ctypes.data, pp["moveouts"].ctypes.data,
             pp["data"].ctypes.data, pp["weights"].ctypes.data, pp["step"], pp["L"], pp["N"],
             T, S, C, n_corr, cc.ctypes.data, pp["normalize"], int(bool(network_sum)),
-            _lib.PRECISIONS[precision], 0, None)
+            _lib.PRECISIONS[precision], flags, None)
     _lib.check(st, lib)
     cc = cc.reshape(T, n_corr) if network_sum else cc.reshape(T, n_corr, S, C)
     _zero_report(cc, pp["moveouts"], pp["weights"], T, n_corr, pp["step"],
@@ -226,11 +227,12 @@ def matched_filter_device(templates, sum_square_templates, moveouts, weights, da
     if stream is None:
         stream = torch.cuda.current_stream()
     handle = stream.cuda_stream if hasattr(stream, "cuda_stream") else int(stream)
+    flags = _lib.FLAG_DEVICE_POINTERS | autotune.flags_for(L, step, S * C, normalize, precision)
     st = lib.fmf_matched_filter_ex(
         templates.data_ptr(), sum_square_templates.data_ptr(), moveouts.data_ptr(),
         data.data_ptr(), weights.data_ptr(), int(step), L, N, T, S, C, n_corr,
         out.data_ptr(), 1 if normalize == "full" else 0, int(bool(network_sum)),
-        _lib.PRECISIONS[precision], _lib.FLAG_DEVICE_POINTERS, handle)
+        _lib.PRECISIONS[precision], flags, handle)
     _lib.check(st, lib)
     return lib.fmf_last_launch_count()
 
@@ -284,3 +286,55 @@ def test_matched_filter(n_templates=1, n_stations=1, n_components=1,
           "{} samples ({} step) ran in {:.3f}s".format(
               arch, n_templates, n_stations, n_components, n_data, step, run_time))
     return templates, moveouts, data, step, cc_sum, run_time
+
+
+class Batch:
+    """Many independent searches run as one CUDA graph (C ABI fmf_batch_*).
+
+    ``add`` takes canonical, contiguous torch CUDA tensors (as
+    ``matched_filter_device``) and keeps references to them; ``run`` launches
+    every search asynchronously on ``stream`` -- preprocessing, then one
+    persistent tensor-core launch over a shared tile queue (or the plain
+    kernel per search for precision='fp32').  The graph is captured on the
+    first ``run`` after the last ``add`` and replayed afterwards.
+    """
+
+    def __init__(self, precision="split_bf16", lag_blocks=0, template_group=0):
+        self._lib = _require_lib()
+        self._h = ct.c_void_p()
+        _lib.check(self._lib.fmf_batch_create(ct.byref(self._h), _lib.PRECISIONS[precision]),
+                   self._lib)
+        self._keep = []
+        if lag_blocks or template_group:
+            _lib.check(self._lib.fmf_batch_set_tiles(self._h, lag_blocks, template_group), self._lib)
+
+    def add(self, templates, sum_square_templates, moveouts, weights, data, step, out,
+            normalize="short", network_sum=True):
+        T, S, C, L = templates.shape
+        N = data.shape[-1]
+        st = self._lib.fmf_batch_add(
+            self._h, templates.data_ptr(), sum_square_templates.data_ptr(), moveouts.data_ptr(),
+            data.data_ptr(), weights.data_ptr(), int(step), L, N, T, S, C, out.shape[1],
+            out.data_ptr(), 1 if normalize == "full" else 0, int(bool(network_sum)))
+        _lib.check(st, self._lib)
+        self._keep.append((templates, sum_square_templates, moveouts, weights, data, out))
+
+    def run(self, stream=None):
+        import torch
+        if stream is None:
+            stream = torch.cuda.current_stream()
+        handle = stream.cuda_stream if hasattr(stream, "cuda_stream") else int(stream)
+        _lib.check(self._lib.fmf_batch_run(self._h, handle), self._lib)
+        return self._lib.fmf_batch_launch_count(self._h)
+
+    def close(self):
+        if self._h:
+            self._lib.fmf_batch_destroy(self._h)
+            self._h = ct.c_void_p()
+            self._keep = []
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

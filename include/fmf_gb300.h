@@ -52,6 +52,10 @@ extern "C" {
 
 /* flags of fmf_matched_filter_ex */
 #define FMF_FLAG_DEVICE_POINTERS 1 /* all array arguments are device pointers */
+/* tensor-core tile: lag blocks of 128 outputs per tile (32, 64 or 128; default: largest that fits) */
+#define FMF_FLAG_TILE(lag_blocks) ((((lag_blocks) / 16) & 0xff) << 8)
+/* tensor-core tile queue: templates interleaved per group of items (1..255; default 16) */
+#define FMF_FLAG_TEMPLATE_GROUP(n) (((n) & 0xff) << 16)
 
 /*
  * Drop-in for the reference GPU entry point
@@ -126,6 +130,35 @@ FMF_API int fmf_matched_filter_noalloc(const float *templates, const float *sum_
                                        size_t n_corr, float *cc_out, int normalize, int sum_cc_mode,
                                        void *stream);
 
+/*
+ * Batches of independent searches (no reference counterpart; the reference
+ * runs one search per call, matched_filter.cu:171-399).  A batch records
+ * searches of any sizes -- device pointers, the same 15 arguments as
+ * fmf_matched_filter -- and runs them all as one CUDA graph: the searches'
+ * preprocessing, then one persistent tensor-core launch per 64 searches over
+ * a shared tile queue (FMF_PREC_SPLIT_BF16 / FMF_PREC_BF16) or the plain kernel
+ * per search (FMF_PREC_FP32).  The graph is captured by the first
+ * fmf_batch_run after the last fmf_batch_add and replayed by later runs,
+ * which read the input buffers anew.  fmf_batch_run is asynchronous on
+ * `stream` (NULL = legacy default stream).  A batch belongs to the device
+ * that was current at fmf_batch_create.
+ */
+typedef struct fmf_batch fmf_batch;
+FMF_API int fmf_batch_create(fmf_batch **batch, int precision);
+FMF_API int fmf_batch_add(fmf_batch *batch, const float *templates, const float *sum_square_templates,
+                          const int *moveouts, const float *data, const float *weights, size_t step,
+                          size_t n_samples_template, size_t n_samples_data, size_t n_templates,
+                          size_t n_stations, size_t n_components, size_t n_corr, float *cc_out,
+                          int normalize, int sum_cc_mode);
+/* Tensor-core tile shape of the batch: lag blocks per tile (0 = largest that
+ * fits every search, else 32/64/128) and templates interleaved per group of
+ * tile-queue items (0 = 16). */
+FMF_API int fmf_batch_set_tiles(fmf_batch *batch, int lag_blocks, int template_group);
+FMF_API int fmf_batch_run(fmf_batch *batch, void *stream);
+/* Kernel launches in one run of the batch graph (known after the first run). */
+FMF_API int fmf_batch_launch_count(const fmf_batch *batch);
+FMF_API int fmf_batch_destroy(fmf_batch *batch);
+
 /* Copies the calling thread's last error message (NUL-terminated, truncated
  * to len) and returns its status.  The reference printed and exited instead
  * (matched_filter.cu:30-39, 236-242, 286-299). */
@@ -143,6 +176,12 @@ FMF_API int fmf_last_launch_count(void);
  * host-pointer entry points check this themselves).  No reference
  * counterpart. */
 FMF_API int fmf_device_errors(void);
+
+/* Self-test of the bounded device waits (no reference counterpart): runs
+ * one CTA that waits on a barrier nothing ever arrives on, with a limit of
+ * `ms` milliseconds (1..5000).  Returns FMF_ERR_TIMEOUT when the wait gave up
+ * and reported it as the library's kernels do; the device stays usable. */
+FMF_API int fmf_selftest_wait_timeout(unsigned ms);
 
 /* Event timing (no reference counterpart; used by the benchmark).
  * fmf_timing_begin() makes every later call on this thread record CUDA

@@ -16,9 +16,11 @@ HEADER = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))
 
 
 def declared_functions():
+    """Names of the functions the header exports (declarations marked FMF_API)."""
     src = open(HEADER).read()
     src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
-    return sorted(set(re.findall(r"\b([A-Za-z_]\w*)\s*\([^;{]*\)\s*;", src)))
+    src = "\n".join(l for l in src.splitlines() if not l.lstrip().startswith("#"))
+    return sorted(set(re.findall(r"FMF_API[^;(]*?\b([A-Za-z_]\w*)\s*\(", src)))
 
 
 @pytest.fixture(scope="module")
