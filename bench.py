@@ -419,6 +419,19 @@ def tc_executed_macs(cfg, nb=None):
     return total, nb
 
 
+def profiled_traffic(kernel_prefix, cfg):
+    """DRAM bytes per launch for this workload, scaled from the committed ncu
+    summary of the kernel (profiles/<kernel>_*.md, line
+    'traffic_bytes_per_template_lag: X'): X * templates * lags, or None."""
+    import glob
+    for path in sorted(glob.glob(os.path.join(HERE, "profiles", kernel_prefix + "_*.md"))):
+        for line in open(path):
+            if line.startswith("traffic_bytes_per_template_lag:"):
+                per = float(line.split(":")[1])
+                return per * cfg["templates"].shape[0] * cfg["n_corr"], os.path.basename(path)
+    return None, None
+
+
 def roofline(cfg, precision, kern_ms, prep_ms):
     peaks, src = load_peaks()
     algo_tflops = 2.0 * cfg["macs"] / (kern_ms / 1e3) / 1e12
@@ -434,8 +447,10 @@ def roofline(cfg, precision, kern_ms, prep_ms):
         products = 3 if precision == "split_bf16" else 1
         ex, nb = tc_executed_macs(cfg)
         executed = 2.0 * ex * products / (kern_ms / 1e3) / 1e12
+        traffic, tsrc = profiled_traffic("tc_persistent", cfg)
         roof = {"bound": "tensor", "achieved": algo_tflops, "peak": peak, "unit": "TFLOP/s",
-                "frac": algo_tflops / peak, "traffic": None, "kernel": "tc_kernel<%d>" % nb,
+                "frac": algo_tflops / peak, "traffic": traffic, "traffic_source": tsrc,
+                "kernel": "tc_persistent (nb=%d)" % nb,
                 "peak_source": "%s bf16_tflops_sustained (cuBLAS bf16 GEMM, seconds-long loop)"
                                % src,
                 "executed_tflops": executed, "executed_frac": executed / peak,

@@ -53,7 +53,8 @@ EXPORTS = ("fmf_matched_filter", "matched_filter", "fmf_matched_filter_ex",
            "fmf_release_cache", "fmf_timing_begin", "fmf_timing_end",
            "fmf_device_errors", "fmf_matched_filter_noalloc", "fmf_batch_create",
            "fmf_batch_add", "fmf_batch_set_tiles", "fmf_batch_run", "fmf_batch_launch_count",
-           "fmf_batch_destroy", "fmf_selftest_wait_timeout")
+           "fmf_batch_destroy", "fmf_selftest_wait_timeout", "fmf_matched_filter_variable",
+           "fmf_matched_filter_variable_ex")
 
 
 class FMFError(RuntimeError):
@@ -90,6 +91,9 @@ def load(path=None):
     lib.fmf_timing_begin.restype = ct.c_int
     lib.fmf_device_errors.restype = ct.c_int
     lib.fmf_selftest_wait_timeout.argtypes = [ct.c_uint]
+    lib.fmf_matched_filter_variable_ex.argtypes = [ct.c_void_p] * 5 + [_sz, ct.c_void_p] + [_sz] * 5 + [
+        ct.c_void_p, ct.c_int, ct.c_int, ct.c_void_p]
+    lib.fmf_matched_filter_variable_ex.restype = ct.c_int
     lib.fmf_selftest_wait_timeout.restype = ct.c_int
     lib.fmf_batch_create.argtypes = [ct.POINTER(ct.c_void_p), ct.c_int]
     lib.fmf_batch_create.restype = ct.c_int

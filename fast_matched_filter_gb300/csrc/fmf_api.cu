@@ -12,6 +12,7 @@
 #include <cstring>
 #include <cstdlib>
 #include <climits>
+#include <vector>
 
 #include "fmf_common.cuh"
 
@@ -250,6 +251,10 @@ int prepare_problem(const Args &a, Scratch &ws, cudaStream_t s, Problem *Pout, c
     P.n_corr = (int)a.n_corr;
     P.normalize = a.normalize;
     P.network_sum = a.sum_mode != 0;
+    P.ntap = nullptr;
+    P.pre2 = nullptr;
+    P.pre1 = nullptr;
+    P.zweight = nullptr;
 
     if (!P.network_sum) {
         size_t bytes = (size_t)T * a.n_corr * SC * sizeof(float);
@@ -261,8 +266,7 @@ int prepare_problem(const Args &a, Scratch &ws, cudaStream_t s, Problem *Pout, c
     return FMF_OK;
 }
 
-// Plain FP32 form over all templates (grid.y carries the template index:
-// slices of 65535 templates).
+// Plain FP32 form over all templates, in launches of at most 65535 templates.
 int launch_plain_all(const Problem &P, cudaStream_t s)
 {
     int rc;
@@ -320,6 +324,104 @@ static int run_device(const Args &a, cudaStream_t s)
 }
 
 // ---------------------------------------------------------------- host-pointer path
+// Templates [t0, t0 + nt) of a prepared problem.
+static Problem problem_subset(const Problem &P, int t0, int nt)
+{
+    Problem Q = P;
+    const size_t o = (size_t)t0 * P.SC;
+    Q.tpl += o * P.L;
+    Q.sst += o;
+    if (Q.tsum)
+        Q.tsum += o;
+    Q.mo += o;
+    Q.w += o;
+    Q.k_lo += t0;
+    Q.k_hi += t0;
+    Q.out += (size_t)t0 * P.n_corr * (P.network_sum ? 1 : P.SC);
+    Q.T = nt;
+    return Q;
+}
+
+// Device-resident search whose result is copied to `host_out` in template
+// chunks on a second stream, each chunk's copy overlapping the next chunk's
+// kernel.  Preprocessing is done once for all templates.
+static int run_streamed(const Args &d, float *host_out, cudaStream_t s)
+{
+    int rc;
+    Scratch ws(s);
+    Problem P;
+    const float *data_for_tc = nullptr;
+    if ((rc = prepare_problem(d, ws, s, &P, &data_for_tc)))
+        return rc;
+    const size_t row = (size_t)P.n_corr * (P.network_sum ? 1 : P.SC);  // floats per template
+    const size_t out_bytes = (size_t)P.T * row * sizeof(float);
+    const int n_chunks = out_bytes < ((size_t)64 << 20) ? 1 : (P.T < 8 ? P.T : 8);
+    const int per = (P.T + n_chunks - 1) / n_chunks;
+    unsigned *err = nullptr;
+    std::vector<unsigned char> tcfull;
+    int split = 0;
+    if (d.precision != FMF_PREC_FP32) {
+        if ((rc = device_error_word(&err)))
+            return rc;
+        split = d.precision == FMF_PREC_SPLIT_BF16;
+        const char *nb_env = getenv("FMF_TC_NB");
+        int forced = nb_env ? atoi(nb_env) : 0;
+        if (d.flags & 0xff00)
+            forced = ((d.flags >> 8) & 0xff) * 16;
+        const int nb = tc_choose_nb(P.L, P.step, split, forced);
+        if (nb == 0)
+            return set_error(FMF_ERR_SMEM, "template length %d, step %d: tensor-core tile does not fit "
+                                           "shared memory", P.L, P.step);
+        tcfull.resize(tc_prob_size());
+        if ((rc = tc_prepare(P, data_for_tc, split, nb, (d.flags >> 16) & 0xff, ws, s,
+                             reinterpret_cast<TcProb *>(tcfull.data()))))
+            return rc;
+    }
+    cudaStream_t s2 = nullptr;
+    cudaEvent_t ev[9] = {};
+    cudaError_t e = cudaStreamCreateWithFlags(&s2, cudaStreamNonBlocking);
+    for (int i = 0; i <= n_chunks && e == cudaSuccess; i++)
+        e = cudaEventCreateWithFlags(&ev[i], cudaEventDisableTiming);
+    if (e == cudaSuccess) {
+        for (int c = 0; c < n_chunks && rc == FMF_OK; c++) {
+            const int t0 = c * per, nt = P.T - t0 < per ? P.T - t0 : per;
+            if (nt <= 0)
+                break;
+            if (!tcfull.empty()) {
+                std::vector<unsigned char> sub(tc_prob_size());
+                unsigned long long *queue;
+                tc_subset(reinterpret_cast<const TcProb *>(tcfull.data()), t0, nt,
+                          reinterpret_cast<TcProb *>(sub.data()));
+                if (!(rc = ws.get(&queue, 1, "tile queue")))
+                    rc = tc_run(reinterpret_cast<const TcProb *>(sub.data()), 1, split, queue, err, s);
+            } else {
+                rc = launch_plain_all(problem_subset(P, t0, nt), s);
+            }
+            if (rc)
+                break;
+            const size_t off = (size_t)t0 * row, n = (size_t)nt * row * sizeof(float);
+            if ((e = cudaEventRecord(ev[c], s)) != cudaSuccess ||
+                (e = cudaStreamWaitEvent(s2, ev[c], 0)) != cudaSuccess ||
+                (e = cudaMemcpyAsync(host_out + off, P.out + off, n, cudaMemcpyDeviceToHost, s2)) !=
+                    cudaSuccess)
+                break;
+        }
+        // scratch is freed on s: let s wait for the last copy
+        if (e == cudaSuccess && (e = cudaEventRecord(ev[n_chunks], s2)) == cudaSuccess)
+            e = cudaStreamWaitEvent(s, ev[n_chunks], 0);
+    }
+    if (e != cudaSuccess && rc == FMF_OK)
+        rc = cuda_status(e, "streaming the result to the host");
+    if (s2) {
+        cudaStreamSynchronize(s2);
+        cudaStreamDestroy(s2);
+    }
+    for (int i = 0; i <= n_chunks; i++)
+        if (ev[i])
+            cudaEventDestroy(ev[i]);
+    return rc;
+}
+
 static int run_host(const Args &a, cudaStream_t s)
 {
     int rc;
@@ -345,10 +447,7 @@ static int run_host(const Args &a, cudaStream_t s)
         d.data = buf[3];
         d.w = buf[4];
         d.out = buf[5];
-        if ((rc = run_device(d, s)))
-            return rc;
-        if ((rc = cuda_status(cudaMemcpyAsync(a.out, d.out, n[5] * 4, cudaMemcpyDeviceToHost, s),
-                              "copying the result to the host")))
+        if ((rc = run_streamed(d, a.out, s)))
             return rc;
     }
     if ((rc = cuda_status(cudaStreamSynchronize(s), "matched filter")))

@@ -38,6 +38,11 @@ struct Problem {
     int T, SC, L, N, step, n_corr;
     int normalize;        // 0 short, 1 full
     int network_sum;      // 1 weighted sum over channels, 0 per channel
+    // Per-channel template lengths (Fisher-z network sum), else null:
+    const int *ntap;      // (T, SC) taps of each channel (templates zero-padded to L)
+    const double *pre2;   // (SC, N+1) FP64 prefix sums of d^2 (centred d for full)
+    const double *pre1;   // (SC, N+1) FP64 prefix sums of centred d (full), else null
+    const float *zweight; // (T, SC) Fisher-z weight of each channel
 };
 
 }  // namespace fmf
@@ -103,6 +108,7 @@ int tc_prepare(const Problem &P, const float *data_for_tc, int split, int nb, in
 int tc_run(const TcProb *probs, int n, int split, unsigned long long *queue, unsigned *err,
            cudaStream_t s);
 size_t tc_prob_size();
+void tc_subset(const TcProb *full, int t0, int nt, TcProb *out);
 int launch_plain(const Problem &P, cudaStream_t stream);
 int launch_plain_all(const Problem &P, cudaStream_t stream);
 int device_error_word(unsigned **out);

@@ -197,6 +197,10 @@ extern "C" int fmf_matched_filter_noalloc(const float *templates, const float *s
     P.n_corr = (int)n_corr;
     P.normalize = normalize;
     P.network_sum = sum_cc_mode != 0;
+    P.ntap = nullptr;
+    P.pre2 = nullptr;
+    P.pre1 = nullptr;
+    P.zweight = nullptr;
     for (int t0 = 0; t0 < T; t0 += 65535) {
         Problem Q = P;
         const int nt = T - t0 < 65535 ? T - t0 : 65535;

@@ -4,7 +4,8 @@
 // (matched_filter.cu:42-168) and the per-lag loop of the CPU library
 // (matched_filter.c:78-92, 416-455, 611-657).
 //
-// One CTA = one template x one tile of 4096 consecutive output indices; it
+// One CTA = one template x one tile of 4096 consecutive output indices (CTAs
+// ordered template-fastest); it
 // walks the template's channels in station-major / component-minor order,
 // skipping channels of weight 0, and keeps the weighted network sum of its
 // 4096 outputs on chip for the whole walk.  Each thread owns 16 consecutive
@@ -28,6 +29,8 @@
 // den, cc = num / sqrt(den), network sum acc = fma(cc, w, acc) in channel
 // order (the reference's accumulation, matched_filter.c:450).  Outputs
 // outside [k_lo, k_hi) are written as 0.
+#include <cfloat>
+
 #include "fmf_common.cuh"
 
 namespace fmf {
@@ -133,8 +136,10 @@ plain_kernel(const Problem P, const PlainGeom g)
     extern __shared__ __align__(16) float smem[];
     float *net = smem + 2 * g.stage_floats;  // [PL_R][PL_THREADS]
 
-    const int t = blockIdx.y;
-    const long long k0 = (long long)blockIdx.x * PL_TILE;
+    // templates fastest: the CTAs running at any time share a few tiles, so
+    // their data windows and window statistics are read from L2
+    const int t = (int)(blockIdx.x % (unsigned)P.T);
+    const long long k0 = (long long)(blockIdx.x / (unsigned)P.T) * PL_TILE;
     const int klo = P.k_lo[t], khi = P.k_hi[t];
     const int tid = threadIdx.x;
     const float *w = P.w + (size_t)t * P.SC;
@@ -166,7 +171,39 @@ plain_kernel(const Problem P, const PlainGeom g)
             cp_async_wait1();
             __syncthreads();
             compute_phase(smem + b * g.stage_floats, g, acc);
-            if (phi == P.step - 1) {
+            if (phi == P.step - 1 && P.ntap) {
+                // per-channel template length: FP64 window sums of that length,
+                // the 'precise' threshold (on the square root, matched_filter.c:650-652)
+                // and a Fisher-z network sum (matched_filter.c:596-601)
+                const size_t row = (size_t)t * P.SC + ch;
+                const float sst = P.sst[row], zw = P.zweight[row];
+                const float ts = P.normalize ? P.tsum[row] : 0.0f;
+                const int n = P.ntap[row];
+                const double *p2 = P.pre2 + (size_t)ch * (P.N + 1);
+                const double *p1 = P.normalize ? P.pre1 + (size_t)ch * (P.N + 1) : nullptr;
+#pragma unroll
+                for (int r = 0; r < PL_R; r++) {
+                    long long k = k0 + tid * PL_R + r;
+                    if (k >= klo && k < khi) {
+                        const long long u = k * P.step + mo[ch];
+                        const double s2 = p2[u + n] - p2[u];
+                        float num = acc[r], ssd;
+                        if (P.normalize) {
+                            const double s1 = p1[u + n] - p1[u];
+                            const double v = s2 - s1 * s1 / (double)n;
+                            num = fmaf(-(float)(s1 / (double)n), ts, num);
+                            ssd = (float)(v > 0.0 ? v : 0.0);
+                        } else {
+                            ssd = (float)s2;
+                        }
+                        const float den = sqrtf(sst * ssd);
+                        const float cc = den > kThreshold ? num / den : 0.0f;
+                        net[r * PL_THREADS + tid] =
+                            fmaf(atanhf(cc - 10.0f * FLT_EPSILON), zw, net[r * PL_THREADS + tid]);
+                    }
+                    acc[r] = 0.0f;
+                }
+            } else if (phi == P.step - 1) {
                 // fused epilogue of channel ch
                 const size_t row = (size_t)t * P.SC + ch;
                 const float sst = P.sst[row], wc = w[ch];
@@ -221,8 +258,10 @@ int launch_plain(const Problem &P, cudaStream_t stream)
     if (e != cudaSuccess)
         return set_error(FMF_ERR_CUDA, "plain kernel shared memory (%zu bytes): %s", g.smem,
                          cudaGetErrorString(e));
-    dim3 grid((unsigned)((P.n_corr + PL_TILE - 1) / PL_TILE), (unsigned)P.T);
-    plain_kernel<<<grid, PL_THREADS, g.smem, stream>>>(P, g);
+    const long long n_tiles = (P.n_corr + PL_TILE - 1) / PL_TILE;
+    if (n_tiles * P.T > 0x7fffffffLL)
+        return set_error(FMF_ERR_ARG, "too many (template, tile) pairs for one launch");
+    plain_kernel<<<(unsigned)(n_tiles * P.T), PL_THREADS, g.smem, stream>>>(P, g);
     count_launch();
     return check_launch("plain_kernel");
 }

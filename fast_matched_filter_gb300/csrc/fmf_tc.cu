@@ -391,6 +391,7 @@ __device__ __forceinline__ void decode_item(const TcBatch &B, long long item, in
 }
 
 constexpr int TC_NB_MAX = 128;  // largest tile; TMEM columns: D0 [0,128), D1 [128,256), sum [256,384)
+constexpr int TC_NACC = 2;      // accumulator buffers
 
 __global__ void __launch_bounds__(TC_THREADS, 1) tc_persistent(const __grid_constant__ TcBatch B)
 {
@@ -530,8 +531,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1) tc_persistent(const __grid_cons
                 for (int ch = 0; ch < SC; ch++) {
                     if (w[ch] == 0.0f)
                         continue;
-                    const int d = c & 1;
-                    if (c >= 2 && !mbar_wait(dempty0 + 8 * d, ((c >> 1) - 1) & 1, abort_flag, B.err, 4u))
+                    const int d = c % TC_NACC;
+                    if (c >= TC_NACC &&
+                        !mbar_wait(dempty0 + 8 * d, ((c / TC_NACC) - 1) & 1, abort_flag, B.err, 4u))
                         goto mma_done;
                     tc_fence_after();
                     const uint32_t dt = tmem + (uint32_t)(d * TC_NB_MAX);
@@ -604,7 +606,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) tc_persistent(const __grid_cons
             const int nb = pr.nb;
             const int NC = nb / (TC_EPI_WARPS / 4);  // columns of this thread (multiple of CH)
             const int a0 = cgroup * NC;
-            const uint32_t s_cols = lane_base + (uint32_t)(2 * TC_NB_MAX + a0);
+            const uint32_t s_cols = lane_base + (uint32_t)(TC_NACC * TC_NB_MAX + a0);
             const int SC = pr.P.SC, step = pr.P.step, n_corr = pr.P.n_corr, N = pr.P.N;
             const bool full = pr.P.normalize != 0, nsum = pr.P.network_sum != 0;
             const float *__restrict__ stat_e = pr.P.stat_e;
@@ -628,7 +630,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) tc_persistent(const __grid_cons
                 const float wc = w[ch];
                 if (wc == 0.0f)
                     continue;
-                const int d = c & 1;
+                const int d = c % TC_NACC;
                 const size_t row = (size_t)t * SC + ch;
                 const float sst = sstp[row];
                 const float ts = full ? tsump[row] : 0.0f;
@@ -648,7 +650,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) tc_persistent(const __grid_cons
                     }
                 };
                 load_chunk(0);
-                if (!mbar_wait_warp(dfull0 + 8 * d, (c >> 1) & 1, abort_flag, B.err, 16u))
+                if (!mbar_wait_warp(dfull0 + 8 * d, (c / TC_NACC) & 1, abort_flag, B.err, 16u))
                     goto epilogue_done;
                 tc_fence_after();
                 const uint32_t dcols = lane_base + (uint32_t)(d * TC_NB_MAX + a0);
@@ -884,6 +886,31 @@ int tc_run(const TcProb *probs, int n, int split, unsigned long long *queue, uns
 }
 
 size_t tc_prob_size() { return sizeof(TcProb); }
+
+// Templates [t0, t0 + nt) of a prepared search, as a search of its own
+// (every template-indexed pointer offset; data streams shared).
+void tc_subset(const TcProb *full, int t0, int nt, TcProb *out)
+{
+    TcProb q = *full;
+    const size_t SC = q.P.SC, step = q.P.step;
+    const size_t o = (size_t)t0 * SC;
+    q.P.tpl += o * q.P.L;
+    q.P.sst += o;
+    if (q.P.tsum)
+        q.P.tsum += o;
+    q.P.mo += o;
+    q.P.w += o;
+    q.P.k_lo += t0;
+    q.P.k_hi += t0;
+    q.P.out += (size_t)t0 * q.P.n_corr * (q.P.network_sum ? 1 : SC);
+    q.P.T = nt;
+    q.w_hi += o * step * q.NW * 64;
+    if (q.w_lo)
+        q.w_lo += o * step * q.NW * 64;
+    q.mu += o * step;
+    q.psi += o * step;
+    *out = q;
+}
 
 // Single search: preprocessing + one persistent launch.
 int launch_tc(const Problem &P, const float *data_for_tc, int precision, unsigned *err, Scratch &ws,

@@ -1,0 +1,470 @@
+// fmf_variable.cu -- per-channel template lengths with a Fisher-z network sum.
+//
+// GPU form of the reference's CPU-only arch 'variable_precise'
+// (matched_filter.c:321-412, 569-606): channel ch of template t uses its
+// first n[t][ch] taps (templates stored zero-padded to the longest, L); each
+// channel's coefficient is the 'precise' one (window mean removed for 'full',
+// threshold on sqrt(sst * ssd), matched_filter.c:629-657); the network value
+// is sum_ch atanh(cc - 10 eps) * z[t][ch] with z = sqrt(n - 3) * w, and every
+// output of template t then becomes
+// (tanh(value / sum_ch z) + used * eps * 10) * scale[t].
+// scale[t] is the reference's max_cc, which accumulates the weights of
+// templates 0..t (it is never reset, matched_filter.c:329,365); it is
+// reproduced as is.  Valid outputs: start <= k*step < stop with
+// start = ceil(|min(0, min mo)| / step) * step and
+// stop = N - L - max(0, max mo) - step (matched_filter.c:384-385); the final
+// transform applies to every output (matched_filter.c:405-408).
+//
+// Kernels: metadata (one thread, the reference's float accumulation order),
+// masked/centred templates, FP64 prefix sums of d^2 and d (global, so that
+// any window length is two subtractions), the plain FP32 kernel with its
+// variable-length epilogue (fmf_plain.cu), and the final transform.
+#include <cfloat>
+#include <climits>
+#include <cmath>
+#include <cstdlib>
+
+#include "fmf_common.cuh"
+
+namespace fmf {
+
+__global__ void channel_mean_kernel(const float *, int, float *);
+int device_error_word(unsigned **out);
+
+// One thread: lag range, Fisher-z weights and the transform constants of
+// every template, in the reference's order of float operations.
+__global__ void vp_meta_kernel(const int *__restrict__ mo, const float *__restrict__ w,
+                               const int *__restrict__ ntap, int T, int SC, int L, int N, int step,
+                               int n_corr, int *k_lo, int *k_hi, float *zweight, float *norm_sum,
+                               float *bias, float *scale)
+{
+    if (threadIdx.x != 0 || blockIdx.x != 0)
+        return;
+    float max_cc = 0.0f;
+    for (int t = 0; t < T; t++) {
+        const int *m = mo + (size_t)t * SC;
+        const float *wt = w + (size_t)t * SC;
+        const int *nt = ntap + (size_t)t * SC;
+        int lo = 0, hi = 0, used = 0;
+        for (int ch = 0; ch < SC; ch++) {
+            lo = min(lo, m[ch]);
+            hi = max(hi, m[ch]);
+            max_cc += wt[ch];
+            if (wt[ch] != 0.0f)
+                used += 1;
+        }
+        float zs = 0.0f;
+        for (int ch = 0; ch < SC; ch++) {
+            const float z = (float)(1.0 / (double)sqrtf((float)(1.0 / (double)(nt[ch] - 3))) * (double)wt[ch]);
+            zweight[(size_t)t * SC + ch] = z;
+            zs += z;
+        }
+        const long long start = (long long)(int)ceilf((float)abs(lo) / (float)step) * step;
+        const long long stop = (long long)N - L - hi - step;
+        long long a = 0, b = 0;
+        if (stop > start) {
+            a = start / step;
+            b = (stop - 1) / step + 1;
+            if (b > n_corr)
+                b = n_corr;
+            if (a > b)
+                a = b;
+        }
+        k_lo[t] = (int)a;
+        k_hi[t] = (int)b;
+        norm_sum[t] = zs;
+        bias[t] = used * FLT_EPSILON * 10;
+        scale[t] = max_cc;
+    }
+}
+
+// grid = T*SC blocks: template ch of t restricted to its first n taps (zero
+// beyond); for 'full' minus its FP64 mean over those taps, with the FP64 sum
+// of the result.
+__global__ void vp_template_kernel(const float *__restrict__ tpl, const int *__restrict__ ntap, int L,
+                                   int full, float *__restrict__ tout, float *__restrict__ tsum)
+{
+    __shared__ double red[33];
+    const size_t row = blockIdx.x;
+    const int n = min(max(ntap[row], 0), L);
+    const float *src = tpl + row * L;
+    float *dst = tout + row * L;
+    float mf = 0.0f;
+    if (full) {
+        double s = 0.0;
+        for (int j = threadIdx.x; j < n; j += blockDim.x)
+            s += (double)src[j];
+        for (int o = 16; o > 0; o >>= 1)
+            s += __shfl_down_sync(0xffffffffu, s, o);
+        if ((threadIdx.x & 31) == 0)
+            red[threadIdx.x >> 5] = s;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double tot = 0.0;
+            for (int i = 0; i < (int)(blockDim.x >> 5); i++)
+                tot += red[i];
+            red[32] = n > 0 ? tot / n : 0.0;
+        }
+        __syncthreads();
+        mf = (float)red[32];
+        __syncthreads();
+    }
+    double s2 = 0.0;
+    for (int j = threadIdx.x; j < L; j += blockDim.x) {
+        const float v = j < n ? src[j] - mf : 0.0f;
+        dst[j] = v;
+        s2 += (double)v;
+    }
+    if (full) {
+        for (int o = 16; o > 0; o >>= 1)
+            s2 += __shfl_down_sync(0xffffffffu, s2, o);
+        if ((threadIdx.x & 31) == 0)
+            red[threadIdx.x >> 5] = s2;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double tot = 0.0;
+            for (int i = 0; i < (int)(blockDim.x >> 5); i++)
+                tot += red[i];
+            tsum[row] = (float)tot;
+        }
+    }
+}
+
+constexpr int kPrefixBlock = 2048;
+
+// Phase 1, grid (blocks, SC): FP64 block sums of d'^2 and d' (d' = d - mu).
+__global__ void prefix_block_kernel(const float *__restrict__ data, int N, const float *__restrict__ mu,
+                                    double *__restrict__ bs2, double *__restrict__ bs1, int nblk)
+{
+    __shared__ double r2[32], r1[32];
+    const int ch = blockIdx.y, blk = blockIdx.x;
+    const float m = mu ? mu[ch] : 0.0f;
+    const float *src = data + (size_t)ch * N;
+    double s2 = 0.0, s1 = 0.0;
+    for (int i = blk * kPrefixBlock + threadIdx.x; i < min(N, (blk + 1) * kPrefixBlock); i += blockDim.x) {
+        const float v = src[i] - m;
+        s2 += (double)v * (double)v;
+        s1 += (double)v;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        s2 += __shfl_down_sync(0xffffffffu, s2, o);
+        s1 += __shfl_down_sync(0xffffffffu, s1, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        r2[threadIdx.x >> 5] = s2;
+        r1[threadIdx.x >> 5] = s1;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double a = 0.0, b = 0.0;
+        for (int i = 0; i < (int)(blockDim.x >> 5); i++) {
+            a += r2[i];
+            b += r1[i];
+        }
+        bs2[(size_t)ch * nblk + blk] = a;
+        bs1[(size_t)ch * nblk + blk] = b;
+    }
+}
+
+// Phase 2, one thread per channel: exclusive scan of the block sums.
+__global__ void prefix_offsets_kernel(double *bs2, double *bs1, int nblk, int SC)
+{
+    const int ch = blockIdx.x * blockDim.x + threadIdx.x;
+    if (ch >= SC)
+        return;
+    double a = 0.0, b = 0.0;
+    for (int i = 0; i < nblk; i++) {
+        const double x = bs2[(size_t)ch * nblk + i], y = bs1[(size_t)ch * nblk + i];
+        bs2[(size_t)ch * nblk + i] = a;
+        bs1[(size_t)ch * nblk + i] = b;
+        a += x;
+        b += y;
+    }
+}
+
+// Phase 3, grid (blocks, SC), 256 threads: inclusive scan of the block plus
+// its offset -> pre[ch][i + 1] = sum_{x <= i} d'^2 (pre[ch][0] = 0); for 'full'
+// also the centred data and its prefix sums.
+__global__ void prefix_write_kernel(const float *__restrict__ data, int N, const float *__restrict__ mu,
+                                    const double *__restrict__ bs2, const double *__restrict__ bs1,
+                                    int nblk, double *__restrict__ pre2, double *__restrict__ pre1,
+                                    float *__restrict__ dcen)
+{
+    __shared__ double part2[32], part1[32];
+    const int ch = blockIdx.y, blk = blockIdx.x;
+    const float m = mu ? mu[ch] : 0.0f;
+    const float *src = data + (size_t)ch * N;
+    const int i0 = blk * kPrefixBlock;
+    const int per = kPrefixBlock / 256;  // 8 consecutive samples per thread
+    double v2[kPrefixBlock / 256], v1[kPrefixBlock / 256];
+    double s2 = 0.0, s1 = 0.0;
+#pragma unroll
+    for (int e = 0; e < per; e++) {
+        const int i = i0 + threadIdx.x * per + e;
+        float v = 0.0f;
+        if (i < N) {
+            v = src[i] - m;
+            if (dcen)
+                dcen[(size_t)ch * N + i] = v;
+        }
+        s2 += (double)v * (double)v;
+        s1 += (double)v;
+        v2[e] = s2;
+        v1[e] = s1;
+    }
+    // exclusive scan of the per-thread totals
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    double x2 = s2, x1 = s1;
+    for (int o = 1; o < 32; o <<= 1) {
+        const double y2 = __shfl_up_sync(0xffffffffu, x2, o), y1 = __shfl_up_sync(0xffffffffu, x1, o);
+        if (lane >= o) {
+            x2 += y2;
+            x1 += y1;
+        }
+    }
+    if (lane == 31) {
+        part2[wid] = x2;
+        part1[wid] = x1;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double a = bs2[(size_t)ch * nblk + blk], b = bs1[(size_t)ch * nblk + blk];
+        for (int k = 0; k < (int)(blockDim.x >> 5); k++) {
+            const double p = part2[k], q = part1[k];
+            part2[k] = a;
+            part1[k] = b;
+            a += p;
+            b += q;
+        }
+    }
+    __syncthreads();
+    const double off2 = part2[wid] + (x2 - s2), off1 = part1[wid] + (x1 - s1);
+    double *p2 = pre2 + (size_t)ch * (N + 1);
+    double *p1 = pre1 ? pre1 + (size_t)ch * (N + 1) : nullptr;
+    if (blk == 0 && threadIdx.x == 0) {
+        p2[0] = 0.0;
+        if (p1)
+            p1[0] = 0.0;
+    }
+#pragma unroll
+    for (int e = 0; e < per; e++) {
+        const int i = i0 + threadIdx.x * per + e;
+        if (i < N) {
+            p2[i + 1] = off2 + v2[e];
+            if (p1)
+                p1[i + 1] = off1 + v1[e];
+        }
+    }
+}
+
+// out[t][k] = (tanh(out / norm_sum[t]) + bias[t]) * scale[t] for every k < n_corr
+__global__ void vp_finalize_kernel(float *__restrict__ out, int T, int n_corr,
+                                   const float *__restrict__ norm_sum, const float *__restrict__ bias,
+                                   const float *__restrict__ scale)
+{
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long long)T * n_corr)
+        return;
+    const int t = (int)(idx / n_corr);
+    out[idx] = (tanhf(out[idx] / norm_sum[t]) + bias[t]) * scale[t];
+}
+
+// ------------------------------------------------------------------ host driver
+struct VArgs {
+    const float *tpl, *sst, *data, *w;
+    const int *mo, *ntap;
+    float *out;
+    size_t step, N, T, S, C, n_corr;
+    int normalize, flags;
+};
+
+static int variable_device(const VArgs &a, int L, cudaStream_t s)
+{
+    int rc;
+    const int T = (int)a.T, SC = (int)(a.S * a.C), N = (int)a.N;
+    const bool full = a.normalize == 1;
+    Scratch ws(s);
+    int *k_lo;
+    float *zweight, *consts, *tmask, *tsum = nullptr, *mu = nullptr, *dcen = nullptr;
+    double *pre2, *pre1 = nullptr, *bs2, *bs1;
+    const int nblk = (N + kPrefixBlock - 1) / kPrefixBlock;
+    if ((rc = ws.get(&k_lo, 2 * (size_t)T, "template ranges")) ||
+        (rc = ws.get(&zweight, (size_t)T * SC, "Fisher-z weights")) ||
+        (rc = ws.get(&consts, 3 * (size_t)T, "transform constants")) ||
+        (rc = ws.get(&tmask, (size_t)T * SC * L, "masked templates")) ||
+        (rc = ws.get(&pre2, (size_t)SC * (N + 1), "prefix sums")) ||
+        (rc = ws.get(&bs2, 2 * (size_t)SC * nblk, "block sums")))
+        return rc;
+    bs1 = bs2 + (size_t)SC * nblk;
+    if (full && ((rc = ws.get(&tsum, (size_t)T * SC, "template sums")) ||
+                 (rc = ws.get(&mu, (size_t)SC, "channel means")) ||
+                 (rc = ws.get(&dcen, (size_t)SC * N, "centred data")) ||
+                 (rc = ws.get(&pre1, (size_t)SC * (N + 1), "prefix sums of d"))))
+        return rc;
+    int *k_hi = k_lo + T;
+    float *norm_sum = consts, *bias = consts + T, *scale = consts + 2 * T;
+
+    vp_meta_kernel<<<1, 32, 0, s>>>(a.mo, a.w, a.ntap, T, SC, L, N, (int)a.step, (int)a.n_corr, k_lo, k_hi,
+                                    zweight, norm_sum, bias, scale);
+    vp_template_kernel<<<(unsigned)((size_t)T * SC), 128, 0, s>>>(a.tpl, a.ntap, L, full ? 1 : 0, tmask, tsum);
+    if (full)
+        channel_mean_kernel<<<SC, 256, 0, s>>>(a.data, N, mu);
+    prefix_block_kernel<<<dim3(nblk, SC), 256, 0, s>>>(a.data, N, mu, bs2, bs1, nblk);
+    prefix_offsets_kernel<<<(SC + 127) / 128, 128, 0, s>>>(bs2, bs1, nblk, SC);
+    prefix_write_kernel<<<dim3(nblk, SC), 256, 0, s>>>(a.data, N, mu, bs2, bs1, nblk, pre2, pre1, dcen);
+    count_launch(full ? 6 : 5);
+    if ((rc = check_launch("variable-length preprocessing")))
+        return rc;
+
+    Problem P;
+    P.tpl = tmask;
+    P.sst = a.sst;
+    P.tsum = tsum;
+    P.mo = a.mo;
+    P.w = a.w;
+    P.data = full ? dcen : a.data;
+    P.stat_e = nullptr;
+    P.stat_m = nullptr;
+    P.k_lo = k_lo;
+    P.k_hi = k_hi;
+    P.out = a.out;
+    P.T = T;
+    P.SC = SC;
+    P.L = L;
+    P.N = N;
+    P.step = (int)a.step;
+    P.n_corr = (int)a.n_corr;
+    P.normalize = a.normalize;
+    P.network_sum = 1;
+    P.ntap = a.ntap;
+    P.pre2 = pre2;
+    P.pre1 = pre1;
+    P.zweight = zweight;
+    if ((rc = launch_plain_all(P, s)))
+        return rc;
+    const long long n = (long long)T * a.n_corr;
+    vp_finalize_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(a.out, T, (int)a.n_corr, norm_sum, bias,
+                                                                   scale);
+    count_launch();
+    return check_launch("variable-length transform");
+}
+
+static int variable_entry(const VArgs &a, void *stream)
+{
+    set_error(FMF_OK, "");
+    if (!a.tpl || !a.sst || !a.mo || !a.data || !a.w || !a.ntap || !a.out)
+        return set_error(FMF_ERR_ARG, "null array argument");
+    if (a.step < 1 || a.T < 1 || a.S < 1 || a.C < 1 || a.n_corr < 1 || a.N < 1)
+        return set_error(FMF_ERR_ARG, "sizes must be positive");
+    if (a.N > (size_t)INT_MAX / 2 || a.n_corr > (size_t)INT_MAX || a.S * a.C > (size_t)INT_MAX ||
+        a.T > (size_t)INT_MAX || a.step > (size_t)INT_MAX / 2)
+        return set_error(FMF_ERR_ARG, "sizes exceed the 32-bit index range of this build");
+    if (a.normalize != 0 && a.normalize != 1)
+        return set_error(FMF_ERR_ARG, "normalize must be 0 or 1");
+    cudaGetLastError();
+    cudaStream_t s = (cudaStream_t)stream;
+    const size_t n_meta = a.T * a.S * a.C;
+    const bool dev = (a.flags & FMF_FLAG_DEVICE_POINTERS) != 0;
+    // the longest template (stride of the template array)
+    int L = 0;
+    if (dev) {
+        int *tmp = (int *)malloc(n_meta * sizeof(int));
+        if (!tmp)
+            return set_error(FMF_ERR_OOM, "host memory for the template lengths");
+        cudaError_t e = cudaMemcpyAsync(tmp, a.ntap, n_meta * sizeof(int), cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess)
+            e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) {
+            free(tmp);
+            return set_error(FMF_ERR_CUDA, "reading the template lengths: %s", cudaGetErrorString(e));
+        }
+        for (size_t i = 0; i < n_meta; i++)
+            L = tmp[i] > L ? tmp[i] : L;
+        free(tmp);
+    } else {
+        for (size_t i = 0; i < n_meta; i++)
+            L = a.ntap[i] > L ? a.ntap[i] : L;
+    }
+    if (L < 1 || (size_t)L > a.N)
+        return set_error(FMF_ERR_ARG, "longest template %d not in [1, N]", L);
+    if (a.n_corr > (a.N - L) / a.step + 1)
+        return set_error(FMF_ERR_ARG, "n_corr exceeds (N - longest template)/step + 1");
+    if (dev)
+        return variable_device(a, L, s);
+
+    int rc;
+    const size_t SC = a.S * a.C;
+    const size_t cnt[7] = {a.T * SC * L, a.T * SC, a.T * SC, SC * a.N, a.T * SC, a.T * SC, a.T * a.n_corr};
+    float *buf[7];
+    {
+        Scratch io(s);
+        for (int i = 0; i < 7; i++)
+            if ((rc = io.get(&buf[i], cnt[i], "input/output copies")))
+                return rc;
+        const void *src[6] = {a.tpl, a.sst, a.mo, a.data, a.w, a.ntap};
+        for (int i = 0; i < 6; i++) {
+            cudaError_t e = cudaMemcpyAsync(buf[i], src[i], cnt[i] * 4, cudaMemcpyHostToDevice, s);
+            if (e != cudaSuccess)
+                return set_error(FMF_ERR_CUDA, "copying inputs: %s", cudaGetErrorString(e));
+        }
+        VArgs d = a;
+        d.tpl = buf[0];
+        d.sst = buf[1];
+        d.mo = reinterpret_cast<const int *>(buf[2]);
+        d.data = buf[3];
+        d.w = buf[4];
+        d.ntap = reinterpret_cast<const int *>(buf[5]);
+        d.out = buf[6];
+        if ((rc = variable_device(d, L, s)))
+            return rc;
+        cudaError_t e = cudaMemcpyAsync(a.out, d.out, cnt[6] * 4, cudaMemcpyDeviceToHost, s);
+        if (e != cudaSuccess)
+            return set_error(FMF_ERR_CUDA, "copying the result: %s", cudaGetErrorString(e));
+    }
+    cudaError_t e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess)
+        return set_error(FMF_ERR_CUDA, "variable-length search: %s", cudaGetErrorString(e));
+    return FMF_OK;
+}
+
+}  // namespace fmf
+
+extern "C" {
+
+int fmf_matched_filter_variable_ex(const float *templates, const float *sum_square_templates,
+                                   const int *moveouts, const float *data, const float *weights,
+                                   size_t step, const int *n_samples_template, size_t n_samples_data,
+                                   size_t n_templates, size_t n_stations, size_t n_components,
+                                   size_t n_corr, float *cc_sum, int normalize, int flags, void *stream)
+{
+    fmf::VArgs a;
+    a.tpl = templates;
+    a.sst = sum_square_templates;
+    a.mo = moveouts;
+    a.data = data;
+    a.w = weights;
+    a.ntap = n_samples_template;
+    a.out = cc_sum;
+    a.step = step;
+    a.N = n_samples_data;
+    a.T = n_templates;
+    a.S = n_stations;
+    a.C = n_components;
+    a.n_corr = n_corr;
+    a.normalize = normalize;
+    a.flags = flags;
+    return fmf::variable_entry(a, stream);
+}
+
+int fmf_matched_filter_variable(const float *templates, const float *sum_square_templates,
+                                const int *moveouts, const float *data, const float *weights,
+                                size_t step, const int *n_samples_template, size_t n_samples_data,
+                                size_t n_templates, size_t n_stations, size_t n_components,
+                                size_t n_corr, float *cc_sum, int normalize)
+{
+    return fmf_matched_filter_variable_ex(templates, sum_square_templates, moveouts, data, weights, step,
+                                          n_samples_template, n_samples_data, n_templates, n_stations,
+                                          n_components, n_corr, cc_sum, normalize, 0, nullptr);
+}
+
+}  // extern "C"

@@ -167,13 +167,16 @@ def matched_filter(templates, moveouts, weights, data, step,
     assert normalize in ("short", "full"), "Only know short or full normalization methods"
     if normalize == "full":
         assert arch != "cpu", "Full normalization not supported with cpu arch - try arch=precise"
+    if n_samples_template is not None or arch.lower() == "variable_precise":
+        if arch.lower() not in ("gpu", "variable_precise"):
+            print("Compiled library for {} not loaded; exiting!".format(arch))
+            return None
+        return _matched_filter_variable(templates, moveouts, weights, data, step,
+                                        n_samples_template, check_zeros, normalize,
+                                        network_sum)
     if arch.lower() != "gpu":
         print("Compiled library for {} not loaded; exiting!".format(arch))
         return None
-    if n_samples_template is not None:
-        raise NotImplementedError(
-            "per-channel template lengths (arch='variable_precise') are not "
-            "implemented by the GPU library")
     if precision not in _lib.PRECISIONS:
         raise ValueError("precision must be one of %s" % sorted(_lib.PRECISIONS))
     lib = _require_lib()
@@ -201,6 +204,38 @@ def matched_filter(templates, moveouts, weights, data, step,
     cc = cc.reshape(T, n_corr) if network_sum else cc.reshape(T, n_corr, S, C)
     _zero_report(cc, pp["moveouts"], pp["weights"], T, n_corr, pp["step"],
                  network_sum, check_zeros)
+    return cc
+
+
+def _matched_filter_variable(templates, moveouts, weights, data, step, n_samples_template,
+                             check_zeros, normalize, network_sum):
+    """Per-channel template lengths (the reference's arch 'variable_precise',
+    fast_matched_filter.py:216-229, 307-313) on the GPU library."""
+    if n_samples_template is None:
+        raise ValueError("arch='variable_precise' needs n_samples_template")
+    if not network_sum:
+        raise NotImplementedError("Variable precise without network sum is not yet implemented.")
+    lib = _require_lib()
+    n_samples_template = np.asarray(n_samples_template)
+    assert n_samples_template.shape == np.asarray(moveouts).shape
+    max_len = int(np.max(n_samples_template))
+    dims = _infer_dims(templates, data)
+    if dims is None:
+        print("Template and data dimensions are not compatible!")
+        return None
+    T, S, C = dims
+    templates = templates.reshape(T, S, C, max_len)
+    pp = prepare(templates, moveouts, weights, data, step, normalize)
+    n_corr = int((pp["N"] - max_len) / pp["step"] + 1)
+    nt = np.ascontiguousarray(n_samples_template.flatten(), dtype=np.int32)
+    cc = np.zeros(T * n_corr, dtype=np.float32)
+    st = lib.fmf_matched_filter_variable_ex(
+        pp["templates"].ctypes.data, pp["sst"].ctypes.data, pp["moveouts"].ctypes.data,
+        pp["data"].ctypes.data, pp["weights"].ctypes.data, pp["step"], nt.ctypes.data,
+        pp["N"], T, S, C, n_corr, cc.ctypes.data, pp["normalize"], 0, None)
+    _lib.check(st, lib)
+    cc = cc.reshape(T, n_corr)
+    _zero_report(cc, pp["moveouts"], pp["weights"], T, n_corr, pp["step"], True, check_zeros)
     return cc
 
 

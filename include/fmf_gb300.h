@@ -159,6 +159,31 @@ FMF_API int fmf_batch_run(fmf_batch *batch, void *stream);
 FMF_API int fmf_batch_launch_count(const fmf_batch *batch);
 FMF_API int fmf_batch_destroy(fmf_batch *batch);
 
+/*
+ * Per-channel template lengths with a Fisher-z network sum: the arguments of
+ * the reference's CPU-only matched_filter_variable_precise
+ * (fast_matched_filter/src/matched_filter_CPU.h, matched_filter.c:321-325,
+ * called from fast_matched_filter.py:307-309), run on the GPU (plain FP32
+ * form).  n_samples_template (T, S, C) gives each channel's length; templates
+ * are (T, S, C, max length), zero-padded; cc_sum is (T, n_corr) with
+ * n_corr = (N - max length) / step + 1.  Host pointers, synchronous.
+ * Semantics, including the reference's template-cumulative scale, are those
+ * of matched_filter.c:321-412 (see fmf_variable.cu).
+ */
+FMF_API int fmf_matched_filter_variable(const float *templates, const float *sum_square_templates,
+                                        const int *moveouts, const float *data, const float *weights,
+                                        size_t step, const int *n_samples_template,
+                                        size_t n_samples_data, size_t n_templates, size_t n_stations,
+                                        size_t n_components, size_t n_corr, float *cc_sum,
+                                        int normalize);
+/* Same, with flags (FMF_FLAG_DEVICE_POINTERS) and a stream. */
+FMF_API int fmf_matched_filter_variable_ex(const float *templates, const float *sum_square_templates,
+                                           const int *moveouts, const float *data, const float *weights,
+                                           size_t step, const int *n_samples_template,
+                                           size_t n_samples_data, size_t n_templates, size_t n_stations,
+                                           size_t n_components, size_t n_corr, float *cc_sum,
+                                           int normalize, int flags, void *stream);
+
 /* Copies the calling thread's last error message (NUL-terminated, truncated
  * to len) and returns its status.  The reference printed and exited instead
  * (matched_filter.cu:30-39, 236-242, 286-299). */

@@ -51,6 +51,9 @@ def oracle_lib():
         lib.fmo_cumsum_sq.argtypes = [_fp, _sz, ct.POINTER(ct.c_double)]
         lib.fmo_cumsum_sq.restype = None
         lib.fmo_max_threads.restype = ct.c_int
+        lib.fmo_matched_filter_variable.argtypes = [_fp, _fp, _ip, _fp, _fp, _sz, _ip, _sz, _sz, _sz,
+                                                    _sz, _sz, _fp, ct.c_int, ct.c_int]
+        lib.fmo_matched_filter_variable.restype = ct.c_int
         _oracle = lib
     return _oracle
 
@@ -69,6 +72,8 @@ def reference_lib():
         for name in ("matched_filter_precise", "matched_filter_precise_no_sum"):
             getattr(lib, name).argtypes = _REF_ARGS + [ct.c_int]
             getattr(lib, name).restype = None
+        lib.matched_filter_variable_precise.argtypes = _REF_ARGS[:6] + [_ip] + _REF_ARGS[7:] + [ct.c_int]
+        lib.matched_filter_variable_precise.restype = None
         lib.neumaier_cumsum_squared.argtypes = [_fp, _sz, ct.POINTER(ct.c_double)]
         lib.neumaier_cumsum_squared.restype = None
         _ref = lib
@@ -142,6 +147,45 @@ def run_reference(templates, moveouts, weights, data, step, arch="cpu",
         fn = lib.matched_filter_precise if network_sum else lib.matched_filter_precise_no_sum
         fn(*args, 1 if normalize == "full" else 0)
     return _shape(cc, dims, network_sum)
+
+
+def _variable_args(templates, n_samples_template, moveouts, weights, data, step):
+    """Flat buffers of the variable-length call, as the reference wrapper
+    builds them (fast_matched_filter.py:216-268): templates (T,S,C,max_len)
+    zero-padded, energies over the padded length, n_samples_template int32."""
+    tp, sst, mo, d, w, dims = flatten_inputs(templates, moveouts, weights, data, step)
+    nt = np.ascontiguousarray(np.asarray(n_samples_template).reshape(-1), dtype=np.int32)
+    dims["n_corr"] = int((dims["N"] - int(nt.max())) / step + 1)
+    return tp, sst, mo, d, w, nt, dims
+
+
+def run_oracle_variable(templates, n_samples_template, moveouts, weights, data, step,
+                        normalize="short", n_threads=0):
+    """Oracle restatement of the per-channel-length Fisher-z search."""
+    tp, sst, mo, d, w, nt, dims = _variable_args(templates, n_samples_template, moveouts,
+                                                 weights, data, step)
+    cc = np.zeros(dims["T"] * dims["n_corr"], dtype=np.float32)
+    rc = oracle_lib().fmo_matched_filter_variable(
+        _ptr(tp, ct.c_float), _ptr(sst, ct.c_float), _ptr(mo, ct.c_int), _ptr(d, ct.c_float),
+        _ptr(w, ct.c_float), dims["step"], _ptr(nt, ct.c_int), dims["N"], dims["T"], dims["S"],
+        dims["C"], dims["n_corr"], _ptr(cc, ct.c_float), 1 if normalize == "full" else 0,
+        int(n_threads))
+    if rc != 0:
+        raise ValueError("oracle rejected the arguments")
+    return cc.reshape(dims["T"], dims["n_corr"])
+
+
+def run_reference_variable(templates, n_samples_template, moveouts, weights, data, step,
+                           normalize="short"):
+    """The reference's matched_filter_variable_precise (oracle/_ref)."""
+    tp, sst, mo, d, w, nt, dims = _variable_args(templates, n_samples_template, moveouts,
+                                                 weights, data, step)
+    cc = np.zeros(dims["T"] * dims["n_corr"], dtype=np.float32)
+    reference_lib().matched_filter_variable_precise(
+        _ptr(tp, ct.c_float), _ptr(sst, ct.c_float), _ptr(mo, ct.c_int), _ptr(d, ct.c_float),
+        _ptr(w, ct.c_float), dims["step"], _ptr(nt, ct.c_int), dims["N"], dims["T"], dims["S"],
+        dims["C"], dims["n_corr"], _ptr(cc, ct.c_float), 1 if normalize == "full" else 0)
+    return cc.reshape(dims["T"], dims["n_corr"])
 
 
 def cumsum_sq(x, use_reference=False):

@@ -34,6 +34,7 @@
  * Lags outside a template's valid range are left untouched (callers pass a
  * zeroed buffer, as the reference wrapper does: fast_matched_filter.py:269-274).
  */
+#include <float.h>
 #include <math.h>
 #include <stddef.h>
 #include <stdint.h>
@@ -203,6 +204,87 @@ int fmo_matched_filter(const float *templates, const float *sst,
         }
     }
     free(csum);
+    return 0;
+}
+
+/* Per-channel template lengths with a Fisher-z network sum: restates
+ * matched_filter_variable_precise (MF.c:321-412) and
+ * network_corr_variable_precise (MF.c:569-606).  Templates are stored with
+ * stride max(n_tpl); channel ch of template t uses its first n_tpl[t][ch]
+ * taps and the 'precise' correlation (MF.c:629-657).  Reproduced exactly,
+ * including two properties of the reference: the scale max_cc accumulates
+ * the weights of every template up to and including t (it is never reset,
+ * MF.c:329,365), and the final tanh transform is applied to every output,
+ * also outside the lag range (MF.c:405-408).
+ * Returns 0, or -1 on bad arguments. */
+int fmo_matched_filter_variable(const float *templates, const float *sst,
+                                const int *moveouts, const float *data,
+                                const float *weights, size_t step,
+                                const int *n_tpl, size_t N, size_t T,
+                                size_t S, size_t C, size_t n_corr, float *cc,
+                                int normalize, int n_threads)
+{
+    const size_t nch = S * C;
+    if (step == 0 || nch == 0)
+        return -1;
+#ifdef _OPENMP
+    if (n_threads > 0)
+        omp_set_num_threads(n_threads);
+#else
+    (void)n_threads;
+#endif
+    float *cc_norm = (float *)malloc(nch * sizeof(float));
+    if (!cc_norm)
+        return -1;
+    int max_len = 0;
+    for (size_t k = 0; k < T * nch; k++)
+        if (n_tpl[k] > max_len)
+            max_len = n_tpl[k];
+    float max_cc = 0.0f;
+    for (size_t t = 0; t < T; t++) {
+        const int *mo = moveouts + t * nch;
+        const float *w = weights + t * nch;
+        const float *ss = sst + t * nch;
+        const int *nt = n_tpl + t * nch;
+        const float *tp = templates + t * nch * (size_t)max_len;
+        int lo = 0, hi = 0, used = 0;
+        for (size_t ch = 0; ch < nch; ch++) {
+            if (mo[ch] < lo)
+                lo = mo[ch];
+            if (mo[ch] > hi)
+                hi = mo[ch];
+            max_cc += w[ch];
+            if (w[ch] != 0.0f)
+                used += 1;
+        }
+        float norm_sum = 0.0f;
+        for (size_t ch = 0; ch < nch; ch++) {
+            cc_norm[ch] = (float)(1.0 / (double)sqrtf((float)(1.0 / (double)(nt[ch] - 3))) * (double)w[ch]);
+            norm_sum += cc_norm[ch];
+        }
+        const size_t start = (size_t)(int)(ceilf(abs(lo) / (float)step)) * step;
+        const long long stop = (long long)N - max_len - hi - (long long)step;
+        long long n_lags = stop > (long long)start ? (stop - (long long)start + (long long)step - 1) / (long long)step : 0;
+#pragma omp parallel for
+        for (long long k = 0; k < n_lags; k++) {
+            size_t i = start + (size_t)k * step;
+            float acc = 0.0f;
+            for (size_t ch = 0; ch < nch; ch++) {
+                if (w[ch] == 0.0f)
+                    continue;
+                size_t off = i + (size_t)((long long)mo[ch]);
+                float v = corr_direct(tp + ch * (size_t)max_len, ss[ch], data + ch * N + off,
+                                      (size_t)nt[ch], normalize);
+                acc = fmaf(atanhf(v - 10 * FLT_EPSILON), cc_norm[ch], acc);
+            }
+            cc[t * n_corr + i / step] = acc;
+        }
+        const float bias = used * FLT_EPSILON * 10;
+#pragma omp parallel for
+        for (long long i = 0; i < (long long)n_corr; i++)
+            cc[t * n_corr + i] = (tanhf(cc[t * n_corr + i] / norm_sum) + bias) * max_cc;
+    }
+    free(cc_norm);
     return 0;
 }
 

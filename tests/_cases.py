@@ -17,9 +17,21 @@ def load_golden(name):
     z = np.load(os.path.join(GOLDEN, name + ".npz"))
     inputs = {k: z[k] for k in ("templates", "moveouts", "weights", "data")}
     inputs["step"] = int(z["step"])
+    if "n_samples_template" in z.files:
+        inputs["n_samples_template"] = z["n_samples_template"]
     opts = dict(arch=str(z["arch"]), normalize=str(z["normalize"]),
                 network_sum=bool(z["network_sum"]))
     return inputs, opts, z["cc"]
+
+
+def golden_names_fixed():
+    """Fixtures of the fixed-length archs ('cpu', 'precise')."""
+    return [n for n in golden_names() if not n.startswith("variable")]
+
+
+def golden_names_variable():
+    """Fixtures of the per-channel-length arch ('variable_precise')."""
+    return [n for n in golden_names() if n.startswith("variable")]
 
 
 def canonical(inputs):

@@ -36,6 +36,8 @@ def load_reference_wrapper(ref_root):
     lib.matched_filter_precise.argtypes = mod.argtypes + [ct.c_int]
     lib.matched_filter_no_sum.argtypes = mod.argtypes
     lib.matched_filter_precise_no_sum.argtypes = mod.argtypes + [ct.c_int]
+    lib.matched_filter_variable_precise.argtypes = (mod.argtypes[0:6] + [ct.POINTER(ct.c_int)]
+                                                    + mod.argtypes[7:] + [ct.c_int])
     mod._libCPU = lib
     mod.CPU_LOADED = True
     return mod
@@ -110,6 +112,20 @@ def cases():
                 dict(templates=tp, moveouts=mo[:, :, 0].copy(), weights=w[:, :, 0].copy(),
                      data=d, step=2),
                 dict(arch="cpu", normalize="short", network_sum=True)))
+    # per-channel template lengths (arch='variable_precise'), short and full
+    for name, seed, step, norm in (("variable_short", 10, 1, "short"),
+                                   ("variable_full_step2", 11, 2, "full")):
+        tp, mo, w, d = base(seed, 2, 3, 2, 90, 2600, -15, 80, dc=1.5 if norm == "full" else 0.0)
+        rng = np.random.default_rng(seed + 100)
+        nt = rng.integers(45, 91, (2, 3, 2)).astype(np.int32)
+        tp = np.ascontiguousarray(tp[..., :int(nt.max())])  # last axis = longest template
+        for t in range(2):
+            for s_ in range(3):
+                for c in range(2):
+                    tp[t, s_, c, nt[t, s_, c]:] = 0.0
+        out.append((name, dict(templates=tp, moveouts=mo, weights=w, data=d, step=step,
+                               n_samples_template=nt),
+                    dict(arch="variable_precise", normalize=norm, network_sum=True)))
     return out
 
 

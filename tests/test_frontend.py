@@ -15,7 +15,7 @@ def test_reference_names_exported():
     assert fmf.CPU_LOADED is False
 
 
-@pytest.mark.parametrize("arch", ["cpu", "precise", "variable_precise"])
+@pytest.mark.parametrize("arch", ["cpu", "precise"])
 def test_cpu_architectures_reported_not_loaded(arch, capsys):
     tp = np.zeros((1, 1, 1, 8), np.float32)
     out = fmf.matched_filter(tp, np.zeros((1, 1, 1)), np.ones((1, 1, 1)),
@@ -98,3 +98,12 @@ def test_zero_report_per_channel_layout_slices_last_axis():
     mo = np.array([0, 0, 0, 0, 0, 48], np.int32)  # stop = 50 - 48 = 2 components kept
     z = _zero_report(cc, mo, np.ones(6, np.float32), 1, 50, 1, False, "first")
     assert list(z) == [50 * 2 * 2]
+
+
+def test_variable_lengths_without_network_sum_not_implemented():
+    # as the reference wrapper (fast_matched_filter.py:310-313)
+    with pytest.raises(NotImplementedError):
+        fmf.matched_filter(np.zeros((1, 1, 1, 8), np.float32), np.zeros((1, 1, 1)),
+                           np.ones((1, 1, 1)), np.zeros((1, 1, 100), np.float32), 1,
+                           n_samples_template=np.full((1, 1, 1), 8), arch="variable_precise",
+                           network_sum=False)

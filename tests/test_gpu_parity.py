@@ -12,7 +12,7 @@ import pytest
 
 import fast_matched_filter_gb300 as fmf
 from fast_matched_filter_gb300 import _lib, synthetic
-from tests._cases import canonical, golden_names, load_golden, random_search
+from tests._cases import canonical, golden_names_fixed, load_golden, random_search
 
 TOL = 1e-5
 pytestmark = pytest.mark.gpu
@@ -31,7 +31,7 @@ def assert_parity(got, ref, tol=TOL):
     assert err <= tol, "max |diff| %.3g" % err
 
 
-@pytest.mark.parametrize("name", golden_names())
+@pytest.mark.parametrize("name", golden_names_fixed())
 def test_golden_fixtures(name):
     inputs, opts, expected = load_golden(name)
     got = fmf.matched_filter(check_zeros=False, arch="gpu", normalize=opts["normalize"],

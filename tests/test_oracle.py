@@ -12,12 +12,13 @@ import os
 import numpy as np
 import pytest
 
-from tests._cases import canonical, golden_names, load_golden, random_search
+from tests._cases import (canonical, golden_names, golden_names_fixed, golden_names_variable,
+                          load_golden, random_search)
 
 REF_DATA = "/root/reference/fast_matched_filter/tests/data"
 
 
-@pytest.mark.parametrize("name", golden_names())
+@pytest.mark.parametrize("name", golden_names_fixed())
 def test_oracle_matches_golden_bit_exact(oracle_built, name):
     inputs, opts, expected = load_golden(name)
     tp, mo, w, d = canonical(inputs)
@@ -27,7 +28,7 @@ def test_oracle_matches_golden_bit_exact(oracle_built, name):
         "max diff %g" % np.abs(got - expected.reshape(got.shape)).max()
 
 
-@pytest.mark.parametrize("name", golden_names())
+@pytest.mark.parametrize("name", golden_names_fixed())
 def test_fp64_oracle_close_to_golden(name):
     from oracle import fp64
     inputs, opts, expected = load_golden(name)
@@ -36,6 +37,21 @@ def test_fp64_oracle_close_to_golden(name):
     got = fp64.fp64_matched_filter(tp, mo, w, d, inputs["step"], opts["normalize"],
                                    opts["network_sum"], threshold=thr)
     assert np.abs(got - expected.reshape(got.shape)).max() < 2e-6
+
+
+def variable_inputs(inputs):
+    """Canonical arrays of a variable-length fixture (the templates' last axis
+    is the longest template)."""
+    tp, mo, w, d = canonical(inputs)
+    return tp, np.asarray(inputs["n_samples_template"]).reshape(mo.shape), mo, w, d
+
+
+@pytest.mark.parametrize("name", golden_names_variable())
+def test_oracle_variable_matches_golden_bit_exact(oracle_built, name):
+    inputs, opts, expected = load_golden(name)
+    tp, nt, mo, w, d = variable_inputs(inputs)
+    got = oracle_built.run_oracle_variable(tp, nt, mo, w, d, inputs["step"], opts["normalize"])
+    assert np.array_equal(got, expected.reshape(got.shape))
 
 
 def test_golden_fixtures_cover_the_reference_options():
@@ -47,6 +63,8 @@ def test_golden_fixtures_cover_the_reference_options():
         seen.add((o["arch"], o["normalize"], o["network_sum"]))
     assert ("cpu", "short", True) in seen and ("cpu", "short", False) in seen
     assert ("precise", "full", True) in seen and ("precise", "full", False) in seen
+    assert ("variable_precise", "short", True) in seen
+    assert ("variable_precise", "full", True) in seen
 
 
 needs_ref = pytest.mark.skipif(
@@ -65,6 +83,21 @@ def test_oracle_matches_reference_library(oracle_built, step, arch, normalize, n
                                  zero_weights=2)
     a = oracle_built.run_oracle(tp, mo, w, d, step, arch, normalize, network_sum)
     b = oracle_built.run_reference(tp, mo, w, d, step, arch, normalize, network_sum)
+    assert np.array_equal(a, b)
+
+
+@needs_ref
+@pytest.mark.parametrize("step,normalize", [(1, "short"), (2, "full"), (3, "short"), (1, "full")])
+def test_oracle_variable_matches_reference_library(oracle_built, step, normalize):
+    rng = np.random.default_rng(40 + step)
+    tp, mo, w, d = random_search(50 + step, 3, 3, 2, 110, 3000, -20, 90,
+                                 dc=2.0 if normalize == "full" else 0.0, zero_weights=1)
+    nt = rng.integers(40, 111, mo.shape).astype(np.int32)
+    tp = np.ascontiguousarray(tp[..., :int(nt.max())])
+    for idx in np.ndindex(nt.shape):
+        tp[idx][nt[idx]:] = 0.0
+    a = oracle_built.run_oracle_variable(tp, nt, mo, w, d, step, normalize)
+    b = oracle_built.run_reference_variable(tp, nt, mo, w, d, step, normalize)
     assert np.array_equal(a, b)
 
 
