@@ -15,5 +15,11 @@ from .fast_matched_filter import (  # noqa: F401
     test_matched_filter,
 )
 from ._lib import FMFError  # noqa: F401
+from .detection import (  # noqa: F401
+    Detections,
+    detect,
+    matched_filter_detect,
+    valid_lag_range,
+)
 
 __version__ = "0.1.0"

@@ -54,7 +54,14 @@ EXPORTS = ("fmf_matched_filter", "matched_filter", "fmf_matched_filter_ex",
            "fmf_device_errors", "fmf_matched_filter_noalloc", "fmf_batch_create",
            "fmf_batch_add", "fmf_batch_set_tiles", "fmf_batch_run", "fmf_batch_launch_count",
            "fmf_batch_destroy", "fmf_selftest_wait_timeout", "fmf_matched_filter_variable",
-           "fmf_matched_filter_variable_ex")
+           "fmf_matched_filter_variable_ex", "fmf_detect", "fmf_matched_filter_detect")
+
+DETECT_CAPACITY = 16384  # FMF_DETECT_CAPACITY
+# detection arguments after the rows: n_mad, min_separation, max_detections, six outputs,
+# flags, stream
+_DETECT_TAIL = [ct.c_float, _sz, _sz] + [ct.c_void_p] * 6 + [ct.c_int, ct.c_void_p]
+ARGTYPES_DETECT = [ct.c_void_p, _sz, _sz, ct.c_void_p, ct.c_void_p] + _DETECT_TAIL
+ARGTYPES_SEARCH_DETECT = [ct.c_void_p] * 5 + [_sz] * 7 + [ct.c_int, ct.c_int] + _DETECT_TAIL
 
 
 class FMFError(RuntimeError):
@@ -110,6 +117,10 @@ def load(path=None):
     lib.fmf_timing_end.argtypes = [ct.POINTER(ct.c_double), ct.POINTER(ct.c_double),
                                    ct.POINTER(ct.c_int)]
     lib.fmf_timing_end.restype = ct.c_int
+    lib.fmf_detect.argtypes = ARGTYPES_DETECT
+    lib.fmf_detect.restype = ct.c_int
+    lib.fmf_matched_filter_detect.argtypes = ARGTYPES_SEARCH_DETECT
+    lib.fmf_matched_filter_detect.restype = ct.c_int
     if path is None:
         _lib = lib
     return lib

@@ -290,11 +290,12 @@ int launch_plain_all(const Problem &P, cudaStream_t s)
     return FMF_OK;
 }
 
-static int run_device(const Args &a, cudaStream_t s)
+// Search on device pointers with its working arrays in `ws` (they stay
+// allocated, and *Pout valid, until ws goes out of scope).
+static int run_device_ws(const Args &a, cudaStream_t s, Scratch &ws, Problem *Pout)
 {
     int rc;
-    Scratch ws(s);
-    Problem P;
+    Problem &P = *Pout;
     const float *data_for_tc = nullptr;
     cudaEvent_t ev_prep0 = mark(s);
     if ((rc = prepare_problem(a, ws, s, &P, &data_for_tc)))
@@ -321,6 +322,13 @@ static int run_device(const Args &a, cudaStream_t s)
     rc = launch_plain_all(P, s);
     span(ev_main0, mark(s), 1);
     return rc;
+}
+
+static int run_device(const Args &a, cudaStream_t s)
+{
+    Scratch ws(s);
+    Problem P;
+    return run_device_ws(a, s, ws, &P);
 }
 
 // ---------------------------------------------------------------- host-pointer path
@@ -422,31 +430,43 @@ static int run_streamed(const Args &d, float *host_out, cudaStream_t s)
     return rc;
 }
 
-static int run_host(const Args &a, cudaStream_t s)
+// Device copies of the five input arrays of a host-pointer call (in `io`);
+// *d = a with its input pointers replaced.
+static int copy_inputs(const Args &a, Scratch &io, cudaStream_t s, Args *d)
 {
     int rc;
     const size_t SC = a.S * a.C;
     const size_t n_tsc = a.T * SC;
-    const size_t out_n = a.T * a.n_corr * (a.sum_mode ? 1 : SC);
-    const size_t n[6] = {n_tsc * a.L, n_tsc, n_tsc, SC * a.N, n_tsc, out_n};
-    float *buf[6];
+    const size_t n[5] = {n_tsc * a.L, n_tsc, n_tsc, SC * a.N, n_tsc};
+    const void *src[5] = {a.tpl, a.sst, a.mo, a.data, a.w};
+    float *buf[5];
+    for (int i = 0; i < 5; i++) {
+        if ((rc = io.get(&buf[i], n[i], "input copies")))
+            return rc;
+        if ((rc = cuda_status(cudaMemcpyAsync(buf[i], src[i], n[i] * 4, cudaMemcpyHostToDevice, s),
+                              "copying inputs to the device")))
+            return rc;
+    }
+    *d = a;
+    d->tpl = buf[0];
+    d->sst = buf[1];
+    d->mo = reinterpret_cast<const int *>(buf[2]);
+    d->data = buf[3];
+    d->w = buf[4];
+    return FMF_OK;
+}
+
+static int run_host(const Args &a, cudaStream_t s)
+{
+    int rc;
+    const size_t out_n = a.T * a.n_corr * (a.sum_mode ? 1 : a.S * a.C);
     {
         Scratch io(s);  // device copies of the arguments, freed in stream order
-        for (int i = 0; i < 6; i++)
-            if ((rc = io.get(&buf[i], n[i], "input/output copies")))
-                return rc;
-        const void *src[5] = {a.tpl, a.sst, a.mo, a.data, a.w};
-        for (int i = 0; i < 5; i++)
-            if ((rc = cuda_status(cudaMemcpyAsync(buf[i], src[i], n[i] * 4, cudaMemcpyHostToDevice, s),
-                                  "copying inputs to the device")))
-                return rc;
-        Args d = a;
-        d.tpl = buf[0];
-        d.sst = buf[1];
-        d.mo = reinterpret_cast<const int *>(buf[2]);
-        d.data = buf[3];
-        d.w = buf[4];
-        d.out = buf[5];
+        Args d;
+        float *out;
+        if ((rc = copy_inputs(a, io, s, &d)) || (rc = io.get(&out, out_n, "output copy")))
+            return rc;
+        d.out = out;
         if ((rc = run_streamed(d, a.out, s)))
             return rc;
     }
@@ -468,6 +488,156 @@ static int entry(const Args &a, void *stream)
     if (a.flags & FMF_FLAG_DEVICE_POINTERS)
         return run_device(a, s);
     return run_host(a, s);
+}
+
+// ---------------------------------------------------------------- detection
+struct DetectOut {
+    float n_mad;
+    size_t min_sep, max_det;
+    float *med, *mad, *thr;
+    int *count, *lag;
+    float *val;
+};
+
+// Device buffers standing in for host outputs (host-pointer calls).
+struct DetectDev {
+    float *med = nullptr, *mad = nullptr, *thr = nullptr, *val = nullptr;
+    int *count = nullptr, *lag = nullptr;
+};
+
+static int detect_outputs(const DetectOut &o, size_t T, bool device, Scratch &ws, DetectDev *d)
+{
+    int rc;
+    if (device) {
+        d->med = o.med;
+        d->mad = o.mad;
+        d->thr = o.thr;
+        d->count = o.count;
+        d->lag = o.lag;
+        d->val = o.val;
+        return FMF_OK;
+    }
+    const size_t nd = T * o.max_det;
+    if ((rc = ws.get(&d->med, T, "detection outputs")) || (rc = ws.get(&d->mad, T, "detection outputs")) ||
+        (rc = ws.get(&d->thr, T, "detection outputs")) || (rc = ws.get(&d->count, T, "detection outputs")) ||
+        (rc = ws.get(&d->lag, nd > 0 ? nd : 1, "detection outputs")) ||
+        (rc = ws.get(&d->val, nd > 0 ? nd : 1, "detection outputs")))
+        return rc;
+    return FMF_OK;
+}
+
+static int detect_copy_back(const DetectOut &o, size_t T, const DetectDev &d, cudaStream_t s)
+{
+    int rc;
+    const size_t nd = T * o.max_det;
+    struct {
+        void *dst;
+        const void *src;
+        size_t bytes;
+    } cp[6] = {{o.med, d.med, T * 4}, {o.mad, d.mad, T * 4}, {o.thr, d.thr, T * 4},
+               {o.count, d.count, T * 4}, {o.lag, d.lag, nd * 4}, {o.val, d.val, nd * 4}};
+    for (auto &c : cp)
+        if (c.dst && c.bytes &&
+            (rc = cuda_status(cudaMemcpyAsync(c.dst, c.src, c.bytes, cudaMemcpyDeviceToHost, s),
+                              "copying detections to the host")))
+            return rc;
+    if ((rc = cuda_status(cudaStreamSynchronize(s), "detection")))
+        return rc;
+    return detect_finish_host(o.count, T);
+}
+
+static int detect_entry(const float *cc, size_t T, size_t n_corr, const int *begin, const int *end,
+                        const DetectOut &o, int flags, cudaStream_t s)
+{
+    int rc;
+    if ((rc = validate_detect(T, n_corr, o.n_mad, o.min_sep, o.max_det, o.count, o.lag, o.val)))
+        return rc;
+    if (!cc)
+        return set_error(FMF_ERR_ARG, "detection: null cc");
+    if ((begin == nullptr) != (end == nullptr))
+        return set_error(FMF_ERR_ARG, "detection: give both lag_begin and lag_end, or neither");
+    const bool device = flags & FMF_FLAG_DEVICE_POINTERS;
+    if (!device && begin)
+        for (size_t t = 0; t < T; t++)
+            if (begin[t] < 0 || end[t] < begin[t] || (size_t)end[t] > n_corr)
+                return set_error(FMF_ERR_ARG, "detection: lag window [%d, %d) of template %zu is not "
+                                              "inside [0, %zu)", begin[t], end[t], t, n_corr);
+    keep_pool_cached();
+    cudaGetLastError();
+    Scratch ws(s);
+    DetectDev d;
+    if ((rc = detect_outputs(o, T, device, ws, &d)))
+        return rc;
+    if (device)
+        return detect_device(cc, (int)T, (int)n_corr, n_corr, begin, end, o.n_mad, (int)o.min_sep,
+                             (int)o.max_det, d.med, d.mad, d.thr, d.count, d.lag, d.val, ws, s);
+    int *range = nullptr;
+    if (begin) {
+        if ((rc = ws.get(&range, 2 * T, "lag windows")) ||
+            (rc = cuda_status(cudaMemcpyAsync(range, begin, T * 4, cudaMemcpyHostToDevice, s),
+                              "copying lag windows")) ||
+            (rc = cuda_status(cudaMemcpyAsync(range + T, end, T * 4, cudaMemcpyHostToDevice, s),
+                              "copying lag windows")))
+            return rc;
+    }
+    // rows in chunks of at most 1 GiB of device memory
+    size_t per = ((size_t)1 << 30) / (n_corr * sizeof(float));
+    per = per < 1 ? 1 : (per > T ? T : per);
+    float *rows;
+    if ((rc = ws.get(&rows, per * n_corr, "cc rows")))
+        return rc;
+    for (size_t t0 = 0; t0 < T; t0 += per) {
+        const size_t nt = T - t0 < per ? T - t0 : per;
+        if ((rc = cuda_status(cudaMemcpyAsync(rows, cc + t0 * n_corr, nt * n_corr * 4,
+                                              cudaMemcpyHostToDevice, s),
+                              "copying cc rows to the device")))
+            return rc;
+        const size_t od = t0 * o.max_det;
+        if ((rc = detect_device(rows, (int)nt, (int)n_corr, n_corr, range ? range + t0 : nullptr,
+                                range ? range + T + t0 : nullptr, o.n_mad, (int)o.min_sep,
+                                (int)o.max_det, d.med + t0, d.mad + t0, d.thr + t0, d.count + t0,
+                                d.lag + od, d.val + od, ws, s)))
+            return rc;
+    }
+    return detect_copy_back(o, T, d, s);
+}
+
+// Search (network sum) into a device buffer, then detection over each
+// template's valid lag range; only the detections leave the device.
+static int search_detect_entry(const Args &a0, const DetectOut &o, cudaStream_t s)
+{
+    int rc;
+    Args a = a0;
+    a.sum_mode = 1;
+    a.out = reinterpret_cast<float *>(o.count);  // placeholder for the argument check
+    if ((rc = validate_args(a)) ||
+        (rc = validate_detect(a.T, a.n_corr, o.n_mad, o.min_sep, o.max_det, o.count, o.lag, o.val)))
+        return rc;
+    keep_pool_cached();
+    cudaGetLastError();
+    const bool device = a.flags & FMF_FLAG_DEVICE_POINTERS;
+    Scratch ws(s);
+    Args d = a;
+    if (!device && (rc = copy_inputs(a, ws, s, &d)))
+        return rc;
+    float *cc;
+    if ((rc = ws.get(&cc, a.T * a.n_corr, "cc sums")))
+        return rc;
+    d.out = cc;
+    Problem P;
+    if ((rc = run_device_ws(d, s, ws, &P)))
+        return rc;
+    DetectDev dd;
+    if ((rc = detect_outputs(o, a.T, device, ws, &dd)) ||
+        (rc = detect_device(cc, (int)a.T, (int)a.n_corr, a.n_corr, P.k_lo, P.k_hi, o.n_mad,
+                            (int)o.min_sep, (int)o.max_det, dd.med, dd.mad, dd.thr, dd.count, dd.lag,
+                            dd.val, ws, s)))
+        return rc;
+    if (device)
+        return FMF_OK;
+    if ((rc = detect_copy_back(o, a.T, dd, s)))
+        return rc;
+    return a.precision != FMF_PREC_FP32 ? collect_device_errors() : FMF_OK;
 }
 
 }  // namespace fmf
@@ -527,6 +697,53 @@ int matched_filter(const float *templates, const float *sum_square_templates, co
     if (rc != FMF_OK)
         fprintf(stderr, "fmf_gb300 matched_filter failed (status %d): %s\n", rc, fmf::g_msg);
     return rc;
+}
+
+int fmf_detect(const float *cc, size_t n_templates, size_t n_corr, const int *lag_begin,
+               const int *lag_end, float n_mad, size_t min_separation, size_t max_detections,
+               float *median_out, float *mad_out, float *threshold_out, int *count_out, int *lag_out,
+               float *value_out, int flags, void *stream)
+{
+    fmf::clear_error();
+    fmf::g_launches = 0;
+    const fmf::DetectOut o{n_mad,      min_separation, max_detections, median_out, mad_out,
+                           threshold_out, count_out,   lag_out,        value_out};
+    return fmf::detect_entry(cc, n_templates, n_corr, lag_begin, lag_end, o, flags,
+                             (cudaStream_t)stream);
+}
+
+int fmf_matched_filter_detect(const float *templates, const float *sum_square_templates,
+                              const int *moveouts, const float *data, const float *weights,
+                              size_t step, size_t n_samples_template, size_t n_samples_data,
+                              size_t n_templates, size_t n_stations, size_t n_components,
+                              size_t n_corr, int normalize, int precision, float n_mad,
+                              size_t min_separation, size_t max_detections, float *median_out,
+                              float *mad_out, float *threshold_out, int *count_out, int *lag_out,
+                              float *value_out, int flags, void *stream)
+{
+    fmf::clear_error();
+    fmf::g_launches = 0;
+    fmf::Args a;
+    a.tpl = templates;
+    a.sst = sum_square_templates;
+    a.mo = moveouts;
+    a.data = data;
+    a.w = weights;
+    a.out = nullptr;
+    a.step = step;
+    a.L = n_samples_template;
+    a.N = n_samples_data;
+    a.T = n_templates;
+    a.S = n_stations;
+    a.C = n_components;
+    a.n_corr = n_corr;
+    a.normalize = normalize;
+    a.sum_mode = 1;
+    a.precision = precision;
+    a.flags = flags;
+    const fmf::DetectOut o{n_mad,      min_separation, max_detections, median_out, mad_out,
+                           threshold_out, count_out,   lag_out,        value_out};
+    return fmf::search_detect_entry(a, o, (cudaStream_t)stream);
 }
 
 int fmf_last_error(char *buf, size_t len)

@@ -112,4 +112,14 @@ void tc_subset(const TcProb *full, int t0, int nt, TcProb *out);
 int launch_plain(const Problem &P, cudaStream_t stream);
 int launch_plain_all(const Problem &P, cudaStream_t stream);
 int device_error_word(unsigned **out);
+
+// Detection on network-summed rows (fmf_detect.cu).
+int detect_device(const float *cc, int T, int n_corr, size_t ld, const int *begin, const int *end,
+                  float n_mad, int min_sep, int max_det, float *med_out, float *mad_out,
+                  float *thr_out, int *count_out, int *lag_out, float *val_out, Scratch &ws,
+                  cudaStream_t s);
+int validate_detect(size_t T, size_t n_corr, float n_mad, size_t min_sep, size_t max_det,
+                    const void *count_out, const void *lag_out, const void *val_out);
+int detect_finish_host(const int *count_host, size_t T);
+int detect_capacity();
 }  // namespace fmf

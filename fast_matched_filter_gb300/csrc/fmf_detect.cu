@@ -1,0 +1,483 @@
+// fmf_detect.cu -- detection on network-summed correlation rows, on the GPU.
+//
+// The callers of the matched filter threshold each template's summed cc
+// trace and pick its peaks.  Done on the host this needs the whole (T, n_corr)
+// result copied out (8.6 GB for 500 templates over a day at 100 Hz); done
+// here only the detections leave the device.  There is no reference
+// counterpart: the semantics are the usual robust threshold and scipy's peak
+// finder, so a caller's numpy/scipy code gives the same answers.
+//
+// For each template row cc[t][0:n_corr) and its lag window [begin_t, end_t):
+//   median = numpy.median of the window (float32: the mean of the two middle
+//            values, summed in float32, for an even count)
+//   mad    = numpy.median of |x - median| (float32 differences)
+//   thr    = median + n_mad * mad (float32; multiply, then add -- no fused
+//            multiply-add)
+//   peaks  = scipy.signal.find_peaks(window, height=thr, distance=min_separation):
+//            local maxima (a flat top counts once, at its middle sample rounded
+//            down; the window's first and last samples never count) whose value
+//            is >= thr; then, from the highest down (equal heights: the later lag
+//            first), each peak still kept removes the peaks closer than
+//            min_separation lags on either side.
+//
+// The order statistics are exact: a radix selection over the order-preserving
+// 32-bit image of the float values, three passes of 11, 11 and 10 bits, each a
+// histogram of the elements that match the bits chosen so far.  Both middle
+// ranks are tracked at once.  Peaks are gathered into a list per template
+// (capacity kDetCap) and filtered by one thread block per template: a sort by
+// lag, a sort by height, and the greedy distance filter.
+//
+// Every launch is stream-ordered and the state lives on the device, so a
+// detection run needs no host round trip and can be captured in a graph.
+#include <cmath>
+
+#include "fmf_common.cuh"
+
+namespace fmf {
+namespace {
+
+constexpr int kDetBins = 2048;            // histogram bins of the 11-bit passes
+constexpr int kDetThreads = 256;          // histogram / peak kernels
+constexpr int kDetSelectThreads = 1024;   // per-template filter kernel
+constexpr int kDetChunk = 1024;           // templates per round of scratch
+constexpr int kDetCap = 16384;            // candidate peaks per template row
+
+struct DetState {
+    int begin, end;        // lag window of the row
+    unsigned prefix[2];    // key bits chosen so far for the lower / upper middle rank
+    int rank[2];           // rank still to find inside the chosen bucket
+    float med, mad, thr;
+    int n_cand;            // local maxima at or above thr (may exceed the capacity)
+};
+
+// Order-preserving image of a float: a < b  <=>  key(a) < key(b) (for non-NaN
+// values; -0 sorts just below +0).
+__device__ __forceinline__ unsigned order_key(float x)
+{
+    const unsigned u = __float_as_uint(x);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+
+__device__ __forceinline__ float key_value(unsigned k)
+{
+    return __uint_as_float((k & 0x80000000u) ? (k & 0x7fffffffu) : ~k);
+}
+
+// Digit of pass p: bits [shift, shift + width) of the key.
+__device__ __forceinline__ int pass_shift(int p) { return p == 0 ? 21 : (p == 1 ? 10 : 0); }
+__device__ __forceinline__ unsigned pass_bins(int p) { return p == 2 ? 1024u : 2048u; }
+__device__ __forceinline__ unsigned pass_high_mask(int p)
+{
+    return p == 0 ? 0u : (p == 1 ? 0xffe00000u : 0xfffffc00u);
+}
+
+__global__ void det_init_kernel(DetState *__restrict__ st, int T, int n_corr,
+                                const int *__restrict__ begin, const int *__restrict__ end)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= T)
+        return;
+    int b = 0, e = n_corr;
+    if (begin) {
+        b = min(max(begin[t], 0), n_corr);
+        e = min(max(end[t], b), n_corr);
+    }
+    const int n = e - b;
+    DetState s;
+    s.begin = b;
+    s.end = e;
+    s.prefix[0] = s.prefix[1] = 0u;
+    s.rank[0] = n > 0 ? (n - 1) / 2 : 0;
+    s.rank[1] = n / 2;
+    s.med = s.mad = s.thr = __int_as_float(0x7fc00000);  // NaN until computed
+    s.n_cand = 0;
+    st[t] = s;
+}
+
+// One selection pass: histogram of the current digit over the elements whose
+// higher key bits equal a rank's prefix.  mode 0 keys the values, mode 1 keys
+// |x - median|.  Grid: (blocks per row, templates).
+__global__ void __launch_bounds__(kDetThreads)
+det_hist_kernel(const float *__restrict__ cc, size_t ld, const DetState *__restrict__ st,
+                unsigned *__restrict__ hist, int pass, int mode)
+{
+    __shared__ unsigned h[2 * kDetBins];
+    const int t = blockIdx.y;
+    const DetState s = st[t];
+    const long long n = s.end - s.begin;
+    if (n <= 0)
+        return;  // uniform over the block, before any barrier
+    for (int i = threadIdx.x; i < 2 * kDetBins; i += kDetThreads)
+        h[i] = 0u;
+    __syncthreads();
+    const int shift = pass_shift(pass);
+    const unsigned dmask = pass_bins(pass) - 1u;
+    const unsigned high = pass_high_mask(pass);
+    const unsigned p0 = s.prefix[0], p1 = s.prefix[1];
+    const bool two = p0 != p1;  // the two middle ranks sit in different buckets
+    const float med = s.med;
+    const float *row = cc + (size_t)t * ld + s.begin;
+    const int lane = threadIdx.x & 31;
+    constexpr int kWarps = kDetThreads / 32;
+    const long long chunks = (n + 127) / 128;  // 128 consecutive values per warp step
+    for (long long c = (long long)blockIdx.x * kWarps + (threadIdx.x >> 5); c < chunks;
+         c += (long long)gridDim.x * kWarps) {
+        float v[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            const long long i = c * 128 + u * 32 + lane;
+            v[u] = i < n ? row[i] : 0.f;
+        }
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            const bool ok = c * 128 + u * 32 + lane < n;
+            const float x = mode == 0 ? v[u] : fabsf(__fsub_rn(v[u], med));
+            const unsigned key = order_key(x);
+            const unsigned dig = (key >> shift) & dmask;
+            const bool m0 = ok && (key & high) == p0;
+            // lanes with the same digit add once (sentinel ~0 for lanes that do not count)
+            unsigned g = __match_any_sync(0xffffffffu, m0 ? dig : 0xffffffffu);
+            if (m0 && (__ffs(g) - 1) == lane)
+                atomicAdd(&h[dig], __popc(g));
+            if (two) {
+                const bool m1 = ok && (key & high) == p1;
+                g = __match_any_sync(0xffffffffu, m1 ? dig : 0xffffffffu);
+                if (m1 && (__ffs(g) - 1) == lane)
+                    atomicAdd(&h[kDetBins + dig], __popc(g));
+            }
+        }
+    }
+    __syncthreads();
+    unsigned *gh = hist + (size_t)t * 2 * kDetBins;
+    for (int i = threadIdx.x; i < (two ? 2 : 1) * kDetBins; i += kDetThreads) {
+        const unsigned c = h[i];
+        if (c)
+            atomicAdd(gh + i, c);
+    }
+}
+
+// Picks each rank's bucket from the pass's histogram (one warp per template),
+// clears the histogram, and after the last pass turns the two keys into the
+// median (mode 0) or the MAD and the threshold (mode 1).
+__global__ void det_resolve_kernel(DetState *__restrict__ st, unsigned *__restrict__ hist, int pass,
+                                   int mode, float n_mad)
+{
+    const int t = blockIdx.x;
+    const int lane = threadIdx.x;
+    DetState s = st[t];
+    const int n = s.end - s.begin;
+    if (n <= 0)
+        return;
+    unsigned *gh = hist + (size_t)t * 2 * kDetBins;
+    const int per = (int)pass_bins(pass) / 32;  // bins per lane
+    const int shift = pass_shift(pass);
+    const bool two = s.prefix[0] != s.prefix[1];
+    for (int r = 0; r < 2; r++) {
+        const unsigned *h = gh + (two ? r : 0) * kDetBins;
+        unsigned sum = 0;
+        for (int i = 0; i < per; i++)
+            sum += h[lane * per + i];
+        unsigned inc = sum;
+        for (int o = 1; o < 32; o <<= 1) {
+            const unsigned y = __shfl_up_sync(0xffffffffu, inc, o);
+            if (lane >= o)
+                inc += y;
+        }
+        const unsigned exc = inc - sum;
+        const unsigned rk = (unsigned)s.rank[r];
+        const unsigned found = __ballot_sync(0xffffffffu, rk >= exc && rk < inc);
+        const int src = found ? __ffs(found) - 1 : 0;
+        unsigned bin = 0, before = 0;
+        if (lane == src) {
+            unsigned c = exc;
+            int i = 0;
+            for (; i < per - 1; i++) {
+                const unsigned hv = h[lane * per + i];
+                if (rk < c + hv)
+                    break;
+                c += hv;
+            }
+            bin = (unsigned)(lane * per + i);
+            before = c;
+        }
+        bin = __shfl_sync(0xffffffffu, bin, src);
+        before = __shfl_sync(0xffffffffu, before, src);
+        s.prefix[r] |= bin << shift;
+        s.rank[r] = (int)(rk - before);
+    }
+    __syncwarp();
+    for (int i = lane; i < 2 * kDetBins; i += 32)
+        gh[i] = 0u;
+    if (pass == 2) {
+        const float a = key_value(s.prefix[0]), b = key_value(s.prefix[1]);
+        const float v = (n & 1) ? a : __fmul_rn(__fadd_rn(a, b), 0.5f);
+        if (mode == 0) {
+            s.med = v;
+        } else {
+            s.mad = v;
+            s.thr = __fadd_rn(s.med, __fmul_rn(n_mad, v));
+        }
+        s.prefix[0] = s.prefix[1] = 0u;
+        s.rank[0] = (n - 1) / 2;
+        s.rank[1] = n / 2;
+    }
+    if (lane == 0)
+        st[t] = s;
+}
+
+// Local maxima at or above the threshold, appended (unordered) to the
+// template's candidate list.  Grid: (blocks per row, templates).
+__global__ void __launch_bounds__(kDetThreads)
+det_peaks_kernel(const float *__restrict__ cc, size_t ld, DetState *__restrict__ st,
+                 int2 *__restrict__ cand, int cap)
+{
+    const int t = blockIdx.y;
+    const long long b = st[t].begin, e = st[t].end;
+    const float thr = st[t].thr;
+    if (e - b < 3)
+        return;
+    const float *row = cc + (size_t)t * ld;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = b + 1 + (long long)blockIdx.x * blockDim.x + threadIdx.x; i < e - 1; i += stride) {
+        const float x = row[i];
+        if (!(x >= thr))
+            continue;  // a flat top has the value of its rising sample
+        if (!(row[i - 1] < x))
+            continue;
+        long long j = i + 1;
+        while (j < e - 1 && row[j] == x)
+            j++;
+        if (row[j] < x) {
+            const int peak = (int)((i + j - 1) >> 1);
+            const int slot = atomicAdd(&st[t].n_cand, 1);
+            if (slot < cap)
+                cand[(size_t)t * cap + slot] = make_int2(peak, __float_as_int(x));
+        }
+    }
+}
+
+// Ascending bitonic sort of P (a power of two) keys in shared memory.
+__device__ void bitonic_sort(unsigned long long *a, int P)
+{
+    for (int k = 2; k <= P; k <<= 1)
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            for (int i = threadIdx.x; i < P; i += blockDim.x) {
+                const int l = i ^ j;
+                if (l > i) {
+                    const unsigned long long x = a[i], y = a[l];
+                    if ((x > y) == ((i & k) == 0)) {
+                        a[i] = y;
+                        a[l] = x;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+}
+
+// Distance filter and output of one template (one block per template).
+// Shared memory: keys (8 B), lags (4 B) and keep flags (1 B) per candidate.
+__global__ void __launch_bounds__(kDetSelectThreads)
+det_select_kernel(const DetState *__restrict__ st, const int2 *__restrict__ cand, int cap, int min_sep,
+                  int max_det, float *med_out, float *mad_out, float *thr_out, int *count_out,
+                  int *lag_out, float *val_out)
+{
+    extern __shared__ unsigned long long sk[];
+    int *lag = reinterpret_cast<int *>(sk + cap);
+    unsigned char *keep = reinterpret_cast<unsigned char *>(lag + cap);
+    __shared__ int warp_tot[kDetSelectThreads / 32];
+    const int t = blockIdx.x;
+    const DetState s = st[t];
+    if (threadIdx.x == 0) {
+        if (med_out)
+            med_out[t] = s.med;
+        if (mad_out)
+            mad_out[t] = s.mad;
+        if (thr_out)
+            thr_out[t] = s.thr;
+    }
+    const int m = s.n_cand;
+    if (m > cap) {
+        if (threadIdx.x == 0)
+            count_out[t] = -1;  // capacity exceeded: no peaks reported for this row
+        return;
+    }
+    int P = 1;
+    while (P < m)
+        P <<= 1;
+    const int2 *c = cand + (size_t)t * cap;
+    // 1. order by lag (lags are distinct)
+    for (int i = threadIdx.x; i < P; i += blockDim.x)
+        sk[i] = i < m ? ((unsigned long long)(unsigned)c[i].x << 32) | (unsigned)c[i].y : ~0ull;
+    __syncthreads();
+    bitonic_sort(sk, P);
+    // 2. order by height, then by lag (position in lag order)
+    for (int i = threadIdx.x; i < P; i += blockDim.x) {
+        const unsigned long long k = sk[i];
+        if (i < m) {
+            lag[i] = (int)(k >> 32);
+            keep[i] = 1;
+            sk[i] = ((unsigned long long)order_key(__uint_as_float((unsigned)k)) << 32) | (unsigned)i;
+        } else {
+            sk[i] = 0ull;
+        }
+    }
+    __syncthreads();
+    bitonic_sort(sk, P);
+    // 3. greedy from the highest: each kept peak removes its close neighbours
+    if (threadIdx.x == 0) {
+        for (int q = P - 1; q >= P - m; q--) {
+            const int j = (int)(unsigned)sk[q];
+            if (!keep[j])
+                continue;
+            const int lj = lag[j];
+            for (int k = j - 1; k >= 0 && lj - lag[k] < min_sep; k--)
+                keep[k] = 0;
+            for (int k = j + 1; k < m && lag[k] - lj < min_sep; k++)
+                keep[k] = 0;
+        }
+    }
+    __syncthreads();
+    // 4. values back into lag order (sk[j] = value bits of the peak at lag position j)
+    constexpr int kPer = 16;  // P <= 16384 = kPer * kDetSelectThreads
+    unsigned long long held[kPer];
+#pragma unroll
+    for (int u = 0; u < kPer; u++) {
+        const int q = threadIdx.x + u * kDetSelectThreads;
+        held[u] = q < P ? sk[q] : 0ull;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int u = 0; u < kPer; u++) {
+        const int q = threadIdx.x + u * kDetSelectThreads;
+        if (q < P && q >= P - m) {
+            const int j = (int)(unsigned)held[u];
+            sk[j] = __float_as_uint(key_value((unsigned)(held[u] >> 32)));
+        }
+    }
+    __syncthreads();
+    // 5. kept peaks in lag order: block-wide exclusive scan of the keep flags
+    const int span = (m + kDetSelectThreads - 1) / kDetSelectThreads;
+    const int i0 = threadIdx.x * span, i1 = min(i0 + span, m);
+    int cnt = 0;
+    for (int i = i0; i < i1; i++)
+        cnt += keep[i];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    int inc = cnt;
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o)
+            inc += y;
+    }
+    if (lane == 31)
+        warp_tot[wid] = inc;
+    __syncthreads();
+    int base = 0, total = 0;
+    for (int w = 0; w < kDetSelectThreads / 32; w++) {
+        if (w < wid)
+            base += warp_tot[w];
+        total += warp_tot[w];
+    }
+    int pos = base + inc - cnt;
+    for (int i = i0; i < i1; i++) {
+        if (!keep[i])
+            continue;
+        if (pos < max_det) {
+            lag_out[(size_t)t * max_det + pos] = lag[i];
+            val_out[(size_t)t * max_det + pos] = __uint_as_float((unsigned)sk[i]);
+        }
+        pos++;
+    }
+    if (threadIdx.x == 0)
+        count_out[t] = total;
+}
+
+size_t select_smem(int cap) { return (size_t)cap * (8 + 4 + 1); }
+
+}  // namespace
+
+// Detection over T rows of device-resident cc (row stride ld floats), every
+// pointer a device pointer.  Stream-ordered; no host synchronisation.
+int detect_device(const float *cc, int T, int n_corr, size_t ld, const int *begin, const int *end,
+                  float n_mad, int min_sep, int max_det, float *med_out, float *mad_out,
+                  float *thr_out, int *count_out, int *lag_out, float *val_out, Scratch &ws,
+                  cudaStream_t s)
+{
+    int rc;
+    const int chunk = T < kDetChunk ? T : kDetChunk;
+    DetState *st;
+    unsigned *hist;
+    int2 *cand;
+    if ((rc = ws.get(&st, (size_t)chunk, "detection state")) ||
+        (rc = ws.get(&hist, (size_t)chunk * 2 * kDetBins, "detection histograms")) ||
+        (rc = ws.get(&cand, (size_t)chunk * kDetCap, "candidate peaks")))
+        return rc;
+    cudaError_t e = cudaFuncSetAttribute(det_select_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)select_smem(kDetCap));
+    if (e != cudaSuccess)
+        return set_error(FMF_ERR_CUDA, "detection filter shared memory: %s", cudaGetErrorString(e));
+    if ((e = cudaMemsetAsync(hist, 0, (size_t)chunk * 2 * kDetBins * sizeof(unsigned), s)) != cudaSuccess)
+        return set_error(FMF_ERR_CUDA, "clearing the detection histograms: %s", cudaGetErrorString(e));
+    for (int t0 = 0; t0 < T; t0 += chunk) {
+        const int nt = T - t0 < chunk ? T - t0 : chunk;
+        const float *rows = cc + (size_t)t0 * ld;
+        // enough blocks per row to fill 152 SMs several times over
+        long long per_row = (152LL * 8 + nt - 1) / nt;
+        const long long row_cap = ((long long)n_corr + 1023) / 1024;
+        if (per_row > row_cap)
+            per_row = row_cap;
+        if (per_row < 1)
+            per_row = 1;
+        const dim3 grid((unsigned)per_row, (unsigned)nt);
+        det_init_kernel<<<(nt + 127) / 128, 128, 0, s>>>(st, nt, n_corr, begin ? begin + t0 : nullptr,
+                                                         end ? end + t0 : nullptr);
+        for (int mode = 0; mode < 2; mode++)
+            for (int pass = 0; pass < 3; pass++) {
+                det_hist_kernel<<<grid, kDetThreads, 0, s>>>(rows, ld, st, hist, pass, mode);
+                det_resolve_kernel<<<nt, 32, 0, s>>>(st, hist, pass, mode, n_mad);
+            }
+        det_peaks_kernel<<<grid, kDetThreads, 0, s>>>(rows, ld, st, cand, kDetCap);
+        det_select_kernel<<<nt, kDetSelectThreads, select_smem(kDetCap), s>>>(
+            st, cand, kDetCap, min_sep, max_det, med_out ? med_out + t0 : nullptr,
+            mad_out ? mad_out + t0 : nullptr, thr_out ? thr_out + t0 : nullptr, count_out + t0,
+            lag_out + (size_t)t0 * max_det, val_out + (size_t)t0 * max_det);
+        count_launch(15);
+        if ((rc = check_launch("detection kernels")))
+            return rc;
+    }
+    return FMF_OK;
+}
+
+int validate_detect(size_t T, size_t n_corr, float n_mad, size_t min_sep, size_t max_det,
+                    const void *count_out, const void *lag_out, const void *val_out)
+{
+    if (T < 1 || n_corr < 1)
+        return set_error(FMF_ERR_ARG, "detection: sizes must be positive (T=%zu n_corr=%zu)", T, n_corr);
+    if (T > (size_t)INT_MAX || n_corr > (size_t)INT_MAX || max_det > (size_t)INT_MAX / 2 ||
+        min_sep > (size_t)INT_MAX)
+        return set_error(FMF_ERR_ARG, "detection: sizes exceed the 32-bit index range");
+    if (min_sep < 1)
+        return set_error(FMF_ERR_ARG, "detection: min_separation must be at least 1");
+    if (!std::isfinite(n_mad))
+        return set_error(FMF_ERR_ARG, "detection: n_mad must be finite");
+    if (!count_out || (max_det > 0 && (!lag_out || !val_out)))
+        return set_error(FMF_ERR_ARG, "detection: null output array");
+    return FMF_OK;
+}
+
+// Host copies of the detection outputs: counts of -1 (capacity exceeded) turn
+// into an error status.
+int detect_finish_host(const int *count_host, size_t T)
+{
+    for (size_t t = 0; t < T; t++)
+        if (count_host[t] < 0)
+            return set_error(FMF_ERR_UNSUPPORTED,
+                             "detection: template %zu has more than %d local maxima above its threshold; "
+                             "raise n_mad",
+                             t, kDetCap);
+    return FMF_OK;
+}
+
+int detect_capacity() { return kDetCap; }
+
+}  // namespace fmf

@@ -184,6 +184,51 @@ FMF_API int fmf_matched_filter_variable_ex(const float *templates, const float *
                                            size_t n_components, size_t n_corr, float *cc_sum,
                                            int normalize, int flags, void *stream);
 
+/*
+ * Detection on network-summed cc rows (no reference counterpart: what the
+ * reference's callers do next with cc_sum, done on the GPU so the rows need
+ * not be copied out).  For each template t, over lags [lag_begin[t],
+ * lag_end[t]) of row t of cc (T, n_corr) -- the whole row when both arrays
+ * are NULL:
+ *   median_out[t]    = numpy.median of the window (float32 arithmetic)
+ *   mad_out[t]       = numpy.median of |x - median|
+ *   threshold_out[t] = median + n_mad * mad (float32, no fused multiply-add)
+ *   peaks            = scipy.signal.find_peaks(window, height=threshold,
+ *                      distance=min_separation); equal heights keep the later lag
+ *   count_out[t]     = number of peaks, or -1 if more than FMF_DETECT_CAPACITY
+ *                      local maxima reach the threshold (no peaks reported)
+ *   lag_out / value_out (T, max_detections): the first min(count,
+ *                      max_detections) peaks in lag order (absolute lag index).
+ * median_out, mad_out, threshold_out may be NULL; lag_out and value_out may be
+ * NULL when max_detections is 0.  min_separation >= 1.  Rows must be free of
+ * NaN.  Host pointers: synchronous, FMF_ERR_UNSUPPORTED when a row exceeded
+ * the capacity.  FMF_FLAG_DEVICE_POINTERS: every array on the device,
+ * asynchronous on `stream`; check count_out for -1.
+ */
+#define FMF_DETECT_CAPACITY 16384
+FMF_API int fmf_detect(const float *cc, size_t n_templates, size_t n_corr, const int *lag_begin,
+                       const int *lag_end, float n_mad, size_t min_separation, size_t max_detections,
+                       float *median_out, float *mad_out, float *threshold_out, int *count_out,
+                       int *lag_out, float *value_out, int flags, void *stream);
+
+/*
+ * Search and detection in one call (no reference counterpart): the network-sum
+ * search of fmf_matched_filter_ex (arguments as there, sum_cc_mode = 1) into
+ * device memory, then fmf_detect over each template's valid lag range (the
+ * lags the search can produce: the reference's per-template start/stop,
+ * matched_filter.c:53-76).  Only the detections are returned; the (T, n_corr)
+ * cc rows never leave the device.
+ */
+FMF_API int fmf_matched_filter_detect(const float *templates, const float *sum_square_templates,
+                                      const int *moveouts, const float *data, const float *weights,
+                                      size_t step, size_t n_samples_template, size_t n_samples_data,
+                                      size_t n_templates, size_t n_stations, size_t n_components,
+                                      size_t n_corr, int normalize, int precision, float n_mad,
+                                      size_t min_separation, size_t max_detections,
+                                      float *median_out, float *mad_out, float *threshold_out,
+                                      int *count_out, int *lag_out, float *value_out, int flags,
+                                      void *stream);
+
 /* Copies the calling thread's last error message (NUL-terminated, truncated
  * to len) and returns its status.  The reference printed and exited instead
  * (matched_filter.cu:30-39, 236-242, 286-299). */

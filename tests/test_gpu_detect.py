@@ -1,0 +1,130 @@
+"""GPU detection (fmf_detect, fmf_matched_filter_detect) against the oracle
+(needs a GB300).  Bar: median, MAD and threshold equal to numpy's float32
+values exactly, the same peak lags and values, the same counts."""
+import numpy as np
+import pytest
+
+import fast_matched_filter_gb300 as fmf
+from fast_matched_filter_gb300 import FMFError
+from oracle import detect as odet
+
+pytestmark = pytest.mark.gpu
+
+
+def same_float(a, b):
+    return (np.isnan(a) and np.isnan(b)) or a == b
+
+
+def assert_matches(det, cc, n_mad, sep, max_det, begin=None, end=None):
+    ref = odet.detect(cc, n_mad, sep, begin, end)
+    for t, (med, mad, thr, lags, vals) in enumerate(ref):
+        assert same_float(det.median[t], med), (t, det.median[t], med)
+        assert same_float(det.mad[t], mad), (t, det.mad[t], mad)
+        assert same_float(det.threshold[t], thr), (t, det.threshold[t], thr)
+        assert det.count[t] == lags.size, (t, det.count[t], lags.size)
+        k = min(lags.size, max_det)
+        assert np.array_equal(det.lags[t], lags[:k]), t
+        assert np.array_equal(det.values[t], vals[:k]), t
+
+
+def cc_rows(seed, T, n, quantise=False):
+    rng = np.random.default_rng(seed)
+    x = np.stack([np.convolve(rng.standard_normal(n), np.hanning(11), mode="same")
+                  for _ in range(T)]) * 0.02
+    for t in range(T):  # planted detections
+        for p in rng.choice(n - 200, 5, replace=False) + 100:
+            x[t, p - 20:p + 21] += 0.3 * np.hanning(41)
+    if quantise:  # equal values: ties, flat tops
+        x = np.round(x * 512) / 512
+    return x.astype(np.float32)
+
+
+@pytest.mark.parametrize("n", [200000, 200001])
+@pytest.mark.parametrize("quantise", [False, True])
+def test_detect_matches_oracle(n, quantise):
+    cc = cc_rows(n + quantise, 4, n, quantise)
+    det = fmf.detect(cc, n_mad=6.0, min_separation=25, max_detections=64)
+    assert_matches(det, cc, 6.0, 25, 64)
+    assert all(c >= 5 for c in det.count)  # the planted peaks
+
+
+@pytest.mark.parametrize("sep", [1, 2, 300])
+def test_detect_separation(sep):
+    cc = cc_rows(11, 3, 50000, quantise=True)
+    det = fmf.detect(cc, n_mad=2.0, min_separation=sep, max_detections=5000)
+    assert_matches(det, cc, 2.0, sep, 5000)
+
+
+def test_detect_windows_and_tiny_rows():
+    cc = cc_rows(5, 6, 3000)
+    begin = np.array([0, 100, 500, 7, 2999, 10], np.int32)
+    end = np.array([3000, 2900, 500, 9, 3000, 13], np.int32)  # full, inner, empty, 2, 1, 3
+    det = fmf.detect(cc, n_mad=1.0, min_separation=3, max_detections=100,
+                     lag_begin=begin, lag_end=end)
+    assert_matches(det, cc, 1.0, 3, 100, begin, end)
+    assert np.isnan(det.median[2]) and det.count[2] == 0
+
+
+def test_detect_truncates_to_max_detections():
+    cc = cc_rows(9, 2, 40000)
+    det = fmf.detect(cc, n_mad=0.5, min_separation=2, max_detections=7)
+    assert_matches(det, cc, 0.5, 2, 7)
+    assert all(c > 7 for c in det.count)
+    assert all(len(l) == 7 for l in det.lags)
+
+
+def test_detect_capacity_exceeded_is_an_error():
+    n = 2 * fmf.detection.DETECT_CAPACITY + 200
+    row = np.tile(np.array([0.0, 1.0], np.float32), n // 2)  # a local maximum every 2 samples
+    cc = np.stack([row, cc_rows(3, 1, n)[0]])
+    with pytest.raises(FMFError) as e:
+        fmf.detect(cc, n_mad=-1.0, min_separation=1, max_detections=4)
+    assert e.value.status == 6 and "template 0" in str(e.value)
+
+
+def test_detect_device_arrays_match_host():
+    torch = pytest.importorskip("torch")
+    cc = cc_rows(21, 3, 120000, quantise=True)
+    host = fmf.detect(cc, n_mad=5.0, min_separation=40, max_detections=32)
+    dev = fmf.detect(torch.from_numpy(cc).cuda(), n_mad=5.0, min_separation=40, max_detections=32)
+    torch.cuda.synchronize()
+    assert np.array_equal(dev.count.cpu().numpy(), host.count)
+    assert np.array_equal(dev.threshold.cpu().numpy(), host.threshold)
+    for t in range(3):
+        k = int(host.count[t])
+        assert np.array_equal(dev.lag_table[t, :k].cpu().numpy(), host.lags[t])
+        assert np.array_equal(dev.value_table[t, :k].cpu().numpy(), host.values[t])
+    # capacity overflow on device arrays: count -1, no exception
+    n = 2 * fmf.detection.DETECT_CAPACITY + 200
+    row = torch.tensor([0.0, 1.0], device="cuda").repeat(n // 2).reshape(1, -1).contiguous()
+    d2 = fmf.detect(row, n_mad=-1.0, min_separation=1, max_detections=4)
+    torch.cuda.synchronize()
+    assert int(d2.count[0]) == -1
+
+
+def test_detect_many_rows_in_chunks():
+    cc = cc_rows(8, 1500, 600)  # more rows than one round of scratch (1024)
+    det = fmf.detect(cc, n_mad=3.0, min_separation=10, max_detections=8)
+    assert_matches(det, cc, 3.0, 10, 8)
+
+
+@pytest.mark.parametrize("precision", ["fp32", "split_bf16"])
+@pytest.mark.parametrize("normalize,step", [("short", 1), ("full", 2)])
+def test_search_and_detect_equals_two_steps(precision, normalize, step):
+    from tests._cases import random_search
+    tp, mo, w, d = random_search(31, 3, 4, 3, 120, 40000, -30, 200, dc=2.0 if normalize == "full" else 0.0)
+    kw = dict(n_mad=5.0, min_separation=50, max_detections=40)
+    fused = fmf.matched_filter_detect(tp, mo, w, d, step, normalize=normalize,
+                                      precision=precision, **kw)
+    cc = fmf.matched_filter(tp, mo, w, d, step, check_zeros=False, normalize=normalize,
+                            precision=precision)
+    b, e = fmf.valid_lag_range(mo, step, tp.shape[-1], d.shape[-1], cc.shape[1])
+    two = fmf.detect(cc, lag_begin=b, lag_end=e, **kw)
+    assert np.array_equal(fused.count, two.count)
+    assert np.array_equal(fused.threshold, two.threshold)
+    assert np.array_equal(fused.median, two.median) and np.array_equal(fused.mad, two.mad)
+    for t in range(tp.shape[0]):
+        assert np.array_equal(fused.lags[t], two.lags[t])
+        assert np.array_equal(fused.values[t], two.values[t])
+    assert_matches(two, cc, 5.0, 50, 40, b, e)
+    assert all(c >= 1 for c in fused.count)  # planted copies are found
