@@ -58,6 +58,8 @@ def parse_args(argv=None):
                    help="skip the plain FP32 comparison run")
     p.add_argument("--no-precision-report", action="store_true",
                    help="skip the FP64 error report on a subset")
+    p.add_argument("--no-detect", action="store_true",
+                   help="skip the detection leg (threshold + peaks on the search output)")
     p.add_argument("--templates", type=int, default=0, help="override T (smaller runs)")
     p.add_argument("--samples", type=int, default=0, help="override N (smaller runs)")
     return p.parse_args(argv)
@@ -353,10 +355,15 @@ def run_ours(args):
 
     if rank == 0 and not args.no_precision_report:
         line["precision_vs_fp64"] = precision_report(cfg)
+    if cfg["network_sum"] and not args.no_detect:
+        # the search output of the last timed step is still in `out`
+        line["detection"] = run_detection(cfg, out, world)
     # end to end through the C ABI with pinned host buffers
     del g
     if not args.no_e2e:
         line["e2e"] = run_e2e(cfg, out, precision, args, world, lib)
+        if cfg["network_sum"] and not args.no_detect:
+            line["e2e_search_detect"] = run_e2e_detect(cfg, precision, args, world, lib)
     del out
     torch.cuda.empty_cache()
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -528,6 +535,94 @@ def run_e2e(cfg, dev_out, precision, args, world, lib):
     return {"value": cfg["macs"] * n * world / secs / 1e12, "unit": UNIT,
             "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "steps": n,
             "api": "fmf_matched_filter_ex (C ABI, host pointers, pinned)"}
+
+
+DETECT_KW = dict(n_mad=8.0, min_separation=100, max_detections=64)
+
+
+def run_detection(cfg, dev_out, world, steps=3, warmup=1):
+    """fmf_detect on the device-resident search output (every template's
+    valid lag window): robust threshold + peaks.  HBM-bound; the algorithmic
+    bytes are one read of the rows (4 B per template*lag)."""
+    import torch
+    import fast_matched_filter_gb300 as fmf
+    from fast_matched_filter_gb300 import _lib
+    lib = _lib.load()
+    T, S, C, L = cfg["templates"].shape
+    N = cfg["data"].shape[-1]
+    b, e = fmf.valid_lag_range(cfg["moveouts"], cfg["step"], L, N, cfg["n_corr"])
+    stream = torch.cuda.current_stream()
+    for _ in range(warmup):
+        fmf.detect(dev_out, lag_begin=b, lag_end=e, stream=stream, **DETECT_KW)
+    torch.cuda.synchronize()
+    barrier(world)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    launches = 0
+    e0.record(stream)
+    for _ in range(steps):
+        det = fmf.detect(dev_out, lag_begin=b, lag_end=e, stream=stream, **DETECT_KW)
+        launches += lib.fmf_last_launch_count()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = dist_max(e0.elapsed_time(e1), world) / steps
+    rows = int(np.sum(e.astype(np.int64) - b))
+    peaks = load_peaks()
+    gbs = rows * 4 / (ms / 1e3) / 1e9
+    counts = det.count.cpu().numpy()
+    return {"ms_per_call": ms, "rows": T, "lags": rows, "launches_per_call": launches // steps,
+            "detections": int(counts[counts > 0].sum()), "settings": DETECT_KW,
+            "roofline": {"bound": "hbm", "achieved": gbs, "peak": peaks["hbm_gbs"],
+                         "unit": "GB/s", "frac": gbs / peaks["hbm_gbs"],
+                         "traffic": rows * 4 * 7,
+                         "traffic_source": "7 reads of the rows per call (6 radix-selection "
+                                           "passes + the peak pass), from the det_hist_kernel "
+                                           "profile: each pass reads the rows once",
+                         "peak_source": "measured hbm_gbs (copy)",
+                         "kernel": "fmf_detect (det_hist x6, det_resolve x6, det_peaks, "
+                                   "det_select)"}}
+
+
+def run_e2e_detect(cfg, precision, args, world, lib):
+    """Search + detection through fmf_matched_filter_detect with pinned host
+    inputs: H2D of every input inside each step, only the detections come
+    back (the (T, n_corr) rows stay in device memory)."""
+    import torch
+    from fast_matched_filter_gb300 import _lib
+    pinned = {k: torch.from_numpy(np.ascontiguousarray(cfg[k])).pin_memory()
+              for k in ("templates", "sst", "moveouts", "weights", "data")}
+    T, S, C, L = cfg["templates"].shape
+    N = cfg["data"].shape[-1]
+    m = DETECT_KW["max_detections"]
+    outs = [torch.empty(T, dtype=torch.float32).pin_memory() for _ in range(3)] + [
+        torch.empty(T, dtype=torch.int32).pin_memory(),
+        torch.empty((T, m), dtype=torch.int32).pin_memory(),
+        torch.empty((T, m), dtype=torch.float32).pin_memory()]
+
+    def call():
+        st = lib.fmf_matched_filter_detect(
+            pinned["templates"].data_ptr(), pinned["sst"].data_ptr(),
+            pinned["moveouts"].data_ptr(), pinned["data"].data_ptr(),
+            pinned["weights"].data_ptr(), cfg["step"], L, N, T, S, C, cfg["n_corr"],
+            1 if cfg["normalize"] == "full" else 0, _lib.PRECISIONS[precision],
+            DETECT_KW["n_mad"], DETECT_KW["min_separation"], m,
+            *[o.data_ptr() for o in outs], 0, None)
+        _lib.check(st, lib)
+
+    call()
+    barrier(world)
+    n = max(1, min(args.steps, 3))
+    t0 = time.perf_counter()
+    for _ in range(n):
+        call()
+    secs = dist_max(time.perf_counter() - t0, world)
+    h2d = sum(int(v.numel() * v.element_size()) for v in pinned.values())
+    d2h = sum(int(o.numel() * o.element_size()) for o in outs)
+    return {"value": cfg["macs"] * n * world / secs / 1e12, "unit": UNIT,
+            "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "steps": n,
+            "detections_per_step": int(outs[3].numpy().clip(min=0).sum()),
+            "api": "fmf_matched_filter_detect (C ABI, host pointers, pinned; search + "
+                   "threshold + peaks, rows kept on the device)"}
 
 
 def run_batch(args):

@@ -54,7 +54,8 @@ EXPORTS = ("fmf_matched_filter", "matched_filter", "fmf_matched_filter_ex",
            "fmf_device_errors", "fmf_matched_filter_noalloc", "fmf_batch_create",
            "fmf_batch_add", "fmf_batch_set_tiles", "fmf_batch_run", "fmf_batch_launch_count",
            "fmf_batch_destroy", "fmf_selftest_wait_timeout", "fmf_matched_filter_variable",
-           "fmf_matched_filter_variable_ex", "fmf_detect", "fmf_matched_filter_detect")
+           "fmf_matched_filter_variable_ex", "fmf_detect", "fmf_matched_filter_detect",
+           "fmf_template_energies")
 
 DETECT_CAPACITY = 16384  # FMF_DETECT_CAPACITY
 # detection arguments after the rows: n_mad, min_separation, max_detections, six outputs,
@@ -121,6 +122,8 @@ def load(path=None):
     lib.fmf_detect.restype = ct.c_int
     lib.fmf_matched_filter_detect.argtypes = ARGTYPES_SEARCH_DETECT
     lib.fmf_matched_filter_detect.restype = ct.c_int
+    lib.fmf_template_energies.argtypes = [ct.c_void_p, _sz, _sz, ct.c_void_p, ct.c_int, ct.c_void_p]
+    lib.fmf_template_energies.restype = ct.c_int
     if path is None:
         _lib = lib
     return lib

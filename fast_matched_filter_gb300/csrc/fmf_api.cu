@@ -98,6 +98,7 @@ static int cuda_status(cudaError_t e, const char *what)
 // ---------------------------------------------------------------- kernels
 __global__ void template_range_kernel(const int *, int, int, int, int, int, int, int *, int *);
 __global__ void template_center_kernel(const float *, int, float *, float *);
+__global__ void template_energy_kernel(const float *, int, int, float *);
 __global__ void channel_mean_kernel(const float *, int, float *);
 __global__ void window_stats_kernel(const float *, int, int, int, const float *, float *,
                                     float *, float *);
@@ -161,8 +162,8 @@ static void keep_pool_cached()
 // ---------------------------------------------------------------- validation
 int validate_args(const Args &a)
 {
-    if (!a.tpl || !a.sst || !a.mo || !a.data || !a.w || !a.out)
-        return set_error(FMF_ERR_ARG, "null array argument");
+    if (!a.tpl || !a.mo || !a.data || !a.w || !a.out)
+        return set_error(FMF_ERR_ARG, "null array argument");  // sst may be null: computed here
     if (a.step < 1 || a.L < 1 || a.T < 1 || a.S < 1 || a.C < 1 || a.n_corr < 1)
         return set_error(FMF_ERR_ARG,
                          "sizes must be positive (step=%zu L=%zu T=%zu S=%zu C=%zu n_corr=%zu)",
@@ -214,6 +215,16 @@ int prepare_problem(const Args &a, Scratch &ws, cudaStream_t s, Problem *Pout, c
     template_range_kernel<<<(T + 127) / 128, 128, 0, s>>>(a.mo, T, SC, L, N, (int)a.step,
                                                             (int)a.n_corr, k_lo, k_hi);
     count_launch();
+    const float *sst = a.sst;
+    if (!sst) {  // template energies as numpy computes them for float32 templates
+        float *e;
+        if ((rc = ws.get(&e, (size_t)T * SC, "template energies")))
+            return rc;
+        const int rows = T * SC;
+        template_energy_kernel<<<(rows + 127) / 128, 128, 0, s>>>(a.tpl, rows, L, e);
+        count_launch();
+        sst = e;
+    }
     if (full) {
         template_center_kernel<<<(unsigned)((size_t)T * SC), 128, 0, s>>>(a.tpl, L, tcen, tsum);
         channel_mean_kernel<<<SC, 256, 0, s>>>(a.data, N, mu);
@@ -233,7 +244,7 @@ int prepare_problem(const Args &a, Scratch &ws, cudaStream_t s, Problem *Pout, c
 
     Problem P;
     P.tpl = full ? tcen : a.tpl;
-    P.sst = a.sst;
+    P.sst = sst;
     P.tsum = tsum;
     P.mo = a.mo;
     P.w = a.w;
@@ -441,6 +452,10 @@ static int copy_inputs(const Args &a, Scratch &io, cudaStream_t s, Args *d)
     const void *src[5] = {a.tpl, a.sst, a.mo, a.data, a.w};
     float *buf[5];
     for (int i = 0; i < 5; i++) {
+        if (!src[i]) {  // template energies left to the library
+            buf[i] = nullptr;
+            continue;
+        }
         if ((rc = io.get(&buf[i], n[i], "input copies")))
             return rc;
         if ((rc = cuda_status(cudaMemcpyAsync(buf[i], src[i], n[i] * 4, cudaMemcpyHostToDevice, s),
@@ -744,6 +759,45 @@ int fmf_matched_filter_detect(const float *templates, const float *sum_square_te
     const fmf::DetectOut o{n_mad,      min_separation, max_detections, median_out, mad_out,
                            threshold_out, count_out,   lag_out,        value_out};
     return fmf::search_detect_entry(a, o, (cudaStream_t)stream);
+}
+
+int fmf_template_energies(const float *templates, size_t n_rows, size_t n_samples_template, float *out,
+                          int flags, void *stream)
+{
+    using namespace fmf;
+    clear_error();
+    g_launches = 0;
+    if (!templates || !out)
+        return set_error(FMF_ERR_ARG, "energies: null array argument");
+    if (n_rows < 1 || n_samples_template < 1 || n_rows > (size_t)INT_MAX ||
+        n_samples_template > (size_t)INT_MAX)
+        return set_error(FMF_ERR_ARG, "energies: sizes out of range (rows=%zu L=%zu)", n_rows,
+                         n_samples_template);
+    keep_pool_cached();
+    cudaGetLastError();
+    cudaStream_t s = (cudaStream_t)stream;
+    const int rows = (int)n_rows, L = (int)n_samples_template;
+    if (flags & FMF_FLAG_DEVICE_POINTERS) {
+        template_energy_kernel<<<(rows + 127) / 128, 128, 0, s>>>(templates, rows, L, out);
+        count_launch();
+        return check_launch("template energies");
+    }
+    int rc;
+    Scratch ws(s);
+    float *dt, *de;
+    if ((rc = ws.get(&dt, n_rows * n_samples_template, "templates")) ||
+        (rc = ws.get(&de, n_rows, "energies")) ||
+        (rc = cuda_status(cudaMemcpyAsync(dt, templates, n_rows * n_samples_template * 4,
+                                          cudaMemcpyHostToDevice, s),
+                          "copying templates")))
+        return rc;
+    template_energy_kernel<<<(rows + 127) / 128, 128, 0, s>>>(dt, rows, L, de);
+    count_launch();
+    if ((rc = check_launch("template energies")) ||
+        (rc = cuda_status(cudaMemcpyAsync(out, de, n_rows * 4, cudaMemcpyDeviceToHost, s),
+                          "copying energies")))
+        return rc;
+    return cuda_status(cudaStreamSynchronize(s), "template energies");
 }
 
 int fmf_last_error(char *buf, size_t len)

@@ -94,9 +94,52 @@ __global__ void det_init_kernel(DetState *__restrict__ st, int T, int n_corr,
     st[t] = s;
 }
 
+// Split of a row at its first 16-byte boundary: `head` scalar elements, then
+// `nvec` float4s, then `tail` scalar elements.
+struct RowSplit {
+    long long head, nvec, tail;
+};
+
+__device__ __forceinline__ RowSplit split_row(const float *row, long long n)
+{
+    RowSplit r;
+    r.head = (long long)(((16u - ((unsigned)(size_t)row & 15u)) & 15u) >> 2);
+    if (r.head > n)
+        r.head = n;
+    r.nvec = (n - r.head) >> 2;
+    r.tail = n - r.head - 4 * r.nvec;
+    return r;
+}
+
+// Histogram update by a whole warp: every lane calls it (lanes whose value
+// does not count pass ok = false); lanes with the same digit add once.
+__device__ __forceinline__ void hist_add(unsigned *h, float v, bool ok, int mode, float med, int shift,
+                                         unsigned dmask, unsigned high, unsigned p0, unsigned p1,
+                                         bool two, int lane)
+{
+    const float x = mode == 0 ? v : fabsf(__fsub_rn(v, med));
+    const unsigned key = order_key(x);
+    const unsigned dig = (key >> shift) & dmask;
+    const bool m0 = ok && (key & high) == p0;
+    if (__any_sync(0xffffffffu, m0)) {
+        const unsigned g = __match_any_sync(0xffffffffu, m0 ? dig : 0xffffffffu);
+        if (m0 && (__ffs(g) - 1) == lane)
+            atomicAdd(&h[dig], __popc(g));
+    }
+    if (two) {
+        const bool m1 = ok && (key & high) == p1;
+        if (__any_sync(0xffffffffu, m1)) {
+            const unsigned g = __match_any_sync(0xffffffffu, m1 ? dig : 0xffffffffu);
+            if (m1 && (__ffs(g) - 1) == lane)
+                atomicAdd(&h[kDetBins + dig], __popc(g));
+        }
+    }
+}
+
 // One selection pass: histogram of the current digit over the elements whose
 // higher key bits equal a rank's prefix.  mode 0 keys the values, mode 1 keys
-// |x - median|.  Grid: (blocks per row, templates).
+// |x - median|.  Grid: (blocks per row, templates).  The row is read with
+// 16-byte loads, two per lane in flight per step.
 __global__ void __launch_bounds__(kDetThreads)
 det_hist_kernel(const float *__restrict__ cc, size_t ld, const DetState *__restrict__ st,
                 unsigned *__restrict__ hist, int pass, int mode)
@@ -118,33 +161,32 @@ det_hist_kernel(const float *__restrict__ cc, size_t ld, const DetState *__restr
     const float med = s.med;
     const float *row = cc + (size_t)t * ld + s.begin;
     const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
     constexpr int kWarps = kDetThreads / 32;
-    const long long chunks = (n + 127) / 128;  // 128 consecutive values per warp step
-    for (long long c = (long long)blockIdx.x * kWarps + (threadIdx.x >> 5); c < chunks;
-         c += (long long)gridDim.x * kWarps) {
-        float v[4];
+    const RowSplit rs = split_row(row, n);
+    if (blockIdx.x == 0 && warp == 0) {  // the unaligned ends, at most 3 + 3 values
+        const long long i = lane < rs.head ? lane : rs.head + 4 * rs.nvec + (lane - rs.head);
+        const bool ok = lane < rs.head + rs.tail;
+        const float v = ok ? row[i] : 0.f;
+        hist_add(h, v, ok, mode, med, shift, dmask, high, p0, p1, two, lane);
+    }
+    const float4 *vrow = reinterpret_cast<const float4 *>(row + rs.head);
+    const long long steps = (rs.nvec + 63) / 64;  // 64 float4s per warp step
+    for (long long c = (long long)blockIdx.x * kWarps + warp; c < steps; c += (long long)gridDim.x * kWarps) {
+        float4 v[2];
+        bool ok[2];
 #pragma unroll
-        for (int u = 0; u < 4; u++) {
-            const long long i = c * 128 + u * 32 + lane;
-            v[u] = i < n ? row[i] : 0.f;
+        for (int u = 0; u < 2; u++) {
+            const long long i = c * 64 + u * 32 + lane;
+            ok[u] = i < rs.nvec;
+            v[u] = ok[u] ? vrow[i] : make_float4(0.f, 0.f, 0.f, 0.f);
         }
 #pragma unroll
-        for (int u = 0; u < 4; u++) {
-            const bool ok = c * 128 + u * 32 + lane < n;
-            const float x = mode == 0 ? v[u] : fabsf(__fsub_rn(v[u], med));
-            const unsigned key = order_key(x);
-            const unsigned dig = (key >> shift) & dmask;
-            const bool m0 = ok && (key & high) == p0;
-            // lanes with the same digit add once (sentinel ~0 for lanes that do not count)
-            unsigned g = __match_any_sync(0xffffffffu, m0 ? dig : 0xffffffffu);
-            if (m0 && (__ffs(g) - 1) == lane)
-                atomicAdd(&h[dig], __popc(g));
-            if (two) {
-                const bool m1 = ok && (key & high) == p1;
-                g = __match_any_sync(0xffffffffu, m1 ? dig : 0xffffffffu);
-                if (m1 && (__ffs(g) - 1) == lane)
-                    atomicAdd(&h[kDetBins + dig], __popc(g));
-            }
+        for (int u = 0; u < 2; u++) {
+            hist_add(h, v[u].x, ok[u], mode, med, shift, dmask, high, p0, p1, two, lane);
+            hist_add(h, v[u].y, ok[u], mode, med, shift, dmask, high, p0, p1, two, lane);
+            hist_add(h, v[u].z, ok[u], mode, med, shift, dmask, high, p0, p1, two, lane);
+            hist_add(h, v[u].w, ok[u], mode, med, shift, dmask, high, p0, p1, two, lane);
         }
     }
     __syncthreads();
@@ -226,7 +268,27 @@ __global__ void det_resolve_kernel(DetState *__restrict__ st, unsigned *__restri
 }
 
 // Local maxima at or above the threshold, appended (unordered) to the
-// template's candidate list.  Grid: (blocks per row, templates).
+// template's candidate list.  Grid: (blocks per row, templates).  Samples are
+// read with 16-byte loads; the rare sample at or above the threshold is
+// examined with scalar loads.
+__device__ __forceinline__ void peak_at(const float *row, long long i, long long b, long long e, float x,
+                                        float thr, DetState *st, int2 *cand, int cap, int t)
+{
+    if (!(x >= thr) || i < b + 1 || i >= e - 1)
+        return;  // a flat top has the value of its rising sample
+    if (!(row[i - 1] < x))
+        return;
+    long long j = i + 1;
+    while (j < e - 1 && row[j] == x)
+        j++;
+    if (row[j] < x) {
+        const int peak = (int)((i + j - 1) >> 1);
+        const int slot = atomicAdd(&st[t].n_cand, 1);
+        if (slot < cap)
+            cand[(size_t)t * cap + slot] = make_int2(peak, __float_as_int(x));
+    }
+}
+
 __global__ void __launch_bounds__(kDetThreads)
 det_peaks_kernel(const float *__restrict__ cc, size_t ld, DetState *__restrict__ st,
                  int2 *__restrict__ cand, int cap)
@@ -237,21 +299,29 @@ det_peaks_kernel(const float *__restrict__ cc, size_t ld, DetState *__restrict__
     if (e - b < 3)
         return;
     const float *row = cc + (size_t)t * ld;
+    const RowSplit rs = split_row(row + b, e - b);
+    const long long gtid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (gtid < rs.head + rs.tail) {
+        const long long i = b + (gtid < rs.head ? gtid : rs.head + 4 * rs.nvec + (gtid - rs.head));
+        peak_at(row, i, b, e, row[i], thr, st, cand, cap, t);
+    }
+    const float4 *vrow = reinterpret_cast<const float4 *>(row + b + rs.head);
+    const long long base = b + rs.head;
     const long long stride = (long long)gridDim.x * blockDim.x;
-    for (long long i = b + 1 + (long long)blockIdx.x * blockDim.x + threadIdx.x; i < e - 1; i += stride) {
-        const float x = row[i];
-        if (!(x >= thr))
-            continue;  // a flat top has the value of its rising sample
-        if (!(row[i - 1] < x))
-            continue;
-        long long j = i + 1;
-        while (j < e - 1 && row[j] == x)
-            j++;
-        if (row[j] < x) {
-            const int peak = (int)((i + j - 1) >> 1);
-            const int slot = atomicAdd(&st[t].n_cand, 1);
-            if (slot < cap)
-                cand[(size_t)t * cap + slot] = make_int2(peak, __float_as_int(x));
+    for (long long v = gtid; v < rs.nvec; v += 2 * stride) {
+        const float4 x0 = vrow[v];
+        const bool has1 = v + stride < rs.nvec;
+        const float4 x1 = has1 ? vrow[v + stride] : make_float4(0.f, 0.f, 0.f, 0.f);
+        const long long i0 = base + 4 * v, i1 = base + 4 * (v + stride);
+        peak_at(row, i0, b, e, x0.x, thr, st, cand, cap, t);
+        peak_at(row, i0 + 1, b, e, x0.y, thr, st, cand, cap, t);
+        peak_at(row, i0 + 2, b, e, x0.z, thr, st, cand, cap, t);
+        peak_at(row, i0 + 3, b, e, x0.w, thr, st, cand, cap, t);
+        if (has1) {
+            peak_at(row, i1, b, e, x1.x, thr, st, cand, cap, t);
+            peak_at(row, i1 + 1, b, e, x1.y, thr, st, cand, cap, t);
+            peak_at(row, i1 + 2, b, e, x1.z, thr, st, cand, cap, t);
+            peak_at(row, i1 + 3, b, e, x1.w, thr, st, cand, cap, t);
         }
     }
 }

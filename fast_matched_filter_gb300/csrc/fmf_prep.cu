@@ -9,6 +9,11 @@
 //    the template's DC term from the products the numerator sums.
 //  * channel_mean_kernel   : "full" only -- FP64 mean of each data channel,
 //    rounded to float; d - mu is exact in FP32 wherever mu/2 <= d <= 2 mu.
+//  * template_energy_kernel: the template energies sum(t^2) when the caller
+//    passes none, computed as the reference wrapper computes them for
+//    float32 templates (numpy.sum(templates**2, axis=-1),
+//    fast_matched_filter.py:256-261): float32 squares summed in numpy's
+//    pairwise order, so the values are bit-identical.
 //  * window_stats_kernel   : FP64 sliding-window statistics of every channel
 //    for windows of L samples starting at each sample index:
 //      short: E = sum d^2                      (matched_filter.c:622)
@@ -63,6 +68,90 @@ __device__ __forceinline__ double block_sum_f64(double v, double *red)
     }
     __syncthreads();
     return red[32];
+}
+
+// numpy's float32 pairwise sum of the squares of a[0:n) (the reduction
+// numpy.sum applies along a contiguous axis): fewer than 8 values -- a running
+// sum from -0; up to 128 -- eight interleaved partial sums, combined as
+// ((r0 + r1) + (r2 + r3)) + ((r4 + r5) + (r6 + r7)), then the values past the
+// last multiple of 8 in order; more -- the sum of the two halves split at n/2
+// rounded down to a multiple of 8.  Explicit round-to-nearest operations: no
+// fused multiply-add may change a rounding.
+__device__ float pairwise_leaf_sq(const float *a, int n)
+{
+    if (n < 8) {
+        float r = -0.0f;
+        for (int i = 0; i < n; i++)
+            r = __fadd_rn(r, __fmul_rn(a[i], a[i]));
+        return r;
+    }
+    float r[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++)
+        r[k] = __fmul_rn(a[k], a[k]);
+    int i = 8;
+    for (; i < n - (n % 8); i += 8) {
+#pragma unroll
+        for (int k = 0; k < 8; k++)
+            r[k] = __fadd_rn(r[k], __fmul_rn(a[i + k], a[i + k]));
+    }
+    float res = __fadd_rn(__fadd_rn(__fadd_rn(r[0], r[1]), __fadd_rn(r[2], r[3])),
+                          __fadd_rn(__fadd_rn(r[4], r[5]), __fadd_rn(r[6], r[7])));
+    for (; i < n; i++)
+        res = __fadd_rn(res, __fmul_rn(a[i], a[i]));
+    return res;
+}
+
+__device__ float pairwise_sq(const float *a, int n)
+{
+    // the recursion of numpy's pairwise sum, unrolled with an explicit stack
+    // (depth <= 32 for any int n): post-order over the split tree
+    int off[32], len[32], stage[32];
+    float left[32];
+    int sp = 0;
+    off[0] = 0;
+    len[0] = n;
+    stage[0] = 0;
+    float ret = 0.f;
+    while (sp >= 0) {
+        const int o = off[sp], m = len[sp];
+        if (m <= 128) {
+            ret = pairwise_leaf_sq(a + o, m);
+            sp--;
+        } else {
+            int m2 = m / 2;
+            m2 -= m2 % 8;
+            if (stage[sp] == 0) {  // descend left
+                stage[sp] = 1;
+                sp++;
+                off[sp] = o;
+                len[sp] = m2;
+                stage[sp] = 0;
+                continue;
+            }
+            if (stage[sp] == 1) {  // left done: descend right
+                left[sp] = ret;
+                stage[sp] = 2;
+                sp++;
+                off[sp] = o + m2;
+                len[sp] = m - m2;
+                stage[sp] = 0;
+                continue;
+            }
+            ret = __fadd_rn(left[sp], ret);  // both done
+            sp--;
+        }
+    }
+    return ret;
+}
+
+// one thread per (template, channel) row
+__global__ void template_energy_kernel(const float *__restrict__ tpl, int rows, int L,
+                                       float *__restrict__ sst)
+{
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r < rows)
+        sst[r] = pairwise_sq(tpl + (size_t)r * L, L);
 }
 
 // grid = T*SC blocks of 128 threads

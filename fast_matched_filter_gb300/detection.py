@@ -184,7 +184,7 @@ def matched_filter_detect(templates, moveouts, weights, data, step, normalize="s
         raise ValueError("precision must be one of %s" % sorted(_lib.PRECISIONS))
     _check_detect_args(n_mad, min_separation, max_detections)
     lib = _require_lib()
-    pp = prepare(templates, moveouts, weights, data, step, normalize)
+    pp = prepare(templates, moveouts, weights, data, step, normalize, energies="device")
     if pp is None:
         print("Template and data dimensions are not compatible!")
         return None
@@ -193,7 +193,8 @@ def matched_filter_detect(templates, moveouts, weights, data, step, normalize="s
                                                               precision)
     out = _host_outputs(T, max_detections)
     st = lib.fmf_matched_filter_detect(
-        pp["templates"].ctypes.data, pp["sst"].ctypes.data, pp["moveouts"].ctypes.data,
+        pp["templates"].ctypes.data, None if pp["sst"] is None else pp["sst"].ctypes.data,
+        pp["moveouts"].ctypes.data,
         pp["data"].ctypes.data, pp["weights"].ctypes.data, pp["step"], pp["L"], pp["N"], T, S, C,
         pp["n_corr"], pp["normalize"], _lib.PRECISIONS[precision], float(n_mad),
         int(min_separation), int(max_detections), *_addresses(out), flags, None)

@@ -109,10 +109,15 @@ def _zero_report(cc, moveouts_flat, weights_flat, n_templates, n_corr, step,
     return zeros
 
 
-def prepare(templates, moveouts, weights, data, step, normalize="short"):
+def prepare(templates, moveouts, weights, data, step, normalize="short", energies="host"):
     """Shape handling of the reference wrapper: returns the flat float32/int32
     buffers and sizes (fast_matched_filter.py:179-268), or None for
-    incompatible dimensions."""
+    incompatible dimensions.
+
+    energies='device' leaves the template energies of float32 templates to
+    the library (``sst`` None): it computes them on the GPU bit-identically
+    to the numpy sum below.  Other dtypes are summed here, in their own dtype,
+    as the reference does."""
     dims = _infer_dims(templates, data)
     if dims is None:
         return None
@@ -132,10 +137,13 @@ def prepare(templates, moveouts, weights, data, step, normalize="short"):
     if N < L:
         raise ValueError("data (%d samples) shorter than the templates (%d)" % (N, L))
     n_corr = int((N - L) / step + 1)
-    sst = np.sum(templates ** 2, axis=-1)
+    if energies == "device" and templates.dtype == np.float32:
+        sst = None
+    else:
+        sst = np.ascontiguousarray(np.sum(templates ** 2, axis=-1).flatten(), dtype=np.float32)
     return dict(
         templates=np.ascontiguousarray(templates.flatten(), dtype=np.float32),
-        sst=np.ascontiguousarray(sst.flatten(), dtype=np.float32),
+        sst=sst,
         moveouts=np.ascontiguousarray(moveouts.flatten(), dtype=np.int32),
         weights=np.ascontiguousarray(weights.flatten(), dtype=np.float32),
         data=np.ascontiguousarray(data.flatten(), dtype=np.float32),
@@ -144,7 +152,11 @@ def prepare(templates, moveouts, weights, data, step, normalize="short"):
 
 
 def _ptr(a, typ):
-    return a.ctypes.data_as(ct.POINTER(typ))
+    return None if a is None else a.ctypes.data_as(ct.POINTER(typ))
+
+
+def _addr(a):
+    return None if a is None else a.ctypes.data
 
 
 def matched_filter(templates, moveouts, weights, data, step,
@@ -180,7 +192,7 @@ def matched_filter(templates, moveouts, weights, data, step,
     if precision not in _lib.PRECISIONS:
         raise ValueError("precision must be one of %s" % sorted(_lib.PRECISIONS))
     lib = _require_lib()
-    pp = prepare(templates, moveouts, weights, data, step, normalize)
+    pp = prepare(templates, moveouts, weights, data, step, normalize, energies="device")
     if pp is None:
         print("Template and data dimensions are not compatible!")
         return None
@@ -196,7 +208,7 @@ def matched_filter(templates, moveouts, weights, data, step,
     else:
         flags = autotune.flags_for(pp["L"], pp["step"], S * C, normalize, precision)
         st = lib.fmf_matched_filter_ex(
-            pp["templates"].ctypes.data, pp["sst"].ctypes.data, pp["moveouts"].ctypes.data,
+            pp["templates"].ctypes.data, _addr(pp["sst"]), pp["moveouts"].ctypes.data,
             pp["data"].ctypes.data, pp["weights"].ctypes.data, pp["step"], pp["L"], pp["N"],
             T, S, C, n_corr, cc.ctypes.data, pp["normalize"], int(bool(network_sum)),
             _lib.PRECISIONS[precision], flags, None)
@@ -243,7 +255,8 @@ def matched_filter_device(templates, sum_square_templates, moveouts, weights, da
                           step, out, normalize="short", network_sum=True,
                           precision="fp32", stream=None):
     """Run on device-resident, canonical, C-contiguous torch CUDA tensors:
-    templates (T,S,C,L) f32, sum_square_templates (T,S,C) f32, moveouts
+    templates (T,S,C,L) f32, sum_square_templates (T,S,C) f32 or None (then
+    computed on the GPU as numpy.sum(templates**2, axis=-1) would), moveouts
     (T,S,C) int32, weights (T,S,C) f32, data (S,C,N) f32, out (T,n_corr) or
     (T,n_corr,S,C) f32.  Asynchronous on ``stream`` (a torch.cuda.Stream or
     raw handle; default: torch's current stream).  Returns the launch count."""
@@ -257,6 +270,8 @@ def matched_filter_device(templates, sum_square_templates, moveouts, weights, da
                         ("sum_square_templates", sum_square_templates, torch.float32),
                         ("moveouts", moveouts, torch.int32), ("weights", weights, torch.float32),
                         ("data", data, torch.float32), ("out", out, torch.float32)):
+        if t is None and name == "sum_square_templates":
+            continue
         if not (t.is_cuda and t.dtype == dt and t.is_contiguous()):
             raise ValueError("%s must be a contiguous CUDA tensor of %s" % (name, dt))
     if stream is None:
@@ -264,8 +279,9 @@ def matched_filter_device(templates, sum_square_templates, moveouts, weights, da
     handle = stream.cuda_stream if hasattr(stream, "cuda_stream") else int(stream)
     flags = _lib.FLAG_DEVICE_POINTERS | autotune.flags_for(L, step, S * C, normalize, precision)
     st = lib.fmf_matched_filter_ex(
-        templates.data_ptr(), sum_square_templates.data_ptr(), moveouts.data_ptr(),
-        data.data_ptr(), weights.data_ptr(), int(step), L, N, T, S, C, n_corr,
+        templates.data_ptr(),
+        None if sum_square_templates is None else sum_square_templates.data_ptr(),
+        moveouts.data_ptr(), data.data_ptr(), weights.data_ptr(), int(step), L, N, T, S, C, n_corr,
         out.data_ptr(), 1 if normalize == "full" else 0, int(bool(network_sum)),
         _lib.PRECISIONS[precision], flags, handle)
     _lib.check(st, lib)

@@ -6,7 +6,12 @@
  * argument packing at fast_matched_filter/fast_matched_filter.py:253-316):
  *
  *   templates            (T, S, C, L)  float32, C-contiguous
- *   sum_square_templates (T, S, C)     float32, sum of templates**2 over L
+ *   sum_square_templates (T, S, C)     float32, sum of templates**2 over L.  An
+ *                                      extension: fmf_matched_filter[_ex], matched_filter,
+ *                                      fmf_batch_add and fmf_matched_filter_detect accept
+ *                                      NULL and then compute it on the device,
+ *                                      bit-identical to the reference wrapper's
+ *                                      numpy.sum(templates**2, axis=-1) on float32 templates
  *   moveouts             (T, S, C)     int32, samples (may be negative)
  *   data                 (S, C, N)     float32
  *   weights              (T, S, C)     float32; weight 0 skips the channel
@@ -228,6 +233,17 @@ FMF_API int fmf_matched_filter_detect(const float *templates, const float *sum_s
                                       float *median_out, float *mad_out, float *threshold_out,
                                       int *count_out, int *lag_out, float *value_out, int flags,
                                       void *stream);
+
+/*
+ * Template energies (no reference counterpart; the reference wrapper computes
+ * them with numpy, fast_matched_filter.py:256-261): out[r] = sum over L of
+ * templates[r][:]**2 for rows r < n_rows, float32 squares summed in numpy's
+ * pairwise order, so out is bit-identical to numpy.sum(templates**2, axis=-1)
+ * for float32 templates.  Host pointers (synchronous) or, with
+ * FMF_FLAG_DEVICE_POINTERS, device pointers (asynchronous on `stream`).
+ */
+FMF_API int fmf_template_energies(const float *templates, size_t n_rows, size_t n_samples_template,
+                                  float *out, int flags, void *stream);
 
 /* Copies the calling thread's last error message (NUL-terminated, truncated
  * to len) and returns its status.  The reference printed and exited instead

@@ -1,4 +1,5 @@
 import os
+import subprocess
 import sys
 
 import pytest
@@ -10,6 +11,12 @@ if REPO not in sys.path:
 
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300, sm_103a)")
+    # Bring libfmf_gb300.so up to date before any test module imports the
+    # package: a library loaded into this process cannot be replaced later.
+    # In a child process, so that the stale copy is never loaded here.
+    subprocess.run([sys.executable, "-c",
+                    "from fast_matched_filter_gb300 import build; build.build()"],
+                   cwd=REPO, check=False)
 
 
 @pytest.fixture(scope="session")
