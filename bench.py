@@ -567,7 +567,7 @@ def run_detection(cfg, dev_out, world, steps=3, warmup=1):
     torch.cuda.synchronize()
     ms = dist_max(e0.elapsed_time(e1), world) / steps
     rows = int(np.sum(e.astype(np.int64) - b))
-    peaks = load_peaks()
+    peaks, peak_kind = load_peaks()
     gbs = rows * 4 / (ms / 1e3) / 1e9
     counts = det.count.cpu().numpy()
     return {"ms_per_call": ms, "rows": T, "lags": rows, "launches_per_call": launches // steps,
@@ -578,7 +578,7 @@ def run_detection(cfg, dev_out, world, steps=3, warmup=1):
                          "traffic_source": "7 reads of the rows per call (6 radix-selection "
                                            "passes + the peak pass), from the det_hist_kernel "
                                            "profile: each pass reads the rows once",
-                         "peak_source": "measured hbm_gbs (copy)",
+                         "peak_source": "%s hbm_gbs (copy)" % peak_kind,
                          "kernel": "fmf_detect (det_hist x6, det_resolve x6, det_peaks, "
                                    "det_select)"}}
 

@@ -100,6 +100,7 @@ __global__ void template_range_kernel(const int *, int, int, int, int, int, int,
 __global__ void template_center_kernel(const float *, int, float *, float *);
 __global__ void template_energy_kernel(const float *, int, int, float *);
 __global__ void channel_mean_kernel(const float *, int, float *);
+__global__ void zero_count_kernel(const float *, long long, long long, long long, unsigned long long *);
 __global__ void window_stats_kernel(const float *, int, int, int, const float *, float *,
                                     float *, float *);
 int launch_tc(const Problem &P, const float *data_for_tc, int precision, unsigned *err, Scratch &ws,
@@ -277,6 +278,26 @@ int prepare_problem(const Args &a, Scratch &ws, cudaStream_t s, Problem *Pout, c
     return FMF_OK;
 }
 
+// check_zeros count of templates [t0, t0 + nt) of a search's output into
+// counts[t0 ..] (device), on stream s.
+static int launch_zero_count(const Args &a, const float *out, int t0, int nt,
+                             unsigned long long *counts, cudaStream_t s)
+{
+    const long long row = (long long)a.n_corr * (a.sum_mode ? 1 : (long long)(a.S * a.C));
+    const long long last = a.sum_mode ? (long long)a.n_corr : (long long)a.C;
+    long long stop = a.zero_stop < 0 ? 0 : (a.zero_stop > last ? last : a.zero_stop);
+    const long long span = last == row ? stop : row;
+    long long blocks = (span + 256 * 8 - 1) / (256 * 8);
+    blocks = blocks < 1 ? 1 : (blocks > 1024 ? 1024 : blocks);
+    for (int c0 = 0; c0 < nt; c0 += 65535) {
+        const int cn = nt - c0 < 65535 ? nt - c0 : 65535;
+        zero_count_kernel<<<dim3((unsigned)blocks, (unsigned)cn), 256, 0, s>>>(
+            out + (size_t)(t0 + c0) * row, row, last, stop, counts + t0 + c0);
+        count_launch();
+    }
+    return check_launch("zero count");
+}
+
 // Plain FP32 form over all templates, in launches of at most 65535 templates.
 int launch_plain_all(const Problem &P, cudaStream_t s)
 {
@@ -339,7 +360,13 @@ static int run_device(const Args &a, cudaStream_t s)
 {
     Scratch ws(s);
     Problem P;
-    return run_device_ws(a, s, ws, &P);
+    int rc = run_device_ws(a, s, ws, &P);
+    if (rc || !a.zero_counts)
+        return rc;
+    if ((rc = cuda_status(cudaMemsetAsync(a.zero_counts, 0, a.T * sizeof(unsigned long long), s),
+                          "clearing the zero counts")))
+        return rc;
+    return launch_zero_count(a, a.out, 0, (int)a.T, a.zero_counts, s);
 }
 
 // ---------------------------------------------------------------- host-pointer path
@@ -396,6 +423,13 @@ static int run_streamed(const Args &d, float *host_out, cudaStream_t s)
                              reinterpret_cast<TcProb *>(tcfull.data()))))
             return rc;
     }
+    unsigned long long *zc = nullptr;  // device zero counts, copied to d.zero_counts (host)
+    if (d.zero_counts) {
+        if ((rc = ws.get(&zc, (size_t)P.T, "zero counts")) ||
+            (rc = cuda_status(cudaMemsetAsync(zc, 0, (size_t)P.T * sizeof(unsigned long long), s),
+                              "clearing the zero counts")))
+            return rc;
+    }
     cudaStream_t s2 = nullptr;
     cudaEvent_t ev[9] = {};
     cudaError_t e = cudaStreamCreateWithFlags(&s2, cudaStreamNonBlocking);
@@ -416,6 +450,8 @@ static int run_streamed(const Args &d, float *host_out, cudaStream_t s)
             } else {
                 rc = launch_plain_all(problem_subset(P, t0, nt), s);
             }
+            if (!rc && zc)
+                rc = launch_zero_count(d, P.out, t0, nt, zc, s);
             if (rc)
                 break;
             const size_t off = (size_t)t0 * row, n = (size_t)nt * row * sizeof(float);
@@ -425,6 +461,9 @@ static int run_streamed(const Args &d, float *host_out, cudaStream_t s)
                     cudaSuccess)
                 break;
         }
+        if (e == cudaSuccess && rc == FMF_OK && zc)
+            e = cudaMemcpyAsync(d.zero_counts, zc, (size_t)P.T * sizeof(unsigned long long),
+                                cudaMemcpyDeviceToHost, s);
         // scratch is freed on s: let s wait for the last copy
         if (e == cudaSuccess && (e = cudaEventRecord(ev[n_chunks], s2)) == cudaSuccess)
             e = cudaStreamWaitEvent(s, ev[n_chunks], 0);
@@ -685,6 +724,41 @@ int fmf_matched_filter_ex(const float *templates, const float *sum_square_templa
     a.sum_mode = sum_cc_mode;
     a.precision = precision;
     a.flags = flags;
+    return fmf::entry(a, stream);
+}
+
+int fmf_matched_filter_check_zeros(const float *templates, const float *sum_square_templates,
+                                   const int *moveouts, const float *data, const float *weights,
+                                   size_t step, size_t n_samples_template, size_t n_samples_data,
+                                   size_t n_templates, size_t n_stations, size_t n_components,
+                                   size_t n_corr, float *cc_out, int normalize, int sum_cc_mode,
+                                   int precision, int flags, void *stream, long long zero_stop,
+                                   unsigned long long *zero_counts)
+{
+    if (!zero_counts) {
+        fmf::clear_error();
+        return fmf::set_error(FMF_ERR_ARG, "null zero_counts");
+    }
+    fmf::Args a;
+    a.tpl = templates;
+    a.sst = sum_square_templates;
+    a.mo = moveouts;
+    a.data = data;
+    a.w = weights;
+    a.out = cc_out;
+    a.step = step;
+    a.L = n_samples_template;
+    a.N = n_samples_data;
+    a.T = n_templates;
+    a.S = n_stations;
+    a.C = n_components;
+    a.n_corr = n_corr;
+    a.normalize = normalize;
+    a.sum_mode = sum_cc_mode;
+    a.precision = precision;
+    a.flags = flags;
+    a.zero_stop = zero_stop;
+    a.zero_counts = zero_counts;
     return fmf::entry(a, stream);
 }
 

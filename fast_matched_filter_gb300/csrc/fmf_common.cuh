@@ -95,6 +95,11 @@ struct Args {
     float *out;
     size_t step, L, N, T, S, C, n_corr;
     int normalize, sum_mode, precision, flags;
+    // check_zeros count (optional): per template, the outputs equal to 0
+    // whose last-axis index is below zero_stop (host or device pointer, as
+    // the other arrays)
+    unsigned long long *zero_counts = nullptr;
+    long long zero_stop = 0;
 };
 int validate_args(const Args &a);
 int prepare_problem(const Args &a, Scratch &ws, cudaStream_t s, Problem *P, const float **data_for_tc);

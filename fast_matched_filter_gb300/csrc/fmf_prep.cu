@@ -154,6 +154,25 @@ __global__ void template_energy_kernel(const float *__restrict__ tpl, int rows, 
         sst[r] = pairwise_sq(tpl + (size_t)r * L, L);
 }
 
+// check_zeros count of the reference wrapper (fast_matched_filter.py:322-361)
+// on the device: counts[t] += number of zeros among out[t][i] with
+// i % last_axis < stop, over a row of row_len values.  Grid (blocks, T).
+__global__ void zero_count_kernel(const float *__restrict__ out, long long row_len, long long last_axis,
+                                  long long stop, unsigned long long *__restrict__ counts)
+{
+    const int t = blockIdx.y;
+    const float *row = out + (size_t)t * row_len;
+    const long long span = last_axis == row_len ? stop : row_len;  // network sum: lags < stop
+    unsigned c = 0;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < span;
+         i += (long long)gridDim.x * blockDim.x)
+        c += (row[i] == 0.0f && i % last_axis < stop) ? 1u : 0u;
+    for (int o = 16; o > 0; o >>= 1)
+        c += __shfl_down_sync(0xffffffffu, c, o);
+    if ((threadIdx.x & 31) == 0 && c)
+        atomicAdd(counts + t, (unsigned long long)c);
+}
+
 // grid = T*SC blocks of 128 threads
 __global__ void template_center_kernel(const float *__restrict__ tpl, int L,
                                        float *__restrict__ tcen,

@@ -550,18 +550,30 @@ __global__ void __launch_bounds__(TC_THREADS, 1) tc_persistent(const __grid_cons
                         const int k_first = sres & ~15;
                         const int k_end = (sres + lphi + TC_Q - 1 + 15) & ~15;
                         const uint32_t zhi = smem_u32(smem + (size_t)s * B.stage_bytes);
-                        const uint32_t zlo = zhi + data_bytes, whi = zhi + w_off, wlo = whi + wbytes;
-                        for (int k = k_first; k < k_end; k += 16) {
-                            const uint32_t wo = (uint32_t)(k >> 3) * 128u;
-                            const uint32_t bo = (uint32_t)((k & (TC_Q - 1)) >> 3) * lbo_b +
-                                                (uint32_t)(k / TC_Q) * 16u;
-                            const uint64_t ah = sdesc(whi + wo, 128, 128);
-                            const uint64_t bh = sdesc(zhi + bo, lbo_b, 128);
-                            mma_bf16(dt, ah, bh, idesc, acc);
-                            acc = 1;
-                            if (split) {
-                                mma_bf16(dt, ah, sdesc(zlo + bo, lbo_b, 128), idesc, 1);
-                                mma_bf16(dt, sdesc(wlo + wo, 128, 128), bh, idesc, 1);
+                        const uint32_t whi = zhi + w_off;
+                        // Descriptors advance by additions: the start-address field (bits 0-13,
+                        // 16-byte units) of an address below 256 KB never carries into the
+                        // next field.  A: +256 bytes per K step (two 128-byte template blocks);
+                        // B: +2 column blocks per K step inside a 128-wide K block, then the
+                        // next data row (+16 bytes) from column block 0.
+                        uint64_t ah = sdesc(whi + (uint32_t)(k_first >> 3) * 128u, 128, 128);
+                        const uint64_t a_lo = wbytes >> 4, b_lo = data_bytes >> 4;
+                        const uint64_t b0 = sdesc(zhi, lbo_b, 128);
+                        const uint64_t b_step = (2u * lbo_b) >> 4;
+                        int k = k_first;
+                        while (k < k_end) {
+                            const int blk_end = min(k_end, (k & ~(TC_Q - 1)) + TC_Q);
+                            uint64_t bh = b0 + (((uint32_t)((k & (TC_Q - 1)) >> 3) * lbo_b +
+                                                 (uint32_t)(k / TC_Q) * 16u) >> 4);
+                            for (; k < blk_end; k += 16) {
+                                mma_bf16(dt, ah, bh, idesc, acc);
+                                acc = 1;
+                                if (split) {
+                                    mma_bf16(dt, ah, bh + b_lo, idesc, 1);
+                                    mma_bf16(dt, ah + a_lo, bh, idesc, 1);
+                                }
+                                ah += 16;
+                                bh += b_step;
                             }
                         }
                         mma_commit(empty0 + 8 * s);

@@ -80,24 +80,41 @@ def _infer_dims(templates, data):
     return None
 
 
-def _zero_report(cc, moveouts_flat, weights_flat, n_templates, n_corr, step,
-                 network_sum, check_zeros):
-    """The check_zeros diagnostic of fast_matched_filter.py:322-361, including
-    its slicing of the last axis in the per-channel layout."""
+def _check_zeros_option(check_zeros):
+    """Option check of fast_matched_filter.py:322-327."""
     if (check_zeros is not False) and (check_zeros != "first") and (check_zeros != "all"):
         print("check_zeros should be False, 'first', or 'all'. Set it to "
               "the default value: 'first'")
         check_zeros = "first"
+    return check_zeros
+
+
+def _zero_stop(moveouts_flat, n_corr, step, last_axis):
+    """The reference's slice end int(n_corr - max moveout / step) applied to
+    the last axis (length last_axis), as Python slicing resolves it."""
+    stop = int(n_corr - moveouts_flat.max() / step)
+    return len(range(last_axis)[:stop])
+
+
+def _zero_report(cc, moveouts_flat, weights_flat, n_templates, n_corr, step,
+                 network_sum, check_zeros, counts=None):
+    """The check_zeros diagnostic of fast_matched_filter.py:322-361, including
+    its slicing of the last axis in the per-channel layout.  ``counts``: the
+    per-template zero counts already made on the device (else counted here)."""
+    check_zeros = _check_zeros_option(check_zeros)
     if not check_zeros:
         return None
-    stop = int(n_corr - moveouts_flat.max() / step)
-    if check_zeros == "first":
-        if network_sum:
-            zeros = np.sum(cc[0:1, :stop] == 0.0, axis=-1)
-        else:
-            zeros = np.sum(cc[0:1, :, :, :stop] == 0.0, axis=(1, 2, 3))
+    if counts is not None:
+        zeros = counts[0:1] if check_zeros == "first" else counts
     else:
-        zeros = np.sum(cc[..., :stop].reshape(n_templates, -1) == 0.0, axis=-1)
+        stop = int(n_corr - moveouts_flat.max() / step)
+        if check_zeros == "first":
+            if network_sum:
+                zeros = np.sum(cc[0:1, :stop] == 0.0, axis=-1)
+            else:
+                zeros = np.sum(cc[0:1, :, :, :stop] == 0.0, axis=(1, 2, 3))
+        else:
+            zeros = np.sum(cc[..., :stop].reshape(n_templates, -1) == 0.0, axis=-1)
     threshold = 10
     if not network_sum:
         threshold *= np.sum(weights_flat[0, ...] > 0.0)
@@ -203,19 +220,26 @@ def matched_filter(templates, moveouts, weights, data, step,
             _ptr(pp["moveouts"], ct.c_int), _ptr(pp["data"], ct.c_float),
             _ptr(pp["weights"], ct.c_float), pp["step"], pp["L"], pp["N"], T, S, C,
             n_corr, _ptr(cc, ct.c_float), pp["normalize"], int(bool(network_sum)))
-    if precision == "fp32":
+    check_zeros = _check_zeros_option(check_zeros)
+    flags = 0 if precision == "fp32" else autotune.flags_for(pp["L"], pp["step"], S * C, normalize,
+                                                              precision)
+    ex = (pp["templates"].ctypes.data, _addr(pp["sst"]), pp["moveouts"].ctypes.data,
+          pp["data"].ctypes.data, pp["weights"].ctypes.data, pp["step"], pp["L"], pp["N"],
+          T, S, C, n_corr, cc.ctypes.data, pp["normalize"], int(bool(network_sum)),
+          _lib.PRECISIONS[precision], flags, None)
+    counts = None
+    if check_zeros:  # counted on the device before the copy out
+        counts = np.zeros(T, dtype=np.uint64)
+        stop = _zero_stop(pp["moveouts"], n_corr, pp["step"], n_corr if network_sum else C)
+        st = lib.fmf_matched_filter_check_zeros(*ex, stop, counts.ctypes.data)
+    elif precision == "fp32":
         st = lib.fmf_matched_filter(*args)
     else:
-        flags = autotune.flags_for(pp["L"], pp["step"], S * C, normalize, precision)
-        st = lib.fmf_matched_filter_ex(
-            pp["templates"].ctypes.data, _addr(pp["sst"]), pp["moveouts"].ctypes.data,
-            pp["data"].ctypes.data, pp["weights"].ctypes.data, pp["step"], pp["L"], pp["N"],
-            T, S, C, n_corr, cc.ctypes.data, pp["normalize"], int(bool(network_sum)),
-            _lib.PRECISIONS[precision], flags, None)
+        st = lib.fmf_matched_filter_ex(*ex)
     _lib.check(st, lib)
     cc = cc.reshape(T, n_corr) if network_sum else cc.reshape(T, n_corr, S, C)
     _zero_report(cc, pp["moveouts"], pp["weights"], T, n_corr, pp["step"],
-                 network_sum, check_zeros)
+                 network_sum, check_zeros, counts)
     return cc
 
 

@@ -106,6 +106,24 @@ FMF_API int fmf_matched_filter_ex(const float *templates, const float *sum_squar
                           int precision, int flags, void *stream);
 
 /*
+ * fmf_matched_filter_ex plus the reference wrapper's check_zeros count
+ * (fast_matched_filter.py:322-361), done on the device before the result is
+ * copied out: zero_counts[t] (T values, host or device pointer like the other
+ * arrays) = number of outputs of template t equal to 0 whose last-axis index
+ * is below zero_stop -- the lag for the network sum, the component for the
+ * per-channel layout (the reference slices the last axis in both cases).
+ * zero_stop is clamped to [0, last-axis length].  No reference counterpart as
+ * an entry point.
+ */
+FMF_API int fmf_matched_filter_check_zeros(const float *templates, const float *sum_square_templates,
+                                           const int *moveouts, const float *data, const float *weights,
+                                           size_t step, size_t n_samples_template, size_t n_samples_data,
+                                           size_t n_templates, size_t n_stations, size_t n_components,
+                                           size_t n_corr, float *cc_out, int normalize, int sum_cc_mode,
+                                           int precision, int flags, void *stream, long long zero_stop,
+                                           unsigned long long *zero_counts);
+
+/*
  * Allocation-free entry point.  No counterpart in the reference.
  *
  * For callers that cannot allocate device memory while they run -- a
