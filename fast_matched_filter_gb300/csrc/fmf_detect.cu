@@ -20,15 +20,25 @@
 //            first), each peak still kept removes the peaks closer than
 //            min_separation lags on either side.
 //
-// The order statistics are exact: a radix selection over the order-preserving
-// 32-bit image of the float values, three passes of 11, 11 and 10 bits, each a
-// histogram of the elements that match the bits chosen so far.  Both middle
-// ranks are tracked at once.  Peaks are gathered into a list per template
-// (capacity kDetCap) and filtered by one thread block per template: a sort by
-// lag, a sort by height, and the greedy distance filter.
+// The order statistics are exact.  Each (median, then MAD) is a sample-select:
+//   1. one block per row sorts a strided sample of the row's 32-bit
+//      order-preserving keys and brackets the two middle ranks with a key
+//      window [klo, khi] six binomial standard deviations wide;
+//   2. one pass over the row counts the keys below klo and gathers the keys
+//      inside the window (about 5 % of the row) into a candidate list;
+//   3. if the window holds both middle ranks, a radix selection (three passes
+//      of 11, 11 and 10 bits, each a shared-memory histogram of the keys that
+//      match the bits chosen so far) runs over the candidates only; if not --
+//      heavy ties, an adversarial row -- the same radix selection runs over
+//      the whole row.  Rows no longer than the sample are sorted whole.
+// So a call reads the rows three times (median, MAD, peaks) in the usual case.
+// Peaks are gathered into a list per template (capacity kDetCap) and filtered
+// by one thread block per template: a sort by lag, a sort by height, and the
+// greedy distance filter.
 //
 // Every launch is stream-ordered and the state lives on the device, so a
 // detection run needs no host round trip and can be captured in a graph.
+#include <algorithm>
 #include <cmath>
 
 #include "fmf_common.cuh"
@@ -41,6 +51,12 @@ constexpr int kDetThreads = 256;          // histogram / peak kernels
 constexpr int kDetSelectThreads = 1024;   // per-template filter kernel
 constexpr int kDetChunk = 1024;           // templates per round of scratch
 constexpr int kDetCap = 16384;            // candidate peaks per template row
+constexpr int kDetSample = 16384;         // sampled keys per row (sample-select)
+
+// source of a row's radix selection
+constexpr int kSrcRow = 0;   // the row itself (fallback)
+constexpr int kSrcCand = 1;  // the candidate keys gathered by det_count_kernel
+constexpr int kSrcDone = 2;  // already exact (the row was sorted whole)
 
 struct DetState {
     int begin, end;        // lag window of the row
@@ -48,6 +64,9 @@ struct DetState {
     int rank[2];           // rank still to find inside the chosen bucket
     float med, mad, thr;
     int n_cand;            // local maxima at or above thr (may exceed the capacity)
+    int src;               // kSrcRow / kSrcCand / kSrcDone
+    unsigned klo, khi;     // sample window of the keys
+    int n_lt, n_in;        // keys below klo, keys inside [klo, khi]
 };
 
 // Order-preserving image of a float: a < b  <=>  key(a) < key(b) (for non-NaN
@@ -71,6 +90,23 @@ __device__ __forceinline__ unsigned pass_high_mask(int p)
     return p == 0 ? 0u : (p == 1 ? 0xffe00000u : 0xfffffc00u);
 }
 
+// Split of a row at its first 16-byte boundary: `head` scalar elements, then
+// `nvec` float4s, then `tail` scalar elements.
+struct RowSplit {
+    long long head, nvec, tail;
+};
+
+__device__ __forceinline__ RowSplit split_row(const float *row, long long n)
+{
+    RowSplit r;
+    r.head = (long long)(((16u - ((unsigned)(size_t)row & 15u)) & 15u) >> 2);
+    if (r.head > n)
+        r.head = n;
+    r.nvec = (n - r.head) >> 2;
+    r.tail = n - r.head - 4 * r.nvec;
+    return r;
+}
+
 __global__ void det_init_kernel(DetState *__restrict__ st, int T, int n_corr,
                                 const int *__restrict__ begin, const int *__restrict__ end)
 {
@@ -91,24 +127,184 @@ __global__ void det_init_kernel(DetState *__restrict__ st, int T, int n_corr,
     s.rank[1] = n / 2;
     s.med = s.mad = s.thr = __int_as_float(0x7fc00000);  // NaN until computed
     s.n_cand = 0;
+    s.src = kSrcRow;
+    s.klo = s.khi = 0u;
+    s.n_lt = s.n_in = 0;
     st[t] = s;
 }
 
-// Split of a row at its first 16-byte boundary: `head` scalar elements, then
-// `nvec` float4s, then `tail` scalar elements.
-struct RowSplit {
-    long long head, nvec, tail;
-};
-
-__device__ __forceinline__ RowSplit split_row(const float *row, long long n)
+// Key of a row value: mode 0 the value, mode 1 |value - median| (float32).
+__device__ __forceinline__ unsigned sel_key(float v, int mode, float med)
 {
-    RowSplit r;
-    r.head = (long long)(((16u - ((unsigned)(size_t)row & 15u)) & 15u) >> 2);
-    if (r.head > n)
-        r.head = n;
-    r.nvec = (n - r.head) >> 2;
-    r.tail = n - r.head - 4 * r.nvec;
-    return r;
+    return order_key(mode == 0 ? v : fabsf(__fsub_rn(v, med)));
+}
+
+// The value of the two middle keys, as numpy's median of float32 data.
+__device__ __forceinline__ float middle_value(unsigned ka, unsigned kb, int n)
+{
+    const float a = key_value(ka), b = key_value(kb);
+    return (n & 1) ? a : __fmul_rn(__fadd_rn(a, b), 0.5f);
+}
+
+__device__ __forceinline__ void finish_select(DetState &s, int mode, float v, float n_mad)
+{
+    if (mode == 0) {
+        s.med = v;
+    } else {
+        s.mad = v;
+        s.thr = __fadd_rn(s.med, __fmul_rn(n_mad, v));
+    }
+}
+
+// Ascending bitonic sort of P (a power of two) 32-bit keys in shared memory.
+__device__ void bitonic_sort32(unsigned *a, int P)
+{
+    for (int k = 2; k <= P; k <<= 1)
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            for (int i = threadIdx.x; i < P; i += blockDim.x) {
+                const int l = i ^ j;
+                if (l > i) {
+                    const unsigned x = a[i], y = a[l];
+                    if ((x > y) == ((i & k) == 0)) {
+                        a[i] = y;
+                        a[l] = x;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+}
+
+// Step 1 of the sample-select (one block per row): a strided sample of the
+// row's keys, sorted; either the exact answer (row no longer than the
+// sample) or the key window around the two middle ranks.
+__global__ void __launch_bounds__(1024)
+det_sample_kernel(const float *__restrict__ cc, size_t ld, DetState *__restrict__ st, int mode,
+                  float n_mad)
+{
+    extern __shared__ unsigned long long sample_smem[];
+    unsigned *sk = reinterpret_cast<unsigned *>(sample_smem);  // kDetSample keys
+    const int t = blockIdx.x;
+    DetState s = st[t];
+    const long long n = s.end - s.begin;
+    if (n <= 0)
+        return;
+    const float *row = cc + (size_t)t * ld + s.begin;
+    const int m = n < kDetSample ? (int)n : kDetSample;
+    int P = 1;
+    while (P < m)
+        P <<= 1;
+    for (int i = threadIdx.x; i < P; i += blockDim.x)
+        sk[i] = i < m ? sel_key(row[(long long)i * n / m], mode, s.med) : 0xffffffffu;
+    __syncthreads();
+    bitonic_sort32(sk, P);
+    if (threadIdx.x != 0)
+        return;
+    const long long a = (n - 1) / 2, b = n / 2;
+    s.prefix[0] = s.prefix[1] = 0u;
+    s.rank[0] = (int)a;
+    s.rank[1] = (int)b;
+    s.n_lt = s.n_in = 0;
+    if (m == n) {  // the whole row is sorted
+        finish_select(s, mode, middle_value(sk[a], sk[b], (int)n), n_mad);
+        s.src = kSrcDone;
+    } else {
+        // sample position of rank r is about r*m/n, with a binomial standard
+        // deviation of at most sqrt(m)/2 = 64 positions: bracket by 6 of them
+        constexpr int kPad = 6 * 64 + 16;
+        const long long pa = a * m / n, pb = (b * m + n - 1) / n;
+        s.klo = sk[pa - kPad > 0 ? pa - kPad : 0];
+        s.khi = sk[pb + kPad < m - 1 ? pb + kPad : m - 1];
+        s.src = kSrcCand;
+    }
+    st[t] = s;
+}
+
+// Step 2: one pass over the row: keys below klo counted, keys inside
+// [klo, khi] appended to the row's candidate list (up to cap).
+__global__ void __launch_bounds__(kDetThreads)
+det_count_kernel(const float *__restrict__ cc, size_t ld, DetState *__restrict__ st,
+                 unsigned *__restrict__ cand, long long cap, int mode)
+{
+    const int t = blockIdx.y;
+    const int src = st[t].src;
+    const long long n = st[t].end - st[t].begin;
+    if (src != kSrcCand || n <= 0)
+        return;
+    const unsigned klo = st[t].klo, khi = st[t].khi;
+    const float med = st[t].med;
+    const float *row = cc + (size_t)t * ld + st[t].begin;
+    unsigned *list = cand + (size_t)t * cap;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    constexpr int kWarps = kDetThreads / 32;
+    unsigned lt = 0;  // per-lane count of keys below klo
+    auto take = [&](float v, bool ok) {
+        const unsigned key = sel_key(v, mode, med);
+        lt += (ok && key < klo) ? 1u : 0u;
+        const bool in = ok && key >= klo && key <= khi;
+        const unsigned mask = __ballot_sync(0xffffffffu, in);
+        if (mask) {
+            const int leader = __ffs(mask) - 1;
+            int base = 0;
+            if (lane == leader)
+                base = atomicAdd(&st[t].n_in, __popc(mask));
+            base = __shfl_sync(0xffffffffu, base, leader);
+            const long long pos = base + __popc(mask & ((1u << lane) - 1u));
+            if (in && pos < cap)
+                list[pos] = key;
+        }
+    };
+    const RowSplit rs = split_row(row, n);
+    if (blockIdx.x == 0 && warp == 0) {
+        const long long i = lane < rs.head ? lane : rs.head + 4 * rs.nvec + (lane - rs.head);
+        const bool ok = lane < rs.head + rs.tail;
+        take(ok ? row[i] : 0.f, ok);
+    }
+    const float4 *vrow = reinterpret_cast<const float4 *>(row + rs.head);
+    const long long steps = (rs.nvec + 63) / 64;
+    for (long long c = (long long)blockIdx.x * kWarps + warp; c < steps; c += (long long)gridDim.x * kWarps) {
+        float4 v[2];
+        bool ok[2];
+#pragma unroll
+        for (int u = 0; u < 2; u++) {
+            const long long i = c * 64 + u * 32 + lane;
+            ok[u] = i < rs.nvec;
+            v[u] = ok[u] ? vrow[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+#pragma unroll
+        for (int u = 0; u < 2; u++) {
+            take(v[u].x, ok[u]);
+            take(v[u].y, ok[u]);
+            take(v[u].z, ok[u]);
+            take(v[u].w, ok[u]);
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1)
+        lt += __shfl_down_sync(0xffffffffu, lt, o);
+    if (lane == 0 && lt)
+        atomicAdd(&st[t].n_lt, (int)lt);
+}
+
+// Step 3: does the window hold both middle ranks?  Then select among the
+// candidates; else fall back to the whole row.
+__global__ void det_check_kernel(DetState *__restrict__ st, int T, long long cap)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= T || st[t].src != kSrcCand)
+        return;
+    DetState s = st[t];
+    const long long n = s.end - s.begin;
+    const long long a = (n - 1) / 2, b = n / 2;
+    if (s.n_in <= cap && s.n_lt <= a && b < (long long)s.n_lt + s.n_in) {
+        s.rank[0] = (int)(a - s.n_lt);
+        s.rank[1] = (int)(b - s.n_lt);
+    } else {
+        s.src = kSrcRow;
+        s.rank[0] = (int)a;
+        s.rank[1] = (int)b;
+    }
+    s.prefix[0] = s.prefix[1] = 0u;
+    st[t] = s;
 }
 
 // Histogram update by a whole warp: every lane calls it (lanes whose value
@@ -117,8 +313,7 @@ __device__ __forceinline__ void hist_add(unsigned *h, float v, bool ok, int mode
                                          unsigned dmask, unsigned high, unsigned p0, unsigned p1,
                                          bool two, int lane)
 {
-    const float x = mode == 0 ? v : fabsf(__fsub_rn(v, med));
-    const unsigned key = order_key(x);
+    const unsigned key = mode == 2 ? __float_as_uint(v) : sel_key(v, mode, med);
     const unsigned dig = (key >> shift) & dmask;
     const bool m0 = ok && (key & high) == p0;
     if (__any_sync(0xffffffffu, m0)) {
@@ -142,14 +337,16 @@ __device__ __forceinline__ void hist_add(unsigned *h, float v, bool ok, int mode
 // 16-byte loads, two per lane in flight per step.
 __global__ void __launch_bounds__(kDetThreads)
 det_hist_kernel(const float *__restrict__ cc, size_t ld, const DetState *__restrict__ st,
-                unsigned *__restrict__ hist, int pass, int mode)
+                unsigned *__restrict__ hist, const unsigned *__restrict__ cand, long long cap, int pass,
+                int mode)
 {
     __shared__ unsigned h[2 * kDetBins];
     const int t = blockIdx.y;
     const DetState s = st[t];
-    const long long n = s.end - s.begin;
-    if (n <= 0)
+    if (s.src == kSrcDone || s.end - s.begin <= 0)
         return;  // uniform over the block, before any barrier
+    const bool keys = s.src == kSrcCand;  // candidate keys instead of row values
+    const long long n = keys ? s.n_in : s.end - s.begin;
     for (int i = threadIdx.x; i < 2 * kDetBins; i += kDetThreads)
         h[i] = 0u;
     __syncthreads();
@@ -159,7 +356,11 @@ det_hist_kernel(const float *__restrict__ cc, size_t ld, const DetState *__restr
     const unsigned p0 = s.prefix[0], p1 = s.prefix[1];
     const bool two = p0 != p1;  // the two middle ranks sit in different buckets
     const float med = s.med;
-    const float *row = cc + (size_t)t * ld + s.begin;
+    // candidate keys are stored as the bits of a float whose order key they
+    // are: key_value() turns them back, so both sources run the same code
+    const float *row = keys ? reinterpret_cast<const float *>(cand + (size_t)t * cap)
+                            : cc + (size_t)t * ld + s.begin;
+    const int kmode = keys ? 2 : mode;
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
     constexpr int kWarps = kDetThreads / 32;
@@ -168,7 +369,7 @@ det_hist_kernel(const float *__restrict__ cc, size_t ld, const DetState *__restr
         const long long i = lane < rs.head ? lane : rs.head + 4 * rs.nvec + (lane - rs.head);
         const bool ok = lane < rs.head + rs.tail;
         const float v = ok ? row[i] : 0.f;
-        hist_add(h, v, ok, mode, med, shift, dmask, high, p0, p1, two, lane);
+        hist_add(h, v, ok, kmode, med, shift, dmask, high, p0, p1, two, lane);
     }
     const float4 *vrow = reinterpret_cast<const float4 *>(row + rs.head);
     const long long steps = (rs.nvec + 63) / 64;  // 64 float4s per warp step
@@ -183,10 +384,10 @@ det_hist_kernel(const float *__restrict__ cc, size_t ld, const DetState *__restr
         }
 #pragma unroll
         for (int u = 0; u < 2; u++) {
-            hist_add(h, v[u].x, ok[u], mode, med, shift, dmask, high, p0, p1, two, lane);
-            hist_add(h, v[u].y, ok[u], mode, med, shift, dmask, high, p0, p1, two, lane);
-            hist_add(h, v[u].z, ok[u], mode, med, shift, dmask, high, p0, p1, two, lane);
-            hist_add(h, v[u].w, ok[u], mode, med, shift, dmask, high, p0, p1, two, lane);
+            hist_add(h, v[u].x, ok[u], kmode, med, shift, dmask, high, p0, p1, two, lane);
+            hist_add(h, v[u].y, ok[u], kmode, med, shift, dmask, high, p0, p1, two, lane);
+            hist_add(h, v[u].z, ok[u], kmode, med, shift, dmask, high, p0, p1, two, lane);
+            hist_add(h, v[u].w, ok[u], kmode, med, shift, dmask, high, p0, p1, two, lane);
         }
     }
     __syncthreads();
@@ -208,7 +409,7 @@ __global__ void det_resolve_kernel(DetState *__restrict__ st, unsigned *__restri
     const int lane = threadIdx.x;
     DetState s = st[t];
     const int n = s.end - s.begin;
-    if (n <= 0)
+    if (n <= 0 || s.src == kSrcDone)
         return;
     unsigned *gh = hist + (size_t)t * 2 * kDetBins;
     const int per = (int)pass_bins(pass) / 32;  // bins per lane
@@ -250,19 +451,8 @@ __global__ void det_resolve_kernel(DetState *__restrict__ st, unsigned *__restri
     __syncwarp();
     for (int i = lane; i < 2 * kDetBins; i += 32)
         gh[i] = 0u;
-    if (pass == 2) {
-        const float a = key_value(s.prefix[0]), b = key_value(s.prefix[1]);
-        const float v = (n & 1) ? a : __fmul_rn(__fadd_rn(a, b), 0.5f);
-        if (mode == 0) {
-            s.med = v;
-        } else {
-            s.mad = v;
-            s.thr = __fadd_rn(s.med, __fmul_rn(n_mad, v));
-        }
-        s.prefix[0] = s.prefix[1] = 0u;
-        s.rank[0] = (n - 1) / 2;
-        s.rank[1] = n / 2;
-    }
+    if (pass == 2)
+        finish_select(s, mode, middle_value(s.prefix[0], s.prefix[1], n), n_mad);
     if (lane == 0)
         st[t] = s;
 }
@@ -476,16 +666,22 @@ int detect_device(const float *cc, int T, int n_corr, size_t ld, const int *begi
     int rc;
     const int chunk = T < kDetChunk ? T : kDetChunk;
     DetState *st;
-    unsigned *hist;
+    unsigned *hist, *keys;
     int2 *cand;
+    // candidate keys per row: the sample window holds about 5 % of a row
+    const long long key_cap = n_corr < 65536 ? n_corr : std::max(65536LL, (long long)n_corr / 8);
     if ((rc = ws.get(&st, (size_t)chunk, "detection state")) ||
         (rc = ws.get(&hist, (size_t)chunk * 2 * kDetBins, "detection histograms")) ||
+        (rc = ws.get(&keys, (size_t)chunk * key_cap, "candidate keys")) ||
         (rc = ws.get(&cand, (size_t)chunk * kDetCap, "candidate peaks")))
         return rc;
     cudaError_t e = cudaFuncSetAttribute(det_select_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)select_smem(kDetCap));
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(det_sample_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)(kDetSample * sizeof(unsigned)));
     if (e != cudaSuccess)
-        return set_error(FMF_ERR_CUDA, "detection filter shared memory: %s", cudaGetErrorString(e));
+        return set_error(FMF_ERR_CUDA, "detection shared memory: %s", cudaGetErrorString(e));
     if ((e = cudaMemsetAsync(hist, 0, (size_t)chunk * 2 * kDetBins * sizeof(unsigned), s)) != cudaSuccess)
         return set_error(FMF_ERR_CUDA, "clearing the detection histograms: %s", cudaGetErrorString(e));
     for (int t0 = 0; t0 < T; t0 += chunk) {
@@ -501,17 +697,22 @@ int detect_device(const float *cc, int T, int n_corr, size_t ld, const int *begi
         const dim3 grid((unsigned)per_row, (unsigned)nt);
         det_init_kernel<<<(nt + 127) / 128, 128, 0, s>>>(st, nt, n_corr, begin ? begin + t0 : nullptr,
                                                          end ? end + t0 : nullptr);
-        for (int mode = 0; mode < 2; mode++)
+        for (int mode = 0; mode < 2; mode++) {
+            det_sample_kernel<<<nt, 1024, kDetSample * sizeof(unsigned), s>>>(rows, ld, st, mode, n_mad);
+            det_count_kernel<<<grid, kDetThreads, 0, s>>>(rows, ld, st, keys, key_cap, mode);
+            det_check_kernel<<<(nt + 127) / 128, 128, 0, s>>>(st, nt, key_cap);
             for (int pass = 0; pass < 3; pass++) {
-                det_hist_kernel<<<grid, kDetThreads, 0, s>>>(rows, ld, st, hist, pass, mode);
+                det_hist_kernel<<<grid, kDetThreads, 0, s>>>(rows, ld, st, hist, keys, key_cap, pass,
+                                                             mode);
                 det_resolve_kernel<<<nt, 32, 0, s>>>(st, hist, pass, mode, n_mad);
             }
+        }
         det_peaks_kernel<<<grid, kDetThreads, 0, s>>>(rows, ld, st, cand, kDetCap);
         det_select_kernel<<<nt, kDetSelectThreads, select_smem(kDetCap), s>>>(
             st, cand, kDetCap, min_sep, max_det, med_out ? med_out + t0 : nullptr,
             mad_out ? mad_out + t0 : nullptr, thr_out ? thr_out + t0 : nullptr, count_out + t0,
             lag_out + (size_t)t0 * max_det, val_out + (size_t)t0 * max_det);
-        count_launch(15);
+        count_launch(21);
         if ((rc = check_launch("detection kernels")))
             return rc;
     }
