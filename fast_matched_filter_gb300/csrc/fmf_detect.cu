@@ -238,46 +238,70 @@ det_count_kernel(const float *__restrict__ cc, size_t ld, DetState *__restrict__
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     constexpr int kWarps = kDetThreads / 32;
     unsigned lt = 0;  // per-lane count of keys below klo
-    auto take = [&](float v, bool ok) {
-        const unsigned key = sel_key(v, mode, med);
-        lt += (ok && key < klo) ? 1u : 0u;
-        const bool in = ok && key >= klo && key <= khi;
-        const unsigned mask = __ballot_sync(0xffffffffu, in);
-        if (mask) {
-            const int leader = __ffs(mask) - 1;
-            int base = 0;
-            if (lane == leader)
-                base = atomicAdd(&st[t].n_in, __popc(mask));
-            base = __shfl_sync(0xffffffffu, base, leader);
-            const long long pos = base + __popc(mask & ((1u << lane) - 1u));
-            if (in && pos < cap)
-                list[pos] = key;
+    // One warp step: each lane's up to 8 keys; the keys inside the window are
+    // appended with one atomic per warp (a warp prefix sum places them).
+    auto take8 = [&](const unsigned (&key)[8], const bool (&ok)[8]) {
+        unsigned in_mask = 0;
+#pragma unroll
+        for (int u = 0; u < 8; u++) {
+            lt += (ok[u] && key[u] < klo) ? 1u : 0u;
+            if (ok[u] && key[u] >= klo && key[u] <= khi)
+                in_mask |= 1u << u;
         }
+        const int cnt = __popc(in_mask);
+        int inc = cnt;
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, inc, o);
+            if (lane >= o)
+                inc += y;
+        }
+        const int total = __shfl_sync(0xffffffffu, inc, 31);
+        if (total == 0)
+            return;
+        int base = 0;
+        if (lane == 31)
+            base = atomicAdd(&st[t].n_in, total);
+        base = __shfl_sync(0xffffffffu, base, 31);
+        long long pos = (long long)base + inc - cnt;
+#pragma unroll
+        for (int u = 0; u < 8; u++)
+            if (in_mask & (1u << u)) {
+                if (pos < cap)
+                    list[pos] = key[u];
+                pos++;
+            }
     };
     const RowSplit rs = split_row(row, n);
     if (blockIdx.x == 0 && warp == 0) {
+        unsigned key[8];
+        bool ok[8];
         const long long i = lane < rs.head ? lane : rs.head + 4 * rs.nvec + (lane - rs.head);
-        const bool ok = lane < rs.head + rs.tail;
-        take(ok ? row[i] : 0.f, ok);
+        ok[0] = lane < rs.head + rs.tail;
+        key[0] = ok[0] ? sel_key(row[i], mode, med) : 0u;
+#pragma unroll
+        for (int u = 1; u < 8; u++) {
+            ok[u] = false;
+            key[u] = 0u;
+        }
+        take8(key, ok);
     }
     const float4 *vrow = reinterpret_cast<const float4 *>(row + rs.head);
     const long long steps = (rs.nvec + 63) / 64;
     for (long long c = (long long)blockIdx.x * kWarps + warp; c < steps; c += (long long)gridDim.x * kWarps) {
-        float4 v[2];
-        bool ok[2];
+        unsigned key[8];
+        bool ok[8];
 #pragma unroll
         for (int u = 0; u < 2; u++) {
             const long long i = c * 64 + u * 32 + lane;
-            ok[u] = i < rs.nvec;
-            v[u] = ok[u] ? vrow[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+            const bool okv = i < rs.nvec;
+            const float4 v = okv ? vrow[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+            key[4 * u + 0] = sel_key(v.x, mode, med);
+            key[4 * u + 1] = sel_key(v.y, mode, med);
+            key[4 * u + 2] = sel_key(v.z, mode, med);
+            key[4 * u + 3] = sel_key(v.w, mode, med);
+            ok[4 * u + 0] = ok[4 * u + 1] = ok[4 * u + 2] = ok[4 * u + 3] = okv;
         }
-#pragma unroll
-        for (int u = 0; u < 2; u++) {
-            take(v[u].x, ok[u]);
-            take(v[u].y, ok[u]);
-            take(v[u].z, ok[u]);
-            take(v[u].w, ok[u]);
-        }
+        take8(key, ok);
     }
     for (int o = 16; o > 0; o >>= 1)
         lt += __shfl_down_sync(0xffffffffu, lt, o);
