@@ -238,12 +238,13 @@ det_count_kernel(const float *__restrict__ cc, size_t ld, DetState *__restrict__
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     constexpr int kWarps = kDetThreads / 32;
     unsigned lt = 0;  // per-lane count of keys below klo
-    // One warp step: each lane's up to 8 keys; the keys inside the window are
+    // One warp step: each lane's up to 16 keys; the keys inside the window are
     // appended with one atomic per warp (a warp prefix sum places them).
-    auto take8 = [&](const unsigned (&key)[8], const bool (&ok)[8]) {
+    constexpr int kK = 16;
+    auto take = [&](const unsigned (&key)[kK], const bool (&ok)[kK]) {
         unsigned in_mask = 0;
 #pragma unroll
-        for (int u = 0; u < 8; u++) {
+        for (int u = 0; u < kK; u++) {
             lt += (ok[u] && key[u] < klo) ? 1u : 0u;
             if (ok[u] && key[u] >= klo && key[u] <= khi)
                 in_mask |= 1u << u;
@@ -264,7 +265,7 @@ det_count_kernel(const float *__restrict__ cc, size_t ld, DetState *__restrict__
         base = __shfl_sync(0xffffffffu, base, 31);
         long long pos = (long long)base + inc - cnt;
 #pragma unroll
-        for (int u = 0; u < 8; u++)
+        for (int u = 0; u < kK; u++)
             if (in_mask & (1u << u)) {
                 if (pos < cap)
                     list[pos] = key[u];
@@ -273,35 +274,39 @@ det_count_kernel(const float *__restrict__ cc, size_t ld, DetState *__restrict__
     };
     const RowSplit rs = split_row(row, n);
     if (blockIdx.x == 0 && warp == 0) {
-        unsigned key[8];
-        bool ok[8];
+        unsigned key[kK];
+        bool ok[kK];
         const long long i = lane < rs.head ? lane : rs.head + 4 * rs.nvec + (lane - rs.head);
         ok[0] = lane < rs.head + rs.tail;
         key[0] = ok[0] ? sel_key(row[i], mode, med) : 0u;
 #pragma unroll
-        for (int u = 1; u < 8; u++) {
+        for (int u = 1; u < kK; u++) {
             ok[u] = false;
             key[u] = 0u;
         }
-        take8(key, ok);
+        take(key, ok);
     }
     const float4 *vrow = reinterpret_cast<const float4 *>(row + rs.head);
-    const long long steps = (rs.nvec + 63) / 64;
+    const long long steps = (rs.nvec + 127) / 128;  // 128 float4s per warp step
     for (long long c = (long long)blockIdx.x * kWarps + warp; c < steps; c += (long long)gridDim.x * kWarps) {
-        unsigned key[8];
-        bool ok[8];
+        unsigned key[kK];
+        bool ok[kK];
+        float4 v[4];
 #pragma unroll
-        for (int u = 0; u < 2; u++) {
-            const long long i = c * 64 + u * 32 + lane;
-            const bool okv = i < rs.nvec;
-            const float4 v = okv ? vrow[i] : make_float4(0.f, 0.f, 0.f, 0.f);
-            key[4 * u + 0] = sel_key(v.x, mode, med);
-            key[4 * u + 1] = sel_key(v.y, mode, med);
-            key[4 * u + 2] = sel_key(v.z, mode, med);
-            key[4 * u + 3] = sel_key(v.w, mode, med);
+        for (int u = 0; u < 4; u++) {
+            const long long i = c * 128 + u * 32 + lane;
+            v[u] = i < rs.nvec ? vrow[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            const bool okv = c * 128 + u * 32 + lane < rs.nvec;
+            key[4 * u + 0] = sel_key(v[u].x, mode, med);
+            key[4 * u + 1] = sel_key(v[u].y, mode, med);
+            key[4 * u + 2] = sel_key(v[u].z, mode, med);
+            key[4 * u + 3] = sel_key(v[u].w, mode, med);
             ok[4 * u + 0] = ok[4 * u + 1] = ok[4 * u + 2] = ok[4 * u + 3] = okv;
         }
-        take8(key, ok);
+        take(key, ok);
     }
     for (int o = 16; o > 0; o >>= 1)
         lt += __shfl_down_sync(0xffffffffu, lt, o);
