@@ -574,13 +574,27 @@ def run_detection(cfg, dev_out, world, steps=3, warmup=1):
             "detections": int(counts[counts > 0].sum()), "settings": DETECT_KW,
             "roofline": {"bound": "hbm", "achieved": gbs, "peak": peaks["hbm_gbs"],
                          "unit": "GB/s", "frac": gbs / peaks["hbm_gbs"],
-                         "traffic": rows * 4 * 7,
-                         "traffic_source": "7 reads of the rows per call (6 radix-selection "
-                                           "passes + the peak pass), from the det_hist_kernel "
-                                           "profile: each pass reads the rows once",
+                         "traffic": profiled_detect_traffic(rows),
+                         "traffic_source": "fmf_detect_64rows_day.md: DRAM bytes of one call's "
+                                           "launches per row byte, scaled to these rows",
                          "peak_source": "%s hbm_gbs (copy)" % peak_kind,
                          "kernel": "fmf_detect (det_hist x6, det_resolve x6, det_peaks, "
                                    "det_select)"}}
+
+
+def profiled_detect_traffic(lags):
+    """DRAM bytes of one detection call over `lags` row values, from the
+    committed launch-list profile (bytes per row byte, which stays constant
+    as the rows grow: every pass reads each row once)."""
+    path = os.path.join(HERE, "profiles", "fmf_detect_64rows_day.md")
+    try:
+        with open(path) as f:
+            for line in f:
+                if line.startswith("dram_bytes_per_row_byte:"):
+                    return float(line.split(":")[1]) * lags * 4
+    except OSError:
+        pass
+    return None
 
 
 def run_e2e_detect(cfg, precision, args, world, lib):

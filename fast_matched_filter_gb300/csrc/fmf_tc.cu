@@ -31,15 +31,20 @@
 //   * Split-BF16: operands are bf16 hi + lo (x = hi + lo to 2^-16 relative);
 //     three MMAs per K step (hi*hi, hi*lo, lo*hi) accumulate in FP32 in TMEM.
 //
-// CTA = one template x NB*Q consecutive outputs, all channels:
-//   warp 0      producer: cp.async.bulk (TMA bulk copies) of the data rows and
-//               the template blocks of one (channel, phase) stage, two stages
-//               in flight, mbarrier complete_tx;
-//   warp 1      allocates TMEM (two NB-column FP32 accumulators) and one
-//               thread issues tcgen05.mma, tcgen05.commit to the barriers;
+// Persistent CTAs (one per SM) take items (one template x NB*Q consecutive
+// outputs, all channels) from a tile queue:
+//   warp 0      producer: claims items, cp.async.bulk (TMA bulk copies) of the
+//               data rows and template blocks of one (channel, phase) stage
+//               into stage buffer b (b = parity of the channel's running
+//               index), mbarrier complete_tx;
+//   warps 1, 2  MMA issuers: one thread each issues tcgen05.mma for the
+//               channels of its parity, from its stage buffer into its FP32
+//               accumulator in TMEM, and commits to the barriers (a single
+//               issuing thread cannot keep the tensor pipe busy);
+//   warp 1      also allocates the TMEM (two accumulators + the network sum);
 //   warps 4-11  epilogue: tcgen05.ld of the accumulator, normalisation by the
 //               FP64 window statistics, threshold, weighted network sum in
-//               registers (channel order, fused multiply-add), outputs.
+//               TMEM (channel order, fused multiply-add), outputs.
 // Every wait is bounded (globaltimer); on timeout the CTA raises an error
 // word, stops issuing, waits for its own copies/MMAs (bounded) and frees TMEM.
 #include <cuda_bf16.h>
@@ -51,7 +56,7 @@ namespace fmf {
 constexpr int TC_Q = 128;
 constexpr int TC_CB = TC_Q / 8;
 constexpr int TC_EPI_WARPS = 8;                    // epilogue warps (2 per TMEM lane quarter)
-constexpr int TC_THREADS = 32 * (4 + TC_EPI_WARPS);  // + producer, MMA and 2 idle warps
+constexpr int TC_THREADS = 32 * (4 + TC_EPI_WARPS);  // + producer, 2 MMA issuers, 1 idle warp
 constexpr int TC_TG = 16;  // templates interleaved per group of CTAs (L2 reuse of data rows)
 constexpr unsigned long long TC_WAIT_NS = 2000000000ull;  // 2 s per wait
 
@@ -413,10 +418,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1) tc_persistent(const __grid_cons
             mbar_init(dfull0 + 8 * i, 1);
             mbar_init(dempty0 + 8 * i, TC_EPI_WARPS);
         }
-        mbar_init(fin, 1);
+        mbar_init(fin, 2);  // one commit per MMA issuer
         for (int i = 0; i < 4; i++) {
             mbar_init(ifull0 + 8 * i, 1);
-            mbar_init(iempty0 + 8 * i, 1 + TC_EPI_WARPS);  // MMA thread + epilogue warps
+            mbar_init(iempty0 + 8 * i, 2 + TC_EPI_WARPS);  // MMA issuers + epilogue warps
         }
         *abort_flag = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -438,14 +443,19 @@ __global__ void __launch_bounds__(TC_THREADS, 1) tc_persistent(const __grid_cons
 
     if (warp == 0) {
         // ---------------------------------------------------------- producer + tile queue
-        int j = 0;
-        for (long long q = 0;; q++) {
+        // Stage buffer b holds the stages of the channels whose running index g
+        // (over the active channels of all items, in order) has parity b; MMA
+        // issuer b consumes them.  uses[b] counts the stages put in buffer b.
+        int uses[2] = {0, 0};
+        long long g = 0;
+        bool ok = true;
+        for (long long q = 0; ok; q++) {
             const int slot = (int)(q & 3);
             long long item = total;
             if (lane == 0) {
-                bool ok = q < 4 || mbar_wait(iempty0 + 8 * slot, (uint32_t)(((q >> 2) - 1) & 1), abort_flag,
-                                             B.err, 1u);
-                if (ok && !*abort_flag)
+                bool got = q < 4 || mbar_wait(iempty0 + 8 * slot, (uint32_t)(((q >> 2) - 1) & 1), abort_flag,
+                                              B.err, 1u);
+                if (got && !*abort_flag)
                     item = (long long)atomicAdd(B.queue, 1ull);
                 ring[slot] = item;
                 mbar_arrive(ifull0 + 8 * slot);
@@ -465,45 +475,70 @@ __global__ void __launch_bounds__(TC_THREADS, 1) tc_persistent(const __grid_cons
             const uint32_t data_bytes = (uint32_t)TC_CB * R * 16, wbytes = (uint32_t)NW * 128;
             const uint32_t w_off = (split ? 2u : 1u) * data_bytes;
             const float *w = P.w + (size_t)t * SC;
-            for (int ch = 0; ch < SC; ch++) {
-                if (w[ch] == 0.0f)
-                    continue;
-                for (int phi = 0; phi < step; phi++, j++) {
-                    const int s = j & 1;
-                    if (j >= 2 &&
-                        !mbar_wait_warp(empty0 + 8 * s, ((j >> 1) - 1) & 1, abort_flag, B.err, 2u))
-                        goto producer_done;
-                    const long long meta = ((long long)t * SC + ch) * step + phi;
-                    const int mu = pr.mu[meta], psi = pr.psi[meta];
-                    const int sres = ((mu % TC_Q) + TC_Q) % TC_Q;
-                    const long long r0 = (I0 + mu - sres) / TC_Q + pr.row_front;
-                    const uint32_t st = smem_u32(smem + (size_t)s * B.stage_bytes);
-                    if (lane == 0)
-                        mbar_expect_tx(full0 + 8 * s, (split ? 2u : 1u) * (data_bytes + wbytes));
-                    __syncwarp();
-                    const int cb = lane & 15, hl = lane >> 4;
-                    if (hl == 0 || split) {
-                        const uint16_t *src = (hl ? pr.g_lo : pr.g_hi) +
-                                              ((((long long)ch * step + psi) * TC_CB + cb) * pr.rows_total + r0) * 8;
-                        bulk_g2s(st + hl * data_bytes + cb * (uint32_t)R * 16, src, (uint32_t)R * 16,
-                                 full0 + 8 * s);
-                    }
-                    if (lane < (split ? 2 : 1)) {
-                        const uint16_t *src = (lane ? pr.w_lo : pr.w_hi) + meta * NW * 64;
-                        bulk_g2s(st + w_off + lane * wbytes, src, wbytes, full0 + 8 * s);
-                    }
+            // one stage: phase phi of channel ch into buffer b
+            auto load_stage = [&](int ch, int phi, int b) -> bool {
+                if (uses[b] >= 1 &&
+                    !mbar_wait_warp(empty0 + 8 * b, (uses[b] - 1) & 1, abort_flag, B.err, 2u))
+                    return false;
+                const long long meta = ((long long)t * SC + ch) * step + phi;
+                const int mu = pr.mu[meta], psi = pr.psi[meta];
+                const int sres = ((mu % TC_Q) + TC_Q) % TC_Q;
+                const long long r0 = (I0 + mu - sres) / TC_Q + pr.row_front;
+                const uint32_t st = smem_u32(smem + (size_t)b * B.stage_bytes);
+                if (lane == 0)
+                    mbar_expect_tx(full0 + 8 * b, (split ? 2u : 1u) * (data_bytes + wbytes));
+                __syncwarp();
+                const int cb = lane & 15, hl = lane >> 4;
+                if (hl == 0 || split) {
+                    const uint16_t *src = (hl ? pr.g_lo : pr.g_hi) +
+                                          ((((long long)ch * step + psi) * TC_CB + cb) * pr.rows_total + r0) * 8;
+                    bulk_g2s(st + hl * data_bytes + cb * (uint32_t)R * 16, src, (uint32_t)R * 16,
+                             full0 + 8 * b);
                 }
+                if (lane < (split ? 2 : 1)) {
+                    const uint16_t *src = (lane ? pr.w_lo : pr.w_hi) + meta * NW * 64;
+                    bulk_g2s(st + w_off + lane * wbytes, src, wbytes, full0 + 8 * b);
+                }
+                uses[b]++;
+                return true;
+            };
+            auto next_active = [&](int ch) {
+                while (ch < SC && w[ch] == 0.0f)
+                    ch++;
+                return ch;
+            };
+            // active channels in order; with step > 1 two consecutive channels
+            // have their phases interleaved, so that both buffers stay fed
+            int ch = next_active(0);
+            while (ok && ch < SC) {
+                const int ch2 = step > 1 ? next_active(ch + 1) : SC;
+                const bool pair = ch2 < SC;
+                const int b = (int)(g & 1);
+                for (int phi = 0; ok && phi < step; phi++) {
+                    ok = load_stage(ch, phi, b);
+                    if (ok && pair)
+                        ok = load_stage(ch2, phi, b ^ 1);
+                }
+                g += pair ? 2 : 1;
+                ch = next_active((pair ? ch2 : ch) + 1);
             }
         }
-    producer_done:
+        // do not leave with copies in flight
         if (lane == 0)
-            for (int k = max(0, j - 2); k < j; k++)
-                mbar_wait(full0 + 8 * (k & 1), (k >> 1) & 1, abort_flag, B.err, 0u);
+            for (int b = 0; b < 2; b++)
+                if (uses[b] >= 1)
+                    mbar_wait(full0 + 8 * b, (uses[b] - 1) & 1, abort_flag, B.err, 0u);
         __syncwarp();
-    } else if (warp == 1) {
-        // ---------------------------------------------------------- MMA issuer
+    } else if (warp == 1 || warp == 2) {
+        // ---------------------------------------------------------- MMA issuers
+        // Two issuing threads (one per warp, on two SM sub-partitions): one
+        // thread cannot issue tcgen05.mma fast enough to keep the tensor pipe
+        // busy.  Issuer m takes the active channels of parity m (running index
+        // c over all items), stage buffer m and accumulator m.
+        const int m = warp - 1;
         if (lane == 0) {
-            int j = 0, c = 0;
+            int used = 0;  // stages consumed from buffer m
+            long long c = 0;
             for (long long q = 0;; q++) {
                 const int slot = (int)(q & 3);
                 if (!mbar_wait(ifull0 + 8 * slot, (uint32_t)((q >> 2) & 1), abort_flag, B.err, 32u))
@@ -531,16 +566,20 @@ __global__ void __launch_bounds__(TC_THREADS, 1) tc_persistent(const __grid_cons
                 for (int ch = 0; ch < SC; ch++) {
                     if (w[ch] == 0.0f)
                         continue;
-                    const int d = c % TC_NACC;
+                    if ((c & 1) != m) {  // the other issuer's channel
+                        c++;
+                        continue;
+                    }
+                    const int d = m;  // accumulator m, reused every second channel
                     if (c >= TC_NACC &&
                         !mbar_wait(dempty0 + 8 * d, ((c / TC_NACC) - 1) & 1, abort_flag, B.err, 4u))
                         goto mma_done;
                     tc_fence_after();
                     const uint32_t dt = tmem + (uint32_t)(d * TC_NB_MAX);
                     uint32_t acc = 0;
-                    for (int phi = 0; phi < step; phi++, j++) {
-                        const int s = j & 1;
-                        if (!mbar_wait(full0 + 8 * s, (j >> 1) & 1, abort_flag, B.err, 8u))
+                    for (int phi = 0; phi < step; phi++, used++) {
+                        const int s = m;
+                        if (!mbar_wait(full0 + 8 * s, used & 1, abort_flag, B.err, 8u))
                             goto mma_done;
                         tc_fence_after();
                         const long long meta = ((long long)t * SC + ch) * step + phi;
