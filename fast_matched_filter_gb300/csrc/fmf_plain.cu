@@ -22,7 +22,10 @@
 // Two stage buffers are in flight.
 //
 // Inner loop: a 20-register sliding window of data per thread; per 4 taps one
-// 16-byte data load, one 16-byte broadcast template load and 64 FMAs.
+// 16-byte data load, one 16-byte broadcast template load and 64 FMAs.  Taps
+// run in blocks of 80 (a multiple of the 16-float padding period), so every
+// shared-memory offset inside a block is a compile-time constant and the loop
+// issues almost nothing but loads and FMAs.
 //
 // Epilogue per channel (fused): numerator of "full" minus m*sum(t'),
 // den = sst * E (E and m from the FP64 window statistics), threshold 1e-6 on
@@ -98,35 +101,57 @@ __device__ __forceinline__ void load_stage(float *buf, const Problem &P, const P
     }
 }
 
+// PL_U taps of one thread: data window advanced in place (ring of PL_U
+// registers), template taps broadcast.  `d` points at data offset q of the
+// thread's window, `tq` at template tap q; PADY(y) is the padded offset of
+// data index q + y (q a multiple of 16, so it is a compile-time constant).
+#define PL_TAPS_BODY(d, tq, PADY)                                                              \
+    _Pragma("unroll") for (int s = 0; s < 5; s++)                                              \
+    {                                                                                          \
+        float4 v = *reinterpret_cast<const float4 *>((d) + PADY(16 + 4 * s));                  \
+        win[(16 + 4 * s + 0) % PL_U] = v.x;                                                    \
+        win[(16 + 4 * s + 1) % PL_U] = v.y;                                                    \
+        win[(16 + 4 * s + 2) % PL_U] = v.z;                                                    \
+        win[(16 + 4 * s + 3) % PL_U] = v.w;                                                    \
+        float4 tv4 = *reinterpret_cast<const float4 *>((tq) + 4 * s);                          \
+        float tv[4] = {tv4.x, tv4.y, tv4.z, tv4.w};                                            \
+        _Pragma("unroll") for (int jj = 0; jj < 4; jj++)                                       \
+            _Pragma("unroll") for (int r = 0; r < PL_R; r++)                                   \
+                acc[r] = fmaf(tv[jj], win[(4 * s + r + jj) % PL_U], acc[r]);                   \
+    }
+
 __device__ __forceinline__ void compute_phase(const float *buf, const PlainGeom &g, float acc[PL_R])
 {
     const float *tb = buf + g.data_floats;
-    const int x0 = threadIdx.x * PL_R;
+    const int x0 = threadIdx.x * PL_R;  // a multiple of 16: padx(x0 + y) = padx(x0) + padx(y)
+    const float *db = buf + padx(x0);
     float win[PL_U];
 #pragma unroll
     for (int i = 0; i < 4; i++) {
-        float4 v = *reinterpret_cast<const float4 *>(buf + padx(x0 + 4 * i));
+        float4 v = *reinterpret_cast<const float4 *>(db + padx(4 * i));
         win[4 * i + 0] = v.x;
         win[4 * i + 1] = v.y;
         win[4 * i + 2] = v.z;
         win[4 * i + 3] = v.w;
     }
-    for (int q = 0; q < g.lq_pad; q += PL_U) {
+    int q = 0;
+    // blocks of 80 taps (a multiple of 16 and of PL_U): every padded offset is a constant
+    for (; q + 4 * PL_U <= g.lq_pad; q += 4 * PL_U) {
+        const float *d = db + padx(q);
+        const float *tq = tb + q;
 #pragma unroll
-        for (int s = 0; s < 5; s++) {
-            float4 v = *reinterpret_cast<const float4 *>(buf + padx(x0 + q + 16 + 4 * s));
-            win[(16 + 4 * s + 0) % PL_U] = v.x;
-            win[(16 + 4 * s + 1) % PL_U] = v.y;
-            win[(16 + 4 * s + 2) % PL_U] = v.z;
-            win[(16 + 4 * s + 3) % PL_U] = v.w;
-            float4 tv4 = *reinterpret_cast<const float4 *>(tb + q + 4 * s);
-            float tv[4] = {tv4.x, tv4.y, tv4.z, tv4.w};
-#pragma unroll
-            for (int jj = 0; jj < 4; jj++)
-#pragma unroll
-                for (int r = 0; r < PL_R; r++)
-                    acc[r] = fmaf(tv[jj], win[(4 * s + r + jj) % PL_U], acc[r]);
+        for (int it = 0; it < 4; it++) {
+#define PL_PADY(y) padx(it * PL_U + (y))
+            PL_TAPS_BODY(d, tq + it * PL_U, PL_PADY)
+#undef PL_PADY
         }
+    }
+    // the remaining taps, PL_U at a time
+    for (; q < g.lq_pad; q += PL_U) {
+#define PL_PADQ(y) (padx(q + (y)) - padx(q))
+        const float *d = db + padx(q);
+        PL_TAPS_BODY(d, tb + q, PL_PADQ)
+#undef PL_PADQ
     }
 }
 
