@@ -673,6 +673,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1) tc_persistent(const __grid_cons
             const int a_lo = (int)max(0LL, (klo - kb + TC_Q - 1) / TC_Q) - a0;
             const int a_hi = (int)min((long long)nb, (khi - kb + TC_Q - 1) / TC_Q) - a0;
             const bool any = busy && a_hi > a_lo;
+            // the whole warp's outputs of this item are valid (the usual case)
+            const bool interior = __all_sync(0xffffffffu, a_lo <= 0 && a_hi >= NC);
             const long long qs = (long long)TC_Q * step;
             const float *w = pr.P.w + (size_t)t * SC;
             const int *mo = pr.P.mo + (size_t)t * SC;
@@ -720,18 +722,39 @@ __global__ void __launch_bounds__(TC_THREADS, 1) tc_persistent(const __grid_cons
                         if (lane == 0)
                             mbar_arrive(dempty0 + 8 * d);
                     }
+                    if (nsum && interior) {
+                        // every output of the warp is valid: no per-value range test
+                        if (first) {
 #pragma unroll
-                    for (int i = 0; i < CH; i++) {
-                        const int a = c0 + i;
-                        const float num = full ? fmaf(-mm[i], ts, x[i]) : x[i];
-                        const float den = sst * e[i];
-                        float cc = den > kThreshold ? num * rsqrtf(den) : 0.0f;
-                        if (!(a >= a_lo && a < a_hi))
-                            cc = 0.0f;
-                        if (nsum)
-                            sv[i] = fmaf(cc, wc, first ? 0.0f : sv[i]);
-                        else if (a >= a_lo && a < a_hi)
-                            oc[(size_t)a * TC_Q * SC] = cc;
+                            for (int i = 0; i < CH; i++) {
+                                const float num = full ? fmaf(-mm[i], ts, x[i]) : x[i];
+                                const float den = sst * e[i];
+                                const float cc = den > kThreshold ? num * rsqrtf(den) : 0.0f;
+                                sv[i] = fmaf(cc, wc, 0.0f);
+                            }
+                        } else {
+#pragma unroll
+                            for (int i = 0; i < CH; i++) {
+                                const float num = full ? fmaf(-mm[i], ts, x[i]) : x[i];
+                                const float den = sst * e[i];
+                                const float cc = den > kThreshold ? num * rsqrtf(den) : 0.0f;
+                                sv[i] = fmaf(cc, wc, sv[i]);
+                            }
+                        }
+                    } else {
+#pragma unroll
+                        for (int i = 0; i < CH; i++) {
+                            const int a = c0 + i;
+                            const float num = full ? fmaf(-mm[i], ts, x[i]) : x[i];
+                            const float den = sst * e[i];
+                            float cc = den > kThreshold ? num * rsqrtf(den) : 0.0f;
+                            if (!(a >= a_lo && a < a_hi))
+                                cc = 0.0f;
+                            if (nsum)
+                                sv[i] = fmaf(cc, wc, first ? 0.0f : sv[i]);
+                            else if (a >= a_lo && a < a_hi)
+                                oc[(size_t)a * TC_Q * SC] = cc;
+                        }
                     }
                     if (nsum)
                         tmem_stc<CH>(s_cols + c0, sv);
