@@ -129,10 +129,26 @@ def cases():
     return out
 
 
+def reference_data_cases(ref_root):
+    """The reference test suite's 'noisy' dataset (tests/data/noisy_*.npy, used by
+    test_python.py:27-40 with weights 1/S), cropped to 10,000 samples around the
+    dataset's largest coefficient (lag 83,437), so that the fixture stays small."""
+    ddir = os.path.join(ref_root, "fast_matched_filter", "tests", "data")
+    data = np.load(os.path.join(ddir, "noisy_data.npy"))
+    tp = np.load(os.path.join(ddir, "noisy_template.npy"))
+    pads = np.load(os.path.join(ddir, "noisy_pads.npy"))
+    T, S = tp.shape[0], data.shape[0]
+    crop = np.ascontiguousarray(data[..., 80000:90000])
+    inputs = dict(templates=tp, moveouts=pads, weights=np.ones((T, S), np.float32) / S,
+                  data=crop, step=1)
+    return [("reference_noisy_crop", inputs,
+             dict(arch="cpu", normalize="short", network_sum=True))]
+
+
 def main(ref_root="/root/reference"):
     cpu.build(os.path.join(ref_root, "fast_matched_filter", "src", "matched_filter.c"))
     ref = load_reference_wrapper(ref_root)
-    for name, inputs, opts in cases():
+    for name, inputs, opts in cases() + reference_data_cases(ref_root):
         cc = ref.matched_filter(check_zeros=False, **inputs, **opts)
         arrays = {k: np.asarray(v) for k, v in inputs.items()}
         np.savez_compressed(os.path.join(HERE, name + ".npz"), cc=cc,

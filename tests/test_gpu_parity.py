@@ -176,3 +176,14 @@ def test_synthetic_self_test_finds_templates():
                                   template_duration=4, data_duration=600, sampling_rate=50)
     cc = out[4]
     assert np.all(np.abs(cc.max(axis=1) - 6.0) < 1e-4)
+
+
+@pytest.mark.parametrize("precision", ["fp32", "split_bf16"])
+def test_reference_noisy_dataset_peak(precision):
+    """The reference test suite's 'noisy' dataset (cropped to 80,000-90,000 in the
+    committed fixture): the known largest coefficient, 0.079792 at lag 83,437."""
+    inputs, opts, expected = load_golden("reference_noisy_crop")
+    got = fmf.matched_filter(check_zeros=False, precision=precision, **inputs)
+    assert_parity(got, expected.reshape(got.shape))
+    assert abs(float(got.max()) - 0.079792) < 5e-7
+    assert int(np.argmax(got[0])) == 83437 - 80000
