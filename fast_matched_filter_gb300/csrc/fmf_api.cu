@@ -674,19 +674,40 @@ static int search_detect_entry(const Args &a0, const DetectOut &o, cudaStream_t 
     Args d = a;
     if (!device && (rc = copy_inputs(a, ws, s, &d)))
         return rc;
-    float *cc;
-    if ((rc = ws.get(&cc, a.T * a.n_corr, "cc sums")))
-        return rc;
-    d.out = cc;
-    Problem P;
-    if ((rc = run_device_ws(d, s, ws, &P)))
-        return rc;
     DetectDev dd;
-    if ((rc = detect_outputs(o, a.T, device, ws, &dd)) ||
-        (rc = detect_device(cc, (int)a.T, (int)a.n_corr, a.n_corr, P.k_lo, P.k_hi, o.n_mad,
-                            (int)o.min_sep, (int)o.max_det, dd.med, dd.mad, dd.thr, dd.count, dd.lag,
-                            dd.val, ws, s)))
+    if ((rc = detect_outputs(o, a.T, device, ws, &dd)))
         return rc;
+    // templates in chunks whose cc rows take at most 16 GiB of device memory
+    // (FMF_SEARCH_DETECT_CHUNK_BYTES overrides the limit)
+    const size_t SC = a.S * a.C;
+    size_t chunk_bytes = (size_t)16 << 30;
+    if (const char *env = getenv("FMF_SEARCH_DETECT_CHUNK_BYTES"))
+        chunk_bytes = (size_t)strtoull(env, nullptr, 10);
+    size_t per = chunk_bytes / (a.n_corr * sizeof(float));
+    per = per < 1 ? 1 : (per > a.T ? a.T : per);
+    for (size_t t0 = 0; t0 < a.T; t0 += per) {
+        const size_t nt = a.T - t0 < per ? a.T - t0 : per;
+        Scratch wc(s);  // this chunk's working arrays, freed in stream order
+        Args dc = d;
+        dc.T = nt;
+        dc.tpl = d.tpl + t0 * SC * a.L;
+        dc.sst = d.sst ? d.sst + t0 * SC : nullptr;
+        dc.mo = d.mo + t0 * SC;
+        dc.w = d.w + t0 * SC;
+        float *cc;
+        if ((rc = wc.get(&cc, nt * a.n_corr, "cc sums")))
+            return rc;
+        dc.out = cc;
+        Problem P;
+        const size_t od = t0 * o.max_det;
+        if ((rc = run_device_ws(dc, s, wc, &P)) ||
+            (rc = detect_device(cc, (int)nt, (int)a.n_corr, a.n_corr, P.k_lo, P.k_hi, o.n_mad,
+                                (int)o.min_sep, (int)o.max_det, dd.med ? dd.med + t0 : nullptr,
+                                dd.mad ? dd.mad + t0 : nullptr, dd.thr ? dd.thr + t0 : nullptr,
+                                dd.count + t0, dd.lag ? dd.lag + od : nullptr,
+                                dd.val ? dd.val + od : nullptr, wc, s)))
+            return rc;
+    }
     if (device)
         return FMF_OK;
     if ((rc = detect_copy_back(o, a.T, dd, s)))

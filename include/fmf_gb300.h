@@ -240,7 +240,9 @@ FMF_API int fmf_detect(const float *cc, size_t n_templates, size_t n_corr, const
  * device memory, then fmf_detect over each template's valid lag range (the
  * lags the search can produce: the reference's per-template start/stop,
  * matched_filter.c:53-76).  Only the detections are returned; the (T, n_corr)
- * cc rows never leave the device.
+ * cc rows never leave the device.  Templates are processed in chunks whose cc
+ * rows take at most 16 GiB of device memory (environment variable
+ * FMF_SEARCH_DETECT_CHUNK_BYTES overrides the limit).
  */
 FMF_API int fmf_matched_filter_detect(const float *templates, const float *sum_square_templates,
                                       const int *moveouts, const float *data, const float *weights,

@@ -128,3 +128,20 @@ def test_search_and_detect_equals_two_steps(precision, normalize, step):
         assert np.array_equal(fused.values[t], two.values[t])
     assert_matches(two, cc, 5.0, 50, 40, b, e)
     assert all(c >= 1 for c in fused.count)  # planted copies are found
+
+
+def test_search_and_detect_in_template_chunks(monkeypatch):
+    """The fused call processes templates in chunks when their correlation rows
+    would not fit its device-memory budget; the result must not depend on it."""
+    from tests._cases import random_search
+    tp, mo, w, d = random_search(41, 7, 3, 2, 90, 20000, 0, 150)
+    kw = dict(n_mad=5.0, min_separation=30, max_detections=16)
+    whole = fmf.matched_filter_detect(tp, mo, w, d, 1, **kw)
+    n_corr = d.shape[-1] - tp.shape[-1] + 1
+    monkeypatch.setenv("FMF_SEARCH_DETECT_CHUNK_BYTES", str(3 * n_corr * 4))  # 3 templates
+    chunked = fmf.matched_filter_detect(tp, mo, w, d, 1, **kw)
+    assert np.array_equal(whole.count, chunked.count)
+    assert np.array_equal(whole.threshold, chunked.threshold)
+    for t in range(tp.shape[0]):
+        assert np.array_equal(whole.lags[t], chunked.lags[t])
+        assert np.array_equal(whole.values[t], chunked.values[t])
