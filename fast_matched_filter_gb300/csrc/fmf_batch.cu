@@ -8,12 +8,20 @@
 // (fmf_tc.cu), or, for FP32, the plain kernel per search.  The graph is
 // captured on the first run (on a stream the batch owns, joined to the
 // caller's stream with events) and replayed afterwards; its scratch lives in
-// graph memory nodes.  Inputs are read when the graph runs, so a batch can be
-// re-run after its input buffers were refilled.
+// graph memory nodes.  The searches' preprocessing (and the FP32 searches)
+// are captured on kBatchBranches forked streams, so they become concurrent
+// branches of the graph: each is small and would leave most of the GPU idle
+// if they ran one after another.  Inputs are read when the graph runs, so a
+// batch can be re-run after its input buffers were refilled.
 #include <cstring>
+#include <memory>
 #include <vector>
 
 #include "fmf_common.cuh"
+
+namespace fmf {
+constexpr int kBatchBranches = 8;  // concurrent graph branches for the per-search work
+}
 
 struct fmf_batch {
     int precision = FMF_PREC_SPLIT_BF16;
@@ -23,6 +31,10 @@ struct fmf_batch {
     std::vector<fmf::Args> searches;
     cudaStream_t stream = nullptr;
     cudaEvent_t ev_in = nullptr, ev_out = nullptr;
+    // fork/join of the capture: branch streams and their events
+    cudaStream_t branch[fmf::kBatchBranches] = {};
+    cudaEvent_t ev_fork = nullptr, ev_main = nullptr;
+    cudaEvent_t ev_join[fmf::kBatchBranches] = {}, ev_rejoin[fmf::kBatchBranches] = {};
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     int launches = 0;  // kernel launches in one replay
@@ -33,45 +45,79 @@ namespace fmf {
 static int batch_record(fmf_batch *b, cudaStream_t s)
 {
     int rc;
-    Scratch ws(s);
-    std::vector<Problem> P(b->searches.size());
-    std::vector<const float *> dtc(b->searches.size());
-    for (size_t i = 0; i < b->searches.size(); i++)
-        if ((rc = prepare_problem(b->searches[i], ws, s, &P[i], &dtc[i])))
-            return rc;
-    if (b->precision == FMF_PREC_FP32) {
-        for (size_t i = 0; i < P.size(); i++)
-            if ((rc = launch_plain_all(P[i], s)))
-                return rc;
-        return FMF_OK;
-    }
-    const int split = b->precision == FMF_PREC_SPLIT_BF16;
-    std::vector<int> nb(P.size());
-    for (size_t i = 0; i < P.size(); i++) {
-        nb[i] = tc_choose_nb(P[i].L, P[i].step, split, b->tile);
-        if (nb[i] == 0)
-            return set_error(FMF_ERR_SMEM, "search %zu: template length %d with step %d does not fit a "
-                                           "tensor-core tile", i, P[i].L, P[i].step);
-    }
-    unsigned *err = nullptr;
-    if ((rc = device_error_word(&err)))
-        return rc;
-    const size_t psz = tc_prob_size();
-    std::vector<unsigned char> probs(psz * P.size());
-    for (size_t i = 0; i < P.size(); i++)
-        if ((rc = tc_prepare(P[i], dtc[i], split, nb[i], b->group, ws, s,
-                             reinterpret_cast<TcProb *>(probs.data() + psz * i))))
-            return rc;
-    for (size_t i0 = 0; i0 < P.size(); i0 += TC_MAX_PROBS) {
-        unsigned long long *queue;
-        if ((rc = ws.get(&queue, 1, "tile queue")))
-            return rc;
-        const int n = (int)(P.size() - i0 < (size_t)TC_MAX_PROBS ? P.size() - i0 : TC_MAX_PROBS);
-        if ((rc = tc_run(reinterpret_cast<const TcProb *>(probs.data() + psz * i0), n, split, queue, err,
-                         s)))
-            return rc;
-    }
-    return FMF_OK;
+    cudaError_t e;
+    Scratch ws(s);  // freed last, on s
+    // fork: the branch streams join the capture
+    if ((e = cudaEventRecord(b->ev_fork, s)) != cudaSuccess)
+        return set_error(FMF_ERR_CUDA, "forking the batch capture: %s", cudaGetErrorString(e));
+    for (int k = 0; k < kBatchBranches; k++)
+        if ((e = cudaStreamWaitEvent(b->branch[k], b->ev_fork, 0)) != cudaSuccess)
+            return set_error(FMF_ERR_CUDA, "forking the batch capture: %s", cudaGetErrorString(e));
+    int status = FMF_OK;
+    {
+        std::vector<std::unique_ptr<Scratch>> bws;  // per-branch scratch, freed on its branch
+        for (int k = 0; k < kBatchBranches; k++)
+            bws.emplace_back(new Scratch(b->branch[k]));
+        const size_t n = b->searches.size();
+        std::vector<Problem> P(n);
+        std::vector<const float *> dtc(n);
+        const int split = b->precision == FMF_PREC_SPLIT_BF16;
+        const bool tc = b->precision != FMF_PREC_FP32;
+        std::vector<int> nb(n);
+        const size_t psz = tc_prob_size();
+        std::vector<unsigned char> probs(psz * n);
+        for (size_t i = 0; i < n && status == FMF_OK; i++) {
+            const int k = (int)(i % kBatchBranches);
+            cudaStream_t si = b->branch[k];
+            if ((status = prepare_problem(b->searches[i], *bws[k], si, &P[i], &dtc[i])))
+                break;
+            if (!tc) {
+                status = launch_plain_all(P[i], si);
+                continue;
+            }
+            nb[i] = tc_choose_nb(P[i].L, P[i].step, split, b->tile);
+            if (nb[i] == 0) {
+                status = set_error(FMF_ERR_SMEM, "search %zu: template length %d with step %d does not "
+                                                 "fit a tensor-core tile", i, P[i].L, P[i].step);
+                break;
+            }
+            status = tc_prepare(P[i], dtc[i], split, nb[i], b->group, *bws[k], si,
+                                reinterpret_cast<TcProb *>(probs.data() + psz * i));
+        }
+        // join the branches, then the persistent launches on s
+        for (int k = 0; k < kBatchBranches; k++)
+            if ((e = cudaEventRecord(b->ev_join[k], b->branch[k])) != cudaSuccess ||
+                (e = cudaStreamWaitEvent(s, b->ev_join[k], 0)) != cudaSuccess)
+                status = status ? status : set_error(FMF_ERR_CUDA, "joining the batch capture: %s",
+                                                     cudaGetErrorString(e));
+        if (status == FMF_OK && tc) {
+            unsigned *err = nullptr;
+            if ((status = device_error_word(&err)) == FMF_OK) {
+                for (size_t i0 = 0; i0 < n && status == FMF_OK; i0 += TC_MAX_PROBS) {
+                    unsigned long long *queue;
+                    if ((status = ws.get(&queue, 1, "tile queue")))
+                        break;
+                    const int m = (int)(n - i0 < (size_t)TC_MAX_PROBS ? n - i0 : TC_MAX_PROBS);
+                    status = tc_run(reinterpret_cast<const TcProb *>(probs.data() + psz * i0), m, split,
+                                    queue, err, s);
+                }
+            }
+        }
+        // the branch scratch is freed after the work on s that reads it
+        if ((e = cudaEventRecord(b->ev_main, s)) == cudaSuccess)
+            for (int k = 0; k < kBatchBranches && e == cudaSuccess; k++)
+                e = cudaStreamWaitEvent(b->branch[k], b->ev_main, 0);
+        if (e != cudaSuccess && status == FMF_OK)
+            status = set_error(FMF_ERR_CUDA, "ordering the batch scratch: %s", cudaGetErrorString(e));
+    }  // branch scratch freed here, on the branch streams
+    // rejoin the branches before the capture ends
+    for (int k = 0; k < kBatchBranches; k++)
+        if ((e = cudaEventRecord(b->ev_rejoin[k], b->branch[k])) != cudaSuccess ||
+            (e = cudaStreamWaitEvent(s, b->ev_rejoin[k], 0)) != cudaSuccess)
+            status = status ? status : set_error(FMF_ERR_CUDA, "joining the batch capture: %s",
+                                                 cudaGetErrorString(e));
+    rc = status;
+    return rc;
 }
 
 static void batch_reset_graph(fmf_batch *b)
@@ -105,6 +151,17 @@ int fmf_batch_create(fmf_batch **out, int precision)
         e = cudaEventCreateWithFlags(&b->ev_in, cudaEventDisableTiming);
     if (e == cudaSuccess)
         e = cudaEventCreateWithFlags(&b->ev_out, cudaEventDisableTiming);
+    if (e == cudaSuccess)
+        e = cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming);
+    if (e == cudaSuccess)
+        e = cudaEventCreateWithFlags(&b->ev_main, cudaEventDisableTiming);
+    for (int k = 0; k < fmf::kBatchBranches && e == cudaSuccess; k++) {
+        e = cudaStreamCreateWithFlags(&b->branch[k], cudaStreamNonBlocking);
+        if (e == cudaSuccess)
+            e = cudaEventCreateWithFlags(&b->ev_join[k], cudaEventDisableTiming);
+        if (e == cudaSuccess)
+            e = cudaEventCreateWithFlags(&b->ev_rejoin[k], cudaEventDisableTiming);
+    }
     if (e != cudaSuccess) {
         fmf_batch_destroy(b);
         return fmf::set_error(FMF_ERR_CUDA, "creating a batch: %s", cudaGetErrorString(e));
@@ -227,6 +284,18 @@ int fmf_batch_destroy(fmf_batch *b)
         cudaEventDestroy(b->ev_in);
     if (b->ev_out)
         cudaEventDestroy(b->ev_out);
+    if (b->ev_fork)
+        cudaEventDestroy(b->ev_fork);
+    if (b->ev_main)
+        cudaEventDestroy(b->ev_main);
+    for (int k = 0; k < fmf::kBatchBranches; k++) {
+        if (b->ev_join[k])
+            cudaEventDestroy(b->ev_join[k]);
+        if (b->ev_rejoin[k])
+            cudaEventDestroy(b->ev_rejoin[k]);
+        if (b->branch[k])
+            cudaStreamDestroy(b->branch[k]);
+    }
     if (b->stream)
         cudaStreamDestroy(b->stream);
     delete b;
