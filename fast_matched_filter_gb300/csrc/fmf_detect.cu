@@ -288,15 +288,25 @@ det_count_kernel(const float *__restrict__ cc, size_t ld, DetState *__restrict__
     }
     const float4 *vrow = reinterpret_cast<const float4 *>(row + rs.head);
     const long long steps = (rs.nvec + 127) / 128;  // 128 float4s per warp step
-    for (long long c = (long long)blockIdx.x * kWarps + warp; c < steps; c += (long long)gridDim.x * kWarps) {
+    const long long cstride = (long long)gridDim.x * kWarps;
+    auto load4 = [&](long long c, float4 (&v)[4]) {
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            const long long i = c * 128 + u * 32 + lane;
+            v[u] = (c < steps && i < rs.nvec) ? vrow[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+    };
+    float4 nv[4];
+    long long c = (long long)blockIdx.x * kWarps + warp;
+    load4(c, nv);
+    for (; c < steps; c += cstride) {
         unsigned key[kK];
         bool ok[kK];
         float4 v[4];
 #pragma unroll
-        for (int u = 0; u < 4; u++) {
-            const long long i = c * 128 + u * 32 + lane;
-            v[u] = i < rs.nvec ? vrow[i] : make_float4(0.f, 0.f, 0.f, 0.f);
-        }
+        for (int u = 0; u < 4; u++)
+            v[u] = nv[u];
+        load4(c + cstride, nv);  // the next step's values are in flight while this one is counted
 #pragma unroll
         for (int u = 0; u < 4; u++) {
             const bool okv = c * 128 + u * 32 + lane < rs.nvec;
