@@ -1,7 +1,8 @@
 """Benchmark of the matched-filter hot path on GB300.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload config4|config1|config2|config0] [--precision ...]
+                    [--workload config4|config1|config2|config0|config3|variable]
+                    [--precision ...]
 
 One *step* is one complete search of the workload (every template against
 every channel and output index: preprocessing kernels + correlation
@@ -83,14 +84,19 @@ def make_workload(name, rank=0, templates=0, samples=0):
     if samples:
         kw["n_samples"] = samples
     gen = {"config0": synthetic.config0, "config1": synthetic.config1,
-           "config2": synthetic.config2, "config4": synthetic.config4}[name]
+           "config2": synthetic.config2, "config4": synthetic.config4,
+           "variable": synthetic.variable}[name]
     if name == "config0":
         cfg = gen(seed=100 + 1000 * rank)
     else:
-        cfg = gen(seed={"config1": 101, "config2": 102, "config4": 104}[name] + 1000 * rank, **kw)
+        cfg = gen(seed={"config1": 101, "config2": 102, "config4": 104, "variable": 105}[name]
+                  + 1000 * rank, **kw)
     tp = cfg["templates"]
     cfg["sst"] = np.sum(tp ** 2, axis=-1).astype(np.float32)
     cfg["macs"] = synthetic.macs(tp.shape, cfg["data"].shape[-1], cfg["step"])
+    if "n_samples_template" in cfg:
+        cfg["macs"] = synthetic.variable_macs(cfg["n_samples_template"], cfg["data"].shape[-1],
+                                              cfg["step"])
     cfg["n_corr"] = (cfg["data"].shape[-1] - tp.shape[-1]) // cfg["step"] + 1
     return cfg
 
@@ -203,6 +209,12 @@ def cpu_sample(cfg, n_templates=1):
     sub["weights"] = cfg["weights"][:n_templates]
     from fast_matched_filter_gb300 import synthetic
     sub["macs"] = synthetic.macs(sub["templates"].shape, cfg["data"].shape[-1], cfg["step"])
+    if "n_samples_template" in cfg:
+        nt = cfg["n_samples_template"][:n_templates]
+        sub["n_samples_template"] = nt
+        # the sample keeps the full template axis, so its lag range is the search's
+        n_corr = cfg["n_corr"]
+        sub["macs"] = int(n_corr) * int(nt.astype(np.int64).sum())
     return sub
 
 
@@ -210,8 +222,13 @@ def run_cpu_once(sub, threads):
     from oracle import cpu
     arch = "cpu" if sub["normalize"] == "short" else "precise"
     t0 = time.perf_counter()
-    cpu.run_oracle(sub["templates"], sub["moveouts"], sub["weights"], sub["data"], sub["step"],
-                   arch, sub["normalize"], sub["network_sum"], n_threads=threads)
+    if "n_samples_template" in sub:
+        cpu.run_oracle_variable(sub["templates"], sub["n_samples_template"], sub["moveouts"],
+                                sub["weights"], sub["data"], sub["step"], sub["normalize"],
+                                n_threads=threads)
+    else:
+        cpu.run_oracle(sub["templates"], sub["moveouts"], sub["weights"], sub["data"],
+                       sub["step"], arch, sub["normalize"], sub["network_sum"], n_threads=threads)
     return time.perf_counter() - t0
 
 
@@ -224,6 +241,8 @@ def cpu_baseline(cfg, reps=1):
     threads = os.cpu_count() or 1
     sub = cpu_sample(cfg)
     kind = "reference" if cpu.reference_available() else "port"
+    if "n_samples_template" in sub:
+        kind = "port"  # the timed run below uses the oracle for this arch too
     if kind == "reference":
         os.environ["OMP_NUM_THREADS"] = str(threads)
         arch = "cpu" if sub["normalize"] == "short" else "precise"
@@ -639,6 +658,91 @@ def run_e2e_detect(cfg, precision, args, world, lib):
                    "threshold + peaks, rows kept on the device)"}
 
 
+def run_variable(args):
+    """Per-channel template lengths (Fisher-z network sum) through
+    fmf_matched_filter_variable_ex: device-resident inputs (value) and host
+    inputs (e2e).  MACs count each channel's own length."""
+    import ctypes as ct
+    import torch
+    from fast_matched_filter_gb300 import _lib
+    torch.cuda.set_device(0)
+    lib = _lib.load()
+    cfg = make_workload("variable", 0, args.templates, args.samples)
+    T, S, C, L = cfg["templates"].shape
+    N = cfg["data"].shape[-1]
+    n_corr = cfg["n_corr"]
+    nt = np.ascontiguousarray(cfg["n_samples_template"], dtype=np.int32)
+    host = {k: np.ascontiguousarray(cfg[k]) for k in ("templates", "sst", "moveouts", "weights",
+                                                      "data")}
+    dev = {k: torch.from_numpy(v).cuda() for k, v in host.items()}
+    dnt = torch.from_numpy(nt).cuda()
+    out = torch.empty((T, n_corr), dtype=torch.float32, device="cuda")
+    stream = torch.cuda.current_stream()
+
+    def call():
+        st = lib.fmf_matched_filter_variable_ex(
+            dev["templates"].data_ptr(), dev["sst"].data_ptr(), dev["moveouts"].data_ptr(),
+            dev["data"].data_ptr(), dev["weights"].data_ptr(), cfg["step"], dnt.data_ptr(), N, T,
+            S, C, n_corr, out.data_ptr(), 0, _lib.FLAG_DEVICE_POINTERS, stream.cuda_stream)
+        _lib.check(st, lib)
+        return lib.fmf_last_launch_count()
+
+    for _ in range(max(args.warmup, 0)):
+        call()
+    torch.cuda.synchronize()
+    launches = 0
+    with ClockSampler(0) as clocks:
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            launches += call()
+        e1.record(stream)
+        torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    _lib.check(lib.fmf_device_errors(), lib)
+    value = cfg["macs"] / (ms / 1e3) / 1e12
+    peaks, kind = load_peaks()
+    fma_peak = N_SM * 128 * 2 * peaks.get("sm_max_mhz", 2070.0) * 1e6 / 1e12  # TFLOP/s
+    executed = T * n_corr * S * C * L  # the kernel runs every channel over the padded length
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": describe(cfg, {"precision": "fp32", "template_lengths": "400-800 per channel",
+                                     "parallelism": "single GPU"}),
+            "roofline": {"bound": "fp32_fma", "achieved": 2 * cfg["macs"] / (ms / 1e3) / 1e12,
+                         "peak": fma_peak, "unit": "TFLOP/s",
+                         "frac": 2 * cfg["macs"] / (ms / 1e3) / 1e12 / fma_peak,
+                         "executed_frac": 2 * executed / (ms / 1e3) / 1e12 / fma_peak,
+                         "traffic": None, "kernel": "plain_kernel (per-channel lengths)",
+                         "peak_source": "nominal FP32 FMA rate: 152 SMs x 128 lanes x max SM clock; "
+                                        "no measured FP32 peak exists"},
+            "gpu_launches": launches, "clocks": clocks.summary()}
+    # end to end: host inputs, synchronous entry point (inputs copied in, cc copied out)
+    cc = np.zeros((T, n_corr), dtype=np.float32)
+
+    def call_host():
+        st = lib.fmf_matched_filter_variable_ex(
+            host["templates"].ctypes.data, host["sst"].ctypes.data, host["moveouts"].ctypes.data,
+            host["data"].ctypes.data, host["weights"].ctypes.data, cfg["step"], nt.ctypes.data, N,
+            T, S, C, n_corr, cc.ctypes.data, 0, 0, None)
+        _lib.check(st, lib)
+
+    call_host()
+    n = max(1, min(args.steps, 3))
+    t0 = time.perf_counter()
+    for _ in range(n):
+        call_host()
+    secs = (time.perf_counter() - t0) / n
+    line["e2e"] = {"value": cfg["macs"] / secs / 1e12, "unit": UNIT,
+                   "h2d_bytes_per_step": int(sum(v.nbytes for v in host.values()) + nt.nbytes),
+                   "d2h_bytes_per_step": int(cc.nbytes), "steps": n,
+                   "api": "fmf_matched_filter_variable_ex (C ABI, host pointers)"}
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(cfg)
+    print(json.dumps(line))
+    return 0
+
+
 def run_batch(args):
     """Batched uneven searches: one graph (preprocessing + persistent tile-queue
     launch) vs the same searches as sequential plain FP32 calls and as
@@ -717,6 +821,8 @@ def main(argv=None):
         return run_reference_arm(args)
     if args.workload == "config3":
         return run_batch(args)
+    if args.workload == "variable":
+        return run_variable(args)
     return run_ours(args)
 
 

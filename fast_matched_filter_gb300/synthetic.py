@@ -155,6 +155,36 @@ def config4(seed=104, n_templates=500, n_samples=4320000):
                 network_sum=True)
 
 
+def variable(seed=105, n_templates=100, n_samples=1080000):
+    """Per-channel template lengths (the reference's 'variable_precise'):
+    data (20, 3, 1,080,000) N(0,1); 100 Hann-tapered templates whose channels
+    keep U{400..800} samples (zero-padded to 800); moveouts U{0..1000}; uniform
+    weights; step 1, short; network sum (Fisher z)."""
+    rng = np.random.default_rng(seed)
+    S, C, N, T, L = 20, 3, n_samples, n_templates, 800
+    data = rng.standard_normal((S, C, N), dtype=np.float32)
+    nt = rng.integers(400, L + 1, (T, S, C)).astype(np.int32)
+    nt[0, 0, 0] = L  # the longest channel sets the template axis and n_corr
+    templates = np.zeros((T, S, C, L), dtype=np.float32)
+    for idx in np.ndindex(nt.shape):
+        n = int(nt[idx])
+        templates[idx][:n] = (rng.standard_normal(n) * np.hanning(n)).astype(np.float32)
+    moveouts = rng.integers(0, 1001, (T, S, C)).astype(np.int32)
+    _plant(rng, data, templates, moveouts, 1, 0.5)
+    weights = np.full((T, S, C), 1.0 / (S * C), dtype=np.float32)
+    return dict(name="variable_S20C3N%d_T%dL400-800" % (N, T), templates=templates,
+                moveouts=moveouts, weights=weights, data=data, step=1, normalize="short",
+                network_sum=True, n_samples_template=nt)
+
+
+def variable_macs(n_samples_template, n_samples, step):
+    """Multiply-accumulates of a per-channel-length search: n_corr times the
+    sum of every template's channel lengths."""
+    nt = np.asarray(n_samples_template)
+    n_corr = (n_samples - int(nt.max())) // step + 1
+    return int(n_corr) * int(nt.astype(np.int64).sum())
+
+
 def macs(templates_shape, n_samples, step):
     """Algorithmic multiply-accumulates of one search: T * n_corr * S * C * L."""
     T, S, C, L = templates_shape
