@@ -200,9 +200,17 @@ def barrier(world):
 
 
 # ---------------------------------------------------------------- CPU baseline
-def cpu_sample(cfg, n_templates=1):
+CPU_SAMPLE_MACS = 4e11  # about 15 s of the CPU algorithm on 16 cores
+
+
+def cpu_sample(cfg, n_templates=None):
     """Bounded sample of the workload for the CPU algorithm: the first
-    template(s) against the whole trace."""
+    template(s) against the whole trace -- as many as fit about 15 s of CPU
+    work (all of them for the small workloads)."""
+    if n_templates is None:
+        T = cfg["templates"].shape[0]
+        per = cfg["macs"] / T
+        n_templates = int(max(1, min(T, CPU_SAMPLE_MACS // max(per, 1.0))))
     sub = dict(cfg)
     sub["templates"] = cfg["templates"][:n_templates]
     sub["moveouts"] = cfg["moveouts"][:n_templates]
@@ -280,10 +288,12 @@ def run_reference_arm(args):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic", "impl": "reference",
-            "config": describe(cfg, {"sample": "first template x full trace per step"}),
+            "config": describe(cfg, {"sample": "first %d template(s) x full trace per step"
+                                               % sub["templates"].shape[0]}),
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                             "sample": "1 of %d templates x full trace, %.3g MAC per step"
-                                       % (cfg["templates"].shape[0], sub["macs"])},
+                             "sample": "%d of %d templates x full trace, %.3g MAC per step"
+                                       % (sub["templates"].shape[0], cfg["templates"].shape[0],
+                                          sub["macs"])},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
