@@ -402,7 +402,22 @@ static int run_streamed(const Args &d, float *host_out, cudaStream_t s)
     const size_t row = (size_t)P.n_corr * (P.network_sum ? 1 : P.SC);  // floats per template
     const size_t out_bytes = (size_t)P.T * row * sizeof(float);
     const int n_chunks = out_bytes < ((size_t)64 << 20) ? 1 : (P.T < 8 ? P.T : 8);
-    const int per = (P.T + n_chunks - 1) / n_chunks;
+    // Template chunks of tapering size (weights 8,8,8,8,4,2,1,1 of 40 when there
+    // are enough templates): each chunk's copy overlaps the next chunk's kernel,
+    // and the last copy, which nothing overlaps, is small.
+    int bounds[9];
+    {
+        static const int wts[8] = {8, 8, 8, 8, 4, 2, 1, 1};
+        const bool taper = n_chunks == 8 && P.T >= 40;
+        int acc = 0;
+        bounds[0] = 0;
+        for (int c = 0; c < n_chunks; c++) {
+            acc += taper ? wts[c] : 1;
+            const int total = taper ? 40 : n_chunks;
+            bounds[c + 1] = (int)(((long long)P.T * acc) / total);
+        }
+        bounds[n_chunks] = P.T;
+    }
     unsigned *err = nullptr;
     std::vector<unsigned char> tcfull;
     int split = 0;
@@ -437,9 +452,9 @@ static int run_streamed(const Args &d, float *host_out, cudaStream_t s)
         e = cudaEventCreateWithFlags(&ev[i], cudaEventDisableTiming);
     if (e == cudaSuccess) {
         for (int c = 0; c < n_chunks && rc == FMF_OK; c++) {
-            const int t0 = c * per, nt = P.T - t0 < per ? P.T - t0 : per;
+            const int t0 = bounds[c], nt = bounds[c + 1] - bounds[c];
             if (nt <= 0)
-                break;
+                continue;
             if (!tcfull.empty()) {
                 std::vector<unsigned char> sub(tc_prob_size());
                 unsigned long long *queue;
