@@ -713,7 +713,8 @@ def run_variable(args):
     value = cfg["macs"] / (ms / 1e3) / 1e12
     peaks, kind = load_peaks()
     fma_peak = N_SM * 128 * 2 * peaks.get("sm_max_mhz", 2070.0) * 1e6 / 1e12  # TFLOP/s
-    executed = T * n_corr * S * C * L  # the kernel runs every channel over the padded length
+    # the kernel runs each channel over its own taps rounded up to its 20-tap unroll
+    executed = int(n_corr) * int(((nt.astype(np.int64) + 19) // 20 * 20).sum())
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",

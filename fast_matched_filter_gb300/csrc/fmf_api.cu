@@ -12,6 +12,7 @@
 #include <cstring>
 #include <cstdlib>
 #include <climits>
+#include <mutex>
 #include <vector>
 
 #include "fmf_common.cuh"
@@ -118,6 +119,8 @@ int device_error_word(unsigned **out)
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess || dev < 0 || dev >= kMaxDevices)
         return set_error(FMF_ERR_CUDA, "no usable current device");
+    static std::mutex m;  // first calls from several host threads allocate once
+    std::lock_guard<std::mutex> lock(m);
     if (!g_err_word[dev]) {
         void *p = nullptr;
         if ((e = cudaMalloc(&p, 64)) != cudaSuccess || (e = cudaMemset(p, 0, 64)) != cudaSuccess) {

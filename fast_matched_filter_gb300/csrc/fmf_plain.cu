@@ -120,7 +120,9 @@ __device__ __forceinline__ void load_stage(float *buf, const Problem &P, const P
                 acc[r] = fmaf(tv[jj], win[(4 * s + r + jj) % PL_U], acc[r]);                   \
     }
 
-__device__ __forceinline__ void compute_phase(const float *buf, const PlainGeom &g, float acc[PL_R])
+// Taps [0, taps) of one phase (taps a multiple of PL_U, at most g.lq_pad).
+__device__ __forceinline__ void compute_phase(const float *buf, const PlainGeom &g, int taps,
+                                              float acc[PL_R])
 {
     const float *tb = buf + g.data_floats;
     const int x0 = threadIdx.x * PL_R;  // a multiple of 16: padx(x0 + y) = padx(x0) + padx(y)
@@ -136,7 +138,7 @@ __device__ __forceinline__ void compute_phase(const float *buf, const PlainGeom 
     }
     int q = 0;
     // blocks of 80 taps (a multiple of 16 and of PL_U): every padded offset is a constant
-    for (; q + 4 * PL_U <= g.lq_pad; q += 4 * PL_U) {
+    for (; q + 4 * PL_U <= taps; q += 4 * PL_U) {
         const float *d = db + padx(q);
         const float *tq = tb + q;
 #pragma unroll
@@ -147,7 +149,7 @@ __device__ __forceinline__ void compute_phase(const float *buf, const PlainGeom 
         }
     }
     // the remaining taps, PL_U at a time
-    for (; q < g.lq_pad; q += PL_U) {
+    for (; q < taps; q += PL_U) {
 #define PL_PADQ(y) (padx(q + (y)) - padx(q))
         const float *d = db + padx(q);
         PL_TAPS_BODY(d, tb + q, PL_PADQ)
@@ -195,7 +197,15 @@ plain_kernel(const Problem P, const PlainGeom g)
             cp_async_commit();
             cp_async_wait1();
             __syncthreads();
-            compute_phase(smem + b * g.stage_floats, g, acc);
+            // per-channel template lengths: the taps past the channel's own length are
+            // zeros, so the phase stops after its own taps (rounded up to PL_U)
+            int taps = g.lq_pad;
+            if (P.ntap) {
+                const int n = P.ntap[(size_t)t * P.SC + ch];
+                const int own = n > phi ? (n - phi + P.step - 1) / P.step : 0;
+                taps = min(g.lq_pad, (own + PL_U - 1) / PL_U * PL_U);
+            }
+            compute_phase(smem + b * g.stage_floats, g, taps, acc);
             if (phi == P.step - 1 && P.ntap) {
                 // per-channel template length: FP64 window sums of that length,
                 // the 'precise' threshold (on the square root, matched_filter.c:650-652)
