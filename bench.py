@@ -25,6 +25,7 @@ data (weak scaling); the only collectives are the barrier and the max of
 the per-rank times.
 """
 import argparse
+import contextlib
 import json
 import os
 import statistics
@@ -443,6 +444,8 @@ def tc_executed_macs(cfg, nb=None):
             continue
         busy = sum(1 for i in range(n_tiles) if i * tile < khi and (i + 1) * tile > klo)
         ksteps = 0
+        own = cfg.get("n_samples_template")
+        own = None if own is None else np.asarray(own).reshape(T, S * C)
         for ch in range(S * C):
             if w[t, ch] == 0:
                 continue
@@ -450,6 +453,9 @@ def tc_executed_macs(cfg, nb=None):
                 mu = (mo[t, ch] + phi) // step
                 s = mu % Q
                 lphi = (L - phi + step - 1) // step
+                if own is not None:  # the issuers stop at the channel's own length
+                    n = int(own[t, ch])
+                    lphi = min(lphi, (n - phi + step - 1) // step if n > phi else 0)
                 ksteps += (((s + lphi + Q - 1 + 15) & ~15) - (s & ~15)) // 16
         total += busy * ksteps * 16 * Q * nb
     return total, nb
@@ -671,12 +677,14 @@ def run_e2e_detect(cfg, precision, args, world, lib):
 def run_variable(args):
     """Per-channel template lengths (Fisher-z network sum) through
     fmf_matched_filter_variable_ex: device-resident inputs (value) and host
-    inputs (e2e).  MACs count each channel's own length."""
-    import ctypes as ct
+    inputs (e2e).  MACs count each channel's own length.  --precision auto
+    runs the tensor-core numerators (split bf16), with the plain FP32 form
+    timed beside them."""
     import torch
     from fast_matched_filter_gb300 import _lib
     torch.cuda.set_device(0)
     lib = _lib.load()
+    precision = "split_bf16" if args.precision == "auto" else args.precision
     cfg = make_workload("variable", 0, args.templates, args.samples)
     T, S, C, L = cfg["templates"].shape
     N = cfg["data"].shape[-1]
@@ -689,45 +697,77 @@ def run_variable(args):
     out = torch.empty((T, n_corr), dtype=torch.float32, device="cuda")
     stream = torch.cuda.current_stream()
 
-    def call():
-        st = lib.fmf_matched_filter_variable_ex(
-            dev["templates"].data_ptr(), dev["sst"].data_ptr(), dev["moveouts"].data_ptr(),
-            dev["data"].data_ptr(), dev["weights"].data_ptr(), cfg["step"], dnt.data_ptr(), N, T,
-            S, C, n_corr, out.data_ptr(), 0, _lib.FLAG_DEVICE_POINTERS, stream.cuda_stream)
-        _lib.check(st, lib)
-        return lib.fmf_last_launch_count()
+    def timed(prec, steps, warmup, sample_clocks):
+        flags = _lib.FLAG_DEVICE_POINTERS | _lib.flag_precision(prec)
 
-    for _ in range(max(args.warmup, 0)):
-        call()
-    torch.cuda.synchronize()
-    launches = 0
-    with ClockSampler(0) as clocks:
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        for _ in range(args.steps):
-            launches += call()
-        e1.record(stream)
+        def call():
+            st = lib.fmf_matched_filter_variable_ex(
+                dev["templates"].data_ptr(), dev["sst"].data_ptr(), dev["moveouts"].data_ptr(),
+                dev["data"].data_ptr(), dev["weights"].data_ptr(), cfg["step"], dnt.data_ptr(), N,
+                T, S, C, n_corr, out.data_ptr(), 0, flags, stream.cuda_stream)
+            _lib.check(st, lib)
+            return lib.fmf_last_launch_count()
+
+        for _ in range(max(warmup, 0)):
+            call()
         torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1) / args.steps
-    _lib.check(lib.fmf_device_errors(), lib)
-    value = cfg["macs"] / (ms / 1e3) / 1e12
+        launches = 0
+        sampler = ClockSampler(0) if sample_clocks else contextlib.nullcontext()
+        with sampler as clocks:
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(steps):
+                launches += call()
+            e1.record(stream)
+            torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / steps
+        _lib.check(lib.fmf_device_errors(), lib)
+        return ms, launches, (clocks.summary() if sample_clocks else None)
+
     peaks, kind = load_peaks()
     fma_peak = N_SM * 128 * 2 * peaks.get("sm_max_mhz", 2070.0) * 1e6 / 1e12  # TFLOP/s
-    # the kernel runs each channel over its own taps rounded up to its 20-tap unroll
-    executed = int(n_corr) * int(((nt.astype(np.int64) + 19) // 20 * 20).sum())
+
+    def plain_roofline(ms):
+        # the kernel runs each channel over its own taps rounded up to its 20-tap unroll
+        executed = int(n_corr) * int(((nt.astype(np.int64) + 19) // 20 * 20).sum())
+        achieved = 2 * cfg["macs"] / (ms / 1e3) / 1e12
+        return {"bound": "fp32_fma", "achieved": achieved, "peak": fma_peak, "unit": "TFLOP/s",
+                "frac": achieved / fma_peak,
+                "executed_frac": 2 * executed / (ms / 1e3) / 1e12 / fma_peak,
+                "traffic": None, "kernel": "plain_kernel (per-channel lengths)",
+                "peak_source": "nominal FP32 FMA rate: 152 SMs x 128 lanes x max SM clock; "
+                               "no measured FP32 peak exists"}
+
+    def tc_roofline(ms):
+        peak = peaks.get("bf16_tflops_sustained", FALLBACK_PEAKS["bf16_tflops_sustained"])
+        achieved = 2 * cfg["macs"] / (ms / 1e3) / 1e12
+        executed, nb = tc_executed_macs(cfg)
+        n_prod = 3 if precision == "split_bf16" else 1
+        ex = 2 * executed * n_prod / (ms / 1e3) / 1e12
+        return {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                "frac": achieved / peak, "traffic": None,
+                "kernel": "tc_persistent (nb=%d, per-channel K ranges)" % nb,
+                "peak_source": "%s bf16_tflops_sustained (cuBLAS bf16 GEMM, seconds-long loop)" % kind,
+                "executed_tflops": ex, "executed_frac": ex / peak,
+                "executed_over_algorithmic": executed * n_prod / cfg["macs"]}
+
+    ms, launches, clocks = timed(precision, args.steps, args.warmup, True)
+    value = cfg["macs"] / (ms / 1e3) / 1e12
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": describe(cfg, {"precision": "fp32", "template_lengths": "400-800 per channel",
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": {"fp32": "f32", "split_bf16": "bf16x3", "bf16": "bf16"}[precision],
+            "data": "synthetic",
+            "config": describe(cfg, {"precision": precision,
+                                     "template_lengths": "400-800 per channel",
                                      "parallelism": "single GPU"}),
-            "roofline": {"bound": "fp32_fma", "achieved": 2 * cfg["macs"] / (ms / 1e3) / 1e12,
-                         "peak": fma_peak, "unit": "TFLOP/s",
-                         "frac": 2 * cfg["macs"] / (ms / 1e3) / 1e12 / fma_peak,
-                         "executed_frac": 2 * executed / (ms / 1e3) / 1e12 / fma_peak,
-                         "traffic": None, "kernel": "plain_kernel (per-channel lengths)",
-                         "peak_source": "nominal FP32 FMA rate: 152 SMs x 128 lanes x max SM clock; "
-                                        "no measured FP32 peak exists"},
-            "gpu_launches": launches, "clocks": clocks.summary()}
+            "roofline": plain_roofline(ms) if precision == "fp32" else tc_roofline(ms),
+            "gpu_launches": launches, "clocks": clocks}
+    if precision != "fp32" and not args.no_compare:
+        pms, _, _ = timed("fp32", max(1, min(args.steps, 2)), 1, False)
+        pv = cfg["macs"] / (pms / 1e3) / 1e12
+        line["plain_fp32"] = {"value": pv, "unit": UNIT, "ms_per_step": pms,
+                              "speedup_of_headline": value / pv, "roofline": plain_roofline(pms)}
     # end to end: host inputs, synchronous entry point (inputs copied in, cc copied out)
     cc = np.zeros((T, n_corr), dtype=np.float32)
 
@@ -735,7 +775,7 @@ def run_variable(args):
         st = lib.fmf_matched_filter_variable_ex(
             host["templates"].ctypes.data, host["sst"].ctypes.data, host["moveouts"].ctypes.data,
             host["data"].ctypes.data, host["weights"].ctypes.data, cfg["step"], nt.ctypes.data, N,
-            T, S, C, n_corr, cc.ctypes.data, 0, 0, None)
+            T, S, C, n_corr, cc.ctypes.data, 0, _lib.flag_precision(precision), None)
         _lib.check(st, lib)
 
     call_host()

@@ -39,6 +39,11 @@ def flag_template_group(n):
     """FMF_FLAG_TEMPLATE_GROUP: templates interleaved per group of tile-queue items."""
     return (int(n) & 0xFF) << 16
 
+
+def flag_precision(precision):
+    """FMF_FLAG_PRECISION: numerator precision of fmf_matched_filter_variable_ex."""
+    return (PRECISIONS[precision] & 3) << 24
+
 _fp = ct.POINTER(ct.c_float)
 _ip = ct.POINTER(ct.c_int)
 _sz = ct.c_size_t

@@ -134,7 +134,7 @@ int device_error_word(unsigned **out)
 }
 
 // Reads and clears the error word after the device has finished the work.
-static int collect_device_errors()
+int collect_device_errors()
 {
     unsigned *w = nullptr;
     int rc = device_error_word(&w);

@@ -47,6 +47,8 @@
 //               TMEM (channel order, fused multiply-add), outputs.
 // Every wait is bounded (globaltimer); on timeout the CTA raises an error
 // word, stops issuing, waits for its own copies/MMAs (bounded) and frees TMEM.
+#include <cfloat>
+
 #include <cuda_bf16.h>
 
 #include "fmf_common.cuh"
@@ -585,7 +587,12 @@ __global__ void __launch_bounds__(TC_THREADS, 1) tc_persistent(const __grid_cons
                         const long long meta = ((long long)t * SC + ch) * step + phi;
                         const int mu = pr.mu[meta];
                         const int sres = ((mu % TC_Q) + TC_Q) % TC_Q;
-                        const int lphi = (P.L - phi + step - 1) / step;
+                        int lphi = (P.L - phi + step - 1) / step;
+                        if (P.ntap) {  // per-channel length: the taps past it are zeros, skip them
+                            const int n = P.ntap[(size_t)t * SC + ch];
+                            const int own = n > phi ? (n - phi + step - 1) / step : 0;
+                            lphi = min(lphi, own);
+                        }
                         const int k_first = sres & ~15;
                         const int k_end = (sres + lphi + TC_Q - 1 + 15) & ~15;
                         const uint32_t zhi = smem_u32(smem + (size_t)s * B.stage_bytes);
@@ -660,6 +667,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1) tc_persistent(const __grid_cons
             const uint32_t s_cols = lane_base + (uint32_t)(TC_NACC * TC_NB_MAX + a0);
             const int SC = pr.P.SC, step = pr.P.step, n_corr = pr.P.n_corr, N = pr.P.N;
             const bool full = pr.P.normalize != 0, nsum = pr.P.network_sum != 0;
+            // per-channel template lengths: FP64 prefix sums and a Fisher-z network sum
+            const bool var = pr.P.ntap != nullptr;
             const float *__restrict__ stat_e = pr.P.stat_e;
             const float *__restrict__ stat_m = pr.P.stat_m;
             const float *__restrict__ sstp = pr.P.sst;
@@ -674,7 +683,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) tc_persistent(const __grid_cons
             const int a_hi = (int)min((long long)nb, (khi - kb + TC_Q - 1) / TC_Q) - a0;
             const bool any = busy && a_hi > a_lo;
             // the whole warp's outputs of this item are valid (the usual case)
-            const bool interior = __all_sync(0xffffffffu, a_lo <= 0 && a_hi >= NC);
+            const bool interior = __all_sync(0xffffffffu, a_lo <= 0 && a_hi >= NC) && !var;
             const long long qs = (long long)TC_Q * step;
             const float *w = pr.P.w + (size_t)t * SC;
             const int *mo = pr.P.mo + (size_t)t * SC;
@@ -688,8 +697,14 @@ __global__ void __launch_bounds__(TC_THREADS, 1) tc_persistent(const __grid_cons
                 const float sst = sstp[row];
                 const float ts = full ? tsump[row] : 0.0f;
                 const long long u0 = (kb + (long long)TC_Q * a0) * step + mo[ch];
-                const float *__restrict__ se = stat_e + (size_t)ch * N + u0;
-                const float *__restrict__ sm = full ? stat_m + (size_t)ch * N + u0 : se;
+                const float *__restrict__ se = var ? nullptr : stat_e + (size_t)ch * N + u0;
+                const float *__restrict__ sm = (full && !var) ? stat_m + (size_t)ch * N + u0 : se;
+                const int ntap = var ? pr.P.ntap[row] : 0;
+                const float zw = var ? pr.P.zweight[row] : 0.0f;
+                const double *__restrict__ p2 = var ? pr.P.pre2 + (size_t)ch * (N + 1) + u0 : nullptr;
+                const double *__restrict__ p1 =
+                    (var && full) ? pr.P.pre1 + (size_t)ch * (N + 1) + u0 : nullptr;
+                const double inv_n = var ? 1.0 / (double)ntap : 0.0;
                 float *oc = outp + ((size_t)t * n_corr + kb + (long long)TC_Q * a0) * SC + ch;
                 // statistics: all loads of a chunk issued together (indices clamped into the
                 // valid range) before any use; the first chunk before waiting for the accumulator
@@ -698,8 +713,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1) tc_persistent(const __grid_cons
 #pragma unroll
                     for (int i = 0; i < CH; i++) {
                         const int ac = min(max(c0 + i, a_lo), a_hi - 1);
-                        e[i] = any ? __ldg(se + ac * qs) : 0.0f;
-                        mm[i] = (any && full) ? __ldg(sm + ac * qs) : 0.0f;
+                        e[i] = (any && !var) ? __ldg(se + ac * qs) : 0.0f;
+                        mm[i] = (any && full && !var) ? __ldg(sm + ac * qs) : 0.0f;
                     }
                 };
                 load_chunk(0);
@@ -722,7 +737,60 @@ __global__ void __launch_bounds__(TC_THREADS, 1) tc_persistent(const __grid_cons
                         if (lane == 0)
                             mbar_arrive(dempty0 + 8 * d);
                     }
-                    if (nsum && interior) {
+                    if (var) {
+                        // window sums of the channel's own length from the FP64 prefix sums,
+                        // the 'precise' threshold on the square root, and
+                        // atanh(cc - 10 eps) * z into the network sum
+                        auto var_value = [&](int i, double s2, double s1) {
+                            const int a = c0 + i;
+                            float num = x[i], ssd;
+                            if (full) {
+                                const double v = s2 - s1 * s1 * inv_n;
+                                num = fmaf(-(float)(s1 * inv_n), ts, num);
+                                ssd = (float)(v > 0.0 ? v : 0.0);
+                            } else {
+                                ssd = (float)s2;
+                            }
+                            const float den = sqrtf(sst * ssd);
+                            const float cc = den > kThreshold ? num / den : 0.0f;
+                            const float prev = first ? 0.0f : sv[i];
+                            sv[i] = (a >= a_lo && a < a_hi)
+                                        ? fmaf(atanhf(cc - 10.0f * FLT_EPSILON), zw, prev)
+                                        : prev;
+                        };
+                        auto off = [&](int i) {
+                            return (long long)min(max(c0 + i, a_lo), a_hi - 1) * qs;
+                        };
+                        if (!full) {
+#pragma unroll
+                            for (int h = 0; h < CH; h += 4) {  // loads of 4 values, then their use
+                                double lo[4], hi[4];
+#pragma unroll
+                                for (int j = 0; j < 4; j++) {
+                                    lo[j] = any ? p2[off(h + j)] : 0.0;
+                                    hi[j] = any ? p2[off(h + j) + ntap] : 0.0;
+                                }
+#pragma unroll
+                                for (int j = 0; j < 4; j++)
+                                    var_value(h + j, hi[j] - lo[j], 0.0);
+                            }
+                        } else {
+#pragma unroll
+                            for (int h = 0; h < CH; h += 2) {
+                                double lo2[2], hi2[2], lo1[2], hi1[2];
+#pragma unroll
+                                for (int j = 0; j < 2; j++) {
+                                    lo2[j] = any ? p2[off(h + j)] : 0.0;
+                                    hi2[j] = any ? p2[off(h + j) + ntap] : 0.0;
+                                    lo1[j] = any ? p1[off(h + j)] : 0.0;
+                                    hi1[j] = any ? p1[off(h + j) + ntap] : 0.0;
+                                }
+#pragma unroll
+                                for (int j = 0; j < 2; j++)
+                                    var_value(h + j, hi2[j] - lo2[j], hi1[j] - lo1[j]);
+                            }
+                        }
+                    } else if (nsum && interior) {
                         // every output of the warp is valid: no per-value range test
                         if (first) {
 #pragma unroll

@@ -17,8 +17,10 @@
 //
 // Kernels: metadata (one thread, the reference's float accumulation order),
 // masked/centred templates, FP64 prefix sums of d^2 and d (global, so that
-// any window length is two subtractions), the plain FP32 kernel with its
-// variable-length epilogue (fmf_plain.cu), and the final transform.
+// any window length is two subtractions), the numerator kernel with its
+// variable-length epilogue -- the plain FP32 kernel (fmf_plain.cu) or the
+// tensor-core kernel (fmf_tc.cu), whose issuers stop each channel's K range
+// at its own length -- and the final transform.
 #include <cfloat>
 #include <climits>
 #include <cmath>
@@ -29,7 +31,9 @@
 namespace fmf {
 
 __global__ void channel_mean_kernel(const float *, int, float *);
-int device_error_word(unsigned **out);
+int launch_tc(const Problem &P, const float *data_for_tc, int precision, unsigned *err, Scratch &ws,
+              cudaStream_t s, int forced_nb, int template_group);
+int collect_device_errors();
 
 // One thread: lag range, Fisher-z weights and the transform constants of
 // every template, in the reference's order of float operations.
@@ -340,8 +344,18 @@ static int variable_device(const VArgs &a, int L, cudaStream_t s)
     P.pre2 = pre2;
     P.pre1 = pre1;
     P.zweight = zweight;
-    if ((rc = launch_plain_all(P, s)))
+    const int precision = FMF_FLAG_PRECISION_OF(a.flags);
+    if (precision != FMF_PREC_FP32) {
+        unsigned *err = nullptr;
+        const int forced = ((a.flags >> 8) & 0xff) * 16;
+        if (forced != 0 && forced != 32 && forced != 64 && forced != 128)
+            return set_error(FMF_ERR_ARG, "tensor-core tile of %d lag blocks (32, 64 or 128)", forced);
+        if ((rc = device_error_word(&err)) ||
+            (rc = launch_tc(P, P.data, precision, err, ws, s, forced, (a.flags >> 16) & 0xff)))
+            return rc;
+    } else if ((rc = launch_plain_all(P, s))) {
         return rc;
+    }
     const long long n = (long long)T * a.n_corr;
     vp_finalize_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(a.out, T, (int)a.n_corr, norm_sum, bias,
                                                                    scale);
@@ -361,6 +375,9 @@ static int variable_entry(const VArgs &a, void *stream)
         return set_error(FMF_ERR_ARG, "sizes exceed the 32-bit index range of this build");
     if (a.normalize != 0 && a.normalize != 1)
         return set_error(FMF_ERR_ARG, "normalize must be 0 or 1");
+    const int precision = FMF_FLAG_PRECISION_OF(a.flags);
+    if (precision != FMF_PREC_FP32 && precision != FMF_PREC_SPLIT_BF16 && precision != FMF_PREC_BF16)
+        return set_error(FMF_ERR_ARG, "unknown precision %d", precision);
     cudaGetLastError();
     cudaStream_t s = (cudaStream_t)stream;
     const size_t n_meta = a.T * a.S * a.C;
@@ -424,7 +441,7 @@ static int variable_entry(const VArgs &a, void *stream)
     cudaError_t e = cudaStreamSynchronize(s);
     if (e != cudaSuccess)
         return set_error(FMF_ERR_CUDA, "variable-length search: %s", cudaGetErrorString(e));
-    return FMF_OK;
+    return precision != FMF_PREC_FP32 ? collect_device_errors() : FMF_OK;
 }
 
 }  // namespace fmf

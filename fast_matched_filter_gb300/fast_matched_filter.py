@@ -202,7 +202,7 @@ def matched_filter(templates, moveouts, weights, data, step,
             return None
         return _matched_filter_variable(templates, moveouts, weights, data, step,
                                         n_samples_template, check_zeros, normalize,
-                                        network_sum)
+                                        network_sum, precision)
     if arch.lower() != "gpu":
         print("Compiled library for {} not loaded; exiting!".format(arch))
         return None
@@ -244,9 +244,12 @@ def matched_filter(templates, moveouts, weights, data, step,
 
 
 def _matched_filter_variable(templates, moveouts, weights, data, step, n_samples_template,
-                             check_zeros, normalize, network_sum):
+                             check_zeros, normalize, network_sum, precision="fp32"):
     """Per-channel template lengths (the reference's arch 'variable_precise',
-    fast_matched_filter.py:216-229, 307-313) on the GPU library."""
+    fast_matched_filter.py:216-229, 307-313) on the GPU library; ``precision``
+    selects the plain FP32 or the tensor-core numerators."""
+    if precision not in _lib.PRECISIONS:
+        raise ValueError("precision must be one of %s" % sorted(_lib.PRECISIONS))
     if n_samples_template is None:
         raise ValueError("arch='variable_precise' needs n_samples_template")
     if not network_sum:
@@ -268,7 +271,8 @@ def _matched_filter_variable(templates, moveouts, weights, data, step, n_samples
     st = lib.fmf_matched_filter_variable_ex(
         pp["templates"].ctypes.data, pp["sst"].ctypes.data, pp["moveouts"].ctypes.data,
         pp["data"].ctypes.data, pp["weights"].ctypes.data, pp["step"], nt.ctypes.data,
-        pp["N"], T, S, C, n_corr, cc.ctypes.data, pp["normalize"], 0, None)
+        pp["N"], T, S, C, n_corr, cc.ctypes.data, pp["normalize"], _lib.flag_precision(precision),
+        None)
     _lib.check(st, lib)
     cc = cc.reshape(T, n_corr)
     _zero_report(cc, pp["moveouts"], pp["weights"], T, n_corr, pp["step"], True, check_zeros)

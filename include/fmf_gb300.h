@@ -61,6 +61,10 @@ extern "C" {
 #define FMF_FLAG_TILE(lag_blocks) ((((lag_blocks) / 16) & 0xff) << 8)
 /* tensor-core tile queue: templates interleaved per group of items (1..255; default 16) */
 #define FMF_FLAG_TEMPLATE_GROUP(n) (((n) & 0xff) << 16)
+/* numerator precision (FMF_PREC_*) of the entry points without a precision
+ * argument (fmf_matched_filter_variable_ex); default FMF_PREC_FP32 */
+#define FMF_FLAG_PRECISION(p) (((p) & 3) << 24)
+#define FMF_FLAG_PRECISION_OF(flags) (((flags) >> 24) & 3)
 
 /*
  * Drop-in for the reference GPU entry point
@@ -187,7 +191,8 @@ FMF_API int fmf_batch_destroy(fmf_batch *batch);
  * the reference's CPU-only matched_filter_variable_precise
  * (fast_matched_filter/src/matched_filter_CPU.h, matched_filter.c:321-325,
  * called from fast_matched_filter.py:307-309), run on the GPU (plain FP32
- * form).  n_samples_template (T, S, C) gives each channel's length; templates
+ * form; the tensor-core form through the flags of the _ex entry point).
+ * n_samples_template (T, S, C) gives each channel's length; templates
  * are (T, S, C, max length), zero-padded; cc_sum is (T, n_corr) with
  * n_corr = (N - max length) / step + 1.  Host pointers, synchronous.
  * Semantics, including the reference's template-cumulative scale, are those
@@ -199,7 +204,10 @@ FMF_API int fmf_matched_filter_variable(const float *templates, const float *sum
                                         size_t n_samples_data, size_t n_templates, size_t n_stations,
                                         size_t n_components, size_t n_corr, float *cc_sum,
                                         int normalize);
-/* Same, with flags (FMF_FLAG_DEVICE_POINTERS) and a stream. */
+/* Same, with flags and a stream: FMF_FLAG_DEVICE_POINTERS;
+ * FMF_FLAG_PRECISION(FMF_PREC_SPLIT_BF16 or FMF_PREC_BF16) runs the numerators
+ * on the tensor cores (each channel's K range cut at its own length),
+ * FMF_FLAG_TILE / FMF_FLAG_TEMPLATE_GROUP as for fmf_matched_filter_ex. */
 FMF_API int fmf_matched_filter_variable_ex(const float *templates, const float *sum_square_templates,
                                            const int *moveouts, const float *data, const float *weights,
                                            size_t step, const int *n_samples_template,

@@ -84,6 +84,27 @@ def test_unknown_precision_rejected(lib):
     assert st == _lib.FMF_ERR_ARG
 
 
+def test_precision_flag_matches_header():
+    src = open(HEADER).read()
+    m = re.search(r"#define FMF_FLAG_PRECISION\(p\) \(\(\(p\) & (\d+)\) << (\d+)\)", src)
+    assert m, "FMF_FLAG_PRECISION not found"
+    mask, shift = int(m.group(1)), int(m.group(2))
+    for name, code in _lib.PRECISIONS.items():
+        assert _lib.flag_precision(name) == (code & mask) << shift
+
+
+def test_variable_unknown_precision_rejected(lib):
+    args, keep = _args()
+    ex = [a if not hasattr(a, "contents") else ct.cast(a, ct.c_void_p).value for a in args]
+    nt = np.full((2, 2, 3), 16, np.int32)
+    # (templates, sst, moveouts, data, weights, step, n_samples_template, N, T, S, C, n_corr, cc,
+    #  normalize, flags, stream)
+    st = lib.fmf_matched_filter_variable_ex(ex[0], ex[1], ex[2], ex[3], ex[4], 1, nt.ctypes.data,
+                                            200, 2, 2, 3, 185, ex[12], 0, 3 << 24, None)
+    assert st == _lib.FMF_ERR_ARG
+    assert "precision" in _lib.last_error(lib)[1]
+
+
 def test_python_layer_raises_on_status(lib):
     with pytest.raises(_lib.FMFError) as e:
         _lib.check(_lib.FMF_ERR_ARG, lib)

@@ -14,25 +14,37 @@ from tests.test_gpu_parity import TOL
 pytestmark = pytest.mark.gpu
 
 
-def _check(got, ref, scale):
+# Tensor-core numerators (split bf16, FP32 accumulation) carry a relative error
+# of about 2^-16 per coefficient; the Fisher-z sum passes it through
+# atanh, whose slope 1 / (1 - cc^2) grows near |cc| = 1, so their bar is wider.
+TOL_TC = 1e-4
+
+
+def _check(got, ref, scale, tol=TOL):
     assert got.shape == ref.shape
     assert np.array_equal(np.isnan(got), np.isnan(ref))
     ok = ~np.isnan(ref)
     err = np.abs(got[ok].astype(np.float64) - ref[ok]).max()
-    assert err <= TOL * max(1.0, scale), "max |diff| %.3g" % err
+    assert err <= tol * max(1.0, scale), "max |diff| %.3g" % err
 
 
+def _tol(precision):
+    return TOL if precision == "fp32" else TOL_TC
+
+
+@pytest.mark.parametrize("precision", ["fp32", "split_bf16"])
 @pytest.mark.parametrize("name", golden_names_variable())
-def test_variable_golden(name):
+def test_variable_golden(name, precision):
     inputs, opts, expected = load_golden(name)
     got = fmf.matched_filter(check_zeros=False, arch="variable_precise",
-                             normalize=opts["normalize"], **inputs)
-    _check(got, expected.reshape(got.shape), float(np.sum(inputs["weights"])))
+                             normalize=opts["normalize"], precision=precision, **inputs)
+    _check(got, expected.reshape(got.shape), float(np.sum(inputs["weights"])), _tol(precision))
 
 
+@pytest.mark.parametrize("precision", ["fp32", "split_bf16"])
 @pytest.mark.parametrize("step", [1, 2, 3])
 @pytest.mark.parametrize("normalize", ["short", "full"])
-def test_variable_random_vs_oracle(oracle_built, step, normalize):
+def test_variable_random_vs_oracle(oracle_built, step, normalize, precision):
     rng = np.random.default_rng(60 + step)
     tp, mo, w, d = random_search(70 + step, 3, 3, 2, 160, 8000, -30, 200,
                                  dc=3.0 if normalize == "full" else 0.0, zero_weights=2)
@@ -41,9 +53,84 @@ def test_variable_random_vs_oracle(oracle_built, step, normalize):
     for idx in np.ndindex(nt.shape):
         tp[idx][nt[idx]:] = 0.0
     got = fmf.matched_filter(tp, mo, w, d, step, n_samples_template=nt, arch="gpu",
-                             check_zeros=False, normalize=normalize)
+                             check_zeros=False, normalize=normalize, precision=precision)
     ref = oracle_built.run_oracle_variable(tp, nt, mo, w, d, step, normalize)
-    _check(got, ref, float(np.sum(w)))
+    _check(got, ref, float(np.sum(w)), _tol(precision))
+
+
+def _bf16(x):
+    """Round float32 to bfloat16 (nearest, ties to even), kept as float64."""
+    u = np.asarray(x, np.float32).view(np.uint32).astype(np.uint64)
+    return (((u + 0x7FFF + ((u >> 16) & 1)) >> 16) << 16).astype(np.uint32).view(
+        np.float32).astype(np.float64)
+
+
+def _split_bf16_shift(tp, nt, mo, w, d, step):
+    """What the split-bf16 numerators (t_hi d_hi + t_hi d_lo + t_lo d_hi, the
+    lo*lo product dropped) change in each 'short' output, computed in FP64:
+    (tanh(sum_ch atanh(cc_split) z / sum z) - the same with exact cc) times
+    the template's scale.  Only the valid lags of the reference's
+    'variable_precise' range (matched_filter.c:384-385) are non-zero."""
+    T, S, C, L = tp.shape
+    N = d.shape[-1]
+    n_corr = (N - L) // step + 1
+    eps = float(np.finfo(np.float32).eps)
+    out = np.zeros((T, n_corr))
+    scale = np.cumsum(w.reshape(T, -1).astype(np.float64).sum(axis=1))
+    for t in range(T):
+        lo, hi = min(0, int(mo[t].min())), max(0, int(mo[t].max()))
+        start = -(-abs(lo) // step) * step
+        ks = np.arange(start, N - L - hi - step, step) // step
+        exact, split, zsum = np.zeros(ks.size), np.zeros(ks.size), 0.0
+        for s in range(S):
+            for c in range(C):
+                n, wt = int(nt[t, s, c]), float(w[t, s, c])
+                z = np.sqrt(n - 3.0) * wt
+                zsum += z
+                if wt == 0.0:
+                    continue
+                tt = tp[t, s, c, :n]
+                win = d[s, c][ks[:, None] * step + mo[t, s, c] + np.arange(n)[None, :]]
+                th, wh = _bf16(tt), _bf16(win)
+                tl, wl = _bf16(tt - th), _bf16(win - wh)
+                den = np.sqrt(np.sum(tt.astype(np.float64) ** 2) *
+                              np.sum(win.astype(np.float64) ** 2, axis=1))
+                for num, acc in ((win @ tt.astype(np.float64), exact),
+                                 (wh @ th + wl @ th + wh @ tl, split)):
+                    cc = np.where(den > 1e-6, num / den, 0.0)
+                    acc += np.arctanh(cc - 10 * eps) * z
+        out[t, ks] = (np.tanh(split / zsum) - np.tanh(exact / zsum)) * scale[t]
+    return out
+
+
+@pytest.mark.parametrize("step", [1, 3])
+@pytest.mark.parametrize("normalize", ["short", "full"])
+def test_variable_tensor_core_short_channels(oracle_built, step, normalize):
+    """Channels far shorter than the longest one (down to 4 taps, fewer taps
+    than some phases reach): the tensor-core issuers stop each channel's K
+    range at its own length, the prefix-sum windows use that length.
+
+    With 4-40 taps many coefficients lie near +-1, where atanh's slope
+    1 / (1 - cc^2) reaches ~100: the split-bf16 rounding of the products
+    alone then moves outputs by up to ~1e-3 (FP64 emulation).  For 'short'
+    the bar is the oracle shifted by that emulated split-bf16 change, within
+    TOL_TC; 'full' (centred windows, no coefficient near 1 here) is held to
+    TOL_TC against the oracle directly."""
+    rng = np.random.default_rng(90 + step)
+    tp, mo, w, d = random_search(95 + step, 4, 3, 3, 300, 12000, -50, 150,
+                                 dc=2.0 if normalize == "full" else 0.0, zero_weights=3)
+    nt = rng.integers(4, 40, mo.shape).astype(np.int32)
+    nt[0, 0, 0] = 300
+    nt[1] = rng.integers(200, 301, nt[1].shape)
+    tp = np.ascontiguousarray(tp[..., :int(nt.max())])
+    for idx in np.ndindex(nt.shape):
+        tp[idx][nt[idx]:] = 0.0
+    got = fmf.matched_filter(tp, mo, w, d, step, n_samples_template=nt, check_zeros=False,
+                             normalize=normalize, precision="split_bf16")
+    ref = oracle_built.run_oracle_variable(tp, nt, mo, w, d, step, normalize)
+    if normalize == "short":
+        ref = ref + _split_bf16_shift(tp, nt, mo, w, d, step)
+    _check(got, ref, float(np.sum(w)), TOL_TC)
 
 
 def test_variable_equal_lengths_match_fixed_length_coefficients(oracle_built):
