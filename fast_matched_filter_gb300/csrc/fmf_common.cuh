@@ -40,8 +40,9 @@ struct Problem {
     int network_sum;      // 1 weighted sum over channels, 0 per channel
     // Per-channel template lengths (Fisher-z network sum), else null:
     const int *ntap;      // (T, SC) taps of each channel (templates zero-padded to L)
-    const double *pre2;   // (SC, N+1) FP64 prefix sums of d^2 (centred d for full)
+    const double *pre2;   // (SC, N+1) FP64 prefix sums of centred d^2 (full), else null
     const double *pre1;   // (SC, N+1) FP64 prefix sums of centred d (full), else null
+    const float2 *pre2f;  // (SC, N+1) prefix sums of d^2 as hi + lo floats (short), else null
     const float *zweight; // (T, SC) Fisher-z weight of each channel
 };
 

@@ -57,8 +57,11 @@ namespace fmf {
 
 constexpr int TC_Q = 128;
 constexpr int TC_CB = TC_Q / 8;
-constexpr int TC_EPI_WARPS = 8;                    // epilogue warps (2 per TMEM lane quarter)
-constexpr int TC_THREADS = 32 * (4 + TC_EPI_WARPS);  // + producer, 2 MMA issuers, 1 idle warp
+// Epilogue warps (2 per TMEM lane quarter; 4 per quarter for per-channel
+// template lengths, whose epilogue does more arithmetic per output and needs
+// more warps to hide its latency) + producer, 2 MMA issuers, 1 idle warp.
+constexpr int tc_epi_warps(bool var) { return var ? 16 : 8; }
+constexpr int tc_threads(bool var) { return 32 * (4 + tc_epi_warps(var)); }
 constexpr int TC_TG = 16;  // templates interleaved per group of CTAs (L2 reuse of data rows)
 constexpr unsigned long long TC_WAIT_NS = 2000000000ull;  // 2 s per wait
 
@@ -400,8 +403,13 @@ __device__ __forceinline__ void decode_item(const TcBatch &B, long long item, in
 constexpr int TC_NB_MAX = 128;  // largest tile; TMEM columns: D0 [0,128), D1 [128,256), sum [256,384)
 constexpr int TC_NACC = 2;      // accumulator buffers
 
-__global__ void __launch_bounds__(TC_THREADS, 1) tc_persistent(const __grid_constant__ TcBatch B)
+// VAR: per-channel template lengths (Problem::ntap set in every search of the
+// batch), a separate instantiation so that the fixed-length epilogue keeps
+// its registers.
+template <bool VAR>
+__global__ void __launch_bounds__(tc_threads(VAR), 1) tc_persistent(const __grid_constant__ TcBatch B)
 {
+    constexpr int TC_EPI_WARPS = tc_epi_warps(VAR);
     extern __shared__ __align__(1024) uint8_t smem[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int split = B.split;
@@ -588,7 +596,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) tc_persistent(const __grid_cons
                         const int mu = pr.mu[meta];
                         const int sres = ((mu % TC_Q) + TC_Q) % TC_Q;
                         int lphi = (P.L - phi + step - 1) / step;
-                        if (P.ntap) {  // per-channel length: the taps past it are zeros, skip them
+                        if (VAR) {  // per-channel length: the taps past it are zeros, skip them
                             const int n = P.ntap[(size_t)t * SC + ch];
                             const int own = n > phi ? (n - phi + step - 1) / step : 0;
                             lphi = min(lphi, own);
@@ -638,7 +646,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) tc_persistent(const __grid_cons
         // TC_EPI_WARPS warps: warp w reads TMEM lane quarter w % 4 (rows
         // 32*(w%4) + lane) and the NC columns [a0, a0 + NC) of the accumulators;
         // the network sum of its outputs lives in TMEM columns 2*NB + [a0, a0 + NC).
-        constexpr int CH = 16;  // columns per TMEM access and per batch of statistics loads
+        constexpr int CH = VAR ? 8 : 16;  // columns per TMEM access and per batch of statistics loads
         const int quarter = warp & 3;
         const int cgroup = (warp - 4) >> 2;  // column group of this warp
         const int m = 32 * quarter + lane;   // accumulator row
@@ -668,7 +676,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) tc_persistent(const __grid_cons
             const int SC = pr.P.SC, step = pr.P.step, n_corr = pr.P.n_corr, N = pr.P.N;
             const bool full = pr.P.normalize != 0, nsum = pr.P.network_sum != 0;
             // per-channel template lengths: FP64 prefix sums and a Fisher-z network sum
-            const bool var = pr.P.ntap != nullptr;
+            constexpr bool var = VAR;
             const float *__restrict__ stat_e = pr.P.stat_e;
             const float *__restrict__ stat_m = pr.P.stat_m;
             const float *__restrict__ sstp = pr.P.sst;
@@ -701,7 +709,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1) tc_persistent(const __grid_cons
                 const float *__restrict__ sm = (full && !var) ? stat_m + (size_t)ch * N + u0 : se;
                 const int ntap = var ? pr.P.ntap[row] : 0;
                 const float zw = var ? pr.P.zweight[row] : 0.0f;
-                const double *__restrict__ p2 = var ? pr.P.pre2 + (size_t)ch * (N + 1) + u0 : nullptr;
+                const double *__restrict__ p2 =
+                    (var && full) ? pr.P.pre2 + (size_t)ch * (N + 1) + u0 : nullptr;
+                const float2 *__restrict__ pf =
+                    (var && !full) ? pr.P.pre2f + (size_t)ch * (N + 1) + u0 : nullptr;
                 const double *__restrict__ p1 =
                     (var && full) ? pr.P.pre1 + (size_t)ch * (N + 1) + u0 : nullptr;
                 const double inv_n = var ? 1.0 / (double)ntap : 0.0;
@@ -741,18 +752,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1) tc_persistent(const __grid_cons
                         // window sums of the channel's own length from the FP64 prefix sums,
                         // the 'precise' threshold on the square root, and
                         // atanh(cc - 10 eps) * z into the network sum
-                        auto var_value = [&](int i, double s2, double s1) {
+                        auto var_value = [&](int i, float num, float ssd) {
                             const int a = c0 + i;
-                            float num = x[i], ssd;
-                            if (full) {
-                                const double v = s2 - s1 * s1 * inv_n;
-                                num = fmaf(-(float)(s1 * inv_n), ts, num);
-                                ssd = (float)(v > 0.0 ? v : 0.0);
-                            } else {
-                                ssd = (float)s2;
-                            }
-                            const float den = sqrtf(sst * ssd);
-                            const float cc = den > kThreshold ? num / den : 0.0f;
+                            // the threshold on sqrt(sst * ssd), as p * rsqrt(p); p = 0 gives NaN there
+                            const float p = sst * ssd, r = rsqrtf(p);
+                            const float cc = p * r > kThreshold ? num * r : 0.0f;
                             const float prev = first ? 0.0f : sv[i];
                             sv[i] = (a >= a_lo && a < a_hi)
                                         ? fmaf(atanhf(cc - 10.0f * FLT_EPSILON), zw, prev)
@@ -761,18 +765,19 @@ __global__ void __launch_bounds__(TC_THREADS, 1) tc_persistent(const __grid_cons
                         auto off = [&](int i) {
                             return (long long)min(max(c0 + i, a_lo), a_hi - 1) * qs;
                         };
-                        if (!full) {
+                        if (!full) {  // hi + lo float prefix pairs: FP32 only
 #pragma unroll
                             for (int h = 0; h < CH; h += 4) {  // loads of 4 values, then their use
-                                double lo[4], hi[4];
+                                float2 lo[4], hi[4];
 #pragma unroll
                                 for (int j = 0; j < 4; j++) {
-                                    lo[j] = any ? p2[off(h + j)] : 0.0;
-                                    hi[j] = any ? p2[off(h + j) + ntap] : 0.0;
+                                    const float2 *q = pf + off(h + j);
+                                    lo[j] = any ? q[0] : make_float2(0.0f, 0.0f);
+                                    hi[j] = any ? q[ntap] : make_float2(0.0f, 0.0f);
                                 }
 #pragma unroll
                                 for (int j = 0; j < 4; j++)
-                                    var_value(h + j, hi[j] - lo[j], 0.0);
+                                    var_value(h + j, x[h + j], (hi[j].x - lo[j].x) + (hi[j].y - lo[j].y));
                             }
                         } else {
 #pragma unroll
@@ -786,8 +791,12 @@ __global__ void __launch_bounds__(TC_THREADS, 1) tc_persistent(const __grid_cons
                                     hi1[j] = any ? p1[off(h + j) + ntap] : 0.0;
                                 }
 #pragma unroll
-                                for (int j = 0; j < 2; j++)
-                                    var_value(h + j, hi2[j] - lo2[j], hi1[j] - lo1[j]);
+                                for (int j = 0; j < 2; j++) {
+                                    const double s2 = hi2[j] - lo2[j], s1 = hi1[j] - lo1[j];
+                                    const double v = s2 - s1 * s1 * inv_n;
+                                    var_value(h + j, fmaf(-(float)(s1 * inv_n), ts, x[h + j]),
+                                              (float)(v > 0.0 ? v : 0.0));
+                                }
                             }
                         }
                     } else if (nsum && interior) {
@@ -1018,11 +1027,17 @@ int tc_run(const TcProb *probs, int n, int split, unsigned long long *queue, uns
     if (e != cudaSuccess)
         return set_error(FMF_ERR_CUDA, "clearing the tile queue: %s", cudaGetErrorString(e));
     const unsigned grid = (unsigned)(items < n_sms() ? (items > 0 ? items : 1) : n_sms());
-    e = cudaFuncSetAttribute(tc_persistent, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    int n_var = 0;
+    for (int i = 0; i < n; i++)
+        n_var += probs[i].P.ntap != nullptr;
+    if (n_var != 0 && n_var != n)
+        return set_error(FMF_ERR_ARG, "a persistent launch mixes per-channel and fixed template lengths");
+    void (*kern)(const TcBatch) = n_var ? tc_persistent<true> : tc_persistent<false>;
+    e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess)
         return set_error(FMF_ERR_CUDA, "tc_persistent shared memory (%zu bytes): %s", smem,
                          cudaGetErrorString(e));
-    tc_persistent<<<grid, TC_THREADS, smem, s>>>(B);
+    kern<<<grid, tc_threads(n_var != 0), smem, s>>>(B);
     count_launch();
     return check_launch("tc_persistent");
 }
