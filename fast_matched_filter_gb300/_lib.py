@@ -60,7 +60,7 @@ EXPORTS = ("fmf_matched_filter", "matched_filter", "fmf_matched_filter_ex",
            "fmf_batch_add", "fmf_batch_set_tiles", "fmf_batch_run", "fmf_batch_launch_count",
            "fmf_batch_destroy", "fmf_selftest_wait_timeout", "fmf_matched_filter_variable",
            "fmf_matched_filter_variable_ex", "fmf_detect", "fmf_matched_filter_detect",
-           "fmf_template_energies", "fmf_matched_filter_check_zeros")
+           "fmf_template_energies", "fmf_matched_filter_check_zeros", "fmf_eval_atanh")
 
 DETECT_CAPACITY = 16384  # FMF_DETECT_CAPACITY
 # detection arguments after the rows: n_mad, min_separation, max_detections, six outputs,
@@ -131,6 +131,8 @@ def load(path=None):
     lib.fmf_matched_filter_check_zeros.restype = ct.c_int
     lib.fmf_template_energies.argtypes = [ct.c_void_p, _sz, _sz, ct.c_void_p, ct.c_int, ct.c_void_p]
     lib.fmf_template_energies.restype = ct.c_int
+    lib.fmf_eval_atanh.argtypes = [ct.c_void_p, ct.c_void_p, _sz, ct.c_void_p]
+    lib.fmf_eval_atanh.restype = ct.c_int
     if path is None:
         _lib = lib
     return lib

@@ -107,6 +107,7 @@ __global__ void window_stats_kernel(const float *, int, int, int, const float *,
 int launch_tc(const Problem &P, const float *data_for_tc, int precision, unsigned *err, Scratch &ws,
               cudaStream_t s, int forced_nb, int template_group);
 int launch_wait_selftest(unsigned *err, unsigned ms, cudaStream_t s);
+int launch_fisher_atanh(const float *y, float *out, long long n, cudaStream_t s);
 
 // ---------------------------------------------------------------- device error word
 // Kernels with bounded waits OR a code into this word when a wait gives up.
@@ -944,6 +945,16 @@ int fmf_selftest_wait_timeout(unsigned ms)
     if ((rc = fmf::launch_wait_selftest(err, ms, nullptr)))
         return rc;
     return fmf_device_errors();
+}
+
+int fmf_eval_atanh(const float *y, float *out, size_t n, void *stream)
+{
+    fmf::clear_error();
+    if (n > 0 && (!y || !out))
+        return fmf::set_error(FMF_ERR_ARG, "null array argument");
+    if (n > ((size_t)1 << 40))
+        return fmf::set_error(FMF_ERR_ARG, "n too large");
+    return fmf::launch_fisher_atanh(y, out, (long long)n, (cudaStream_t)stream);
 }
 
 int fmf_device_errors(void)

@@ -403,6 +403,70 @@ __device__ __forceinline__ void decode_item(const TcBatch &B, long long item, in
 constexpr int TC_NB_MAX = 128;  // largest tile; TMEM columns: D0 [0,128), D1 [128,256), sum [256,384)
 constexpr int TC_NACC = 2;      // accumulator buffers
 
+// 1/sqrt(x), one approximate MUFU operation; subnormal x is flushed to zero
+// (result +inf).
+__device__ __forceinline__ float rsqrt_ftz(float x)
+{
+    float r;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
+// atanh(y) in FP32 for the Fisher-z network sum, at most a few ulp from the
+// exact value (the accuracy of the CUDA library's atanhf) with far fewer
+// instructions for the common small arguments:
+//  |y| <= 1/4: the Maclaurin series y + y^3/3 + ... + y^13/13 (the first
+//    omitted term is below 2^-25 of the result);
+//  1/4 < |y| < 1: atanh(a) = ln(q) / 2 with q = (1 + a) / (1 - a); q = 2^k m
+//    with m in [sqrt(1/2), sqrt(2)) and ln(m) = 2 atanh(s), s = (m - 1) / (m + 1),
+//    |s| <= 0.1716, from the same series to s^9/9;
+//  |y| = 1 gives +-inf, |y| > 1 and NaN give NaN.
+__device__ __forceinline__ float fisher_atanh(float y)
+{
+    const float a = fabsf(y);
+    float r;
+    if (a <= 0.25f) {
+        const float z = y * y;
+        float p = fmaf(1.0f / 13.0f, z, 1.0f / 11.0f);
+        p = fmaf(p, z, 1.0f / 9.0f);
+        p = fmaf(p, z, 1.0f / 7.0f);
+        p = fmaf(p, z, 1.0f / 5.0f);
+        p = fmaf(p, z, 1.0f / 3.0f);
+        return fmaf(y * z, p, y);
+    }
+    if (!(a < 1.0f))  // 1, above 1, NaN
+        return a == 1.0f ? copysignf(INFINITY, y) : __int_as_float(0x7fc00000);
+    const float q = __fdividef(1.0f + a, 1.0f - a);  // in (5/3, 2^25]
+    const int bits = __float_as_int(q);
+    const int k = (bits - 0x3f3504f3) >> 23;  // 0x3f3504f3 = sqrt(1/2)
+    const float m = __int_as_float(bits - (k << 23));
+    const float s = __fdividef(m - 1.0f, m + 1.0f);
+    const float z = s * s;
+    float p = fmaf(1.0f / 9.0f, z, 1.0f / 7.0f);
+    p = fmaf(p, z, 1.0f / 5.0f);
+    p = fmaf(p, z, 1.0f / 3.0f);
+    r = fmaf(s * z, p, s);                               // ln(m) / 2
+    r = fmaf((float)k, 0.5f * 0.693145751953125f, r);    // + k ln2 / 2 (ln2 in two parts)
+    r = fmaf((float)k, 0.5f * 1.4286068203094172e-06f, r);
+    return copysignf(r, y);
+}
+
+__global__ void fisher_atanh_kernel(const float *__restrict__ y, float *__restrict__ out, long long n)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n)
+        out[i] = fisher_atanh(y[i]);
+}
+
+int launch_fisher_atanh(const float *y, float *out, long long n, cudaStream_t s)
+{
+    if (n <= 0)
+        return FMF_OK;
+    fisher_atanh_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(y, out, n);
+    count_launch();
+    return check_launch("fisher_atanh_kernel");
+}
+
 // VAR: per-channel template lengths (Problem::ntap set in every search of the
 // batch), a separate instantiation so that the fixed-length epilogue keeps
 // its registers.
@@ -691,8 +755,9 @@ __global__ void __launch_bounds__(tc_threads(VAR), 1) tc_persistent(const __grid
             const int a_hi = (int)min((long long)nb, (khi - kb + TC_Q - 1) / TC_Q) - a0;
             const bool any = busy && a_hi > a_lo;
             // the whole warp's outputs of this item are valid (the usual case)
-            const bool interior = __all_sync(0xffffffffu, a_lo <= 0 && a_hi >= NC) && !var;
+            const bool interior = __all_sync(0xffffffffu, a_lo <= 0 && a_hi >= NC);
             const long long qs = (long long)TC_Q * step;
+            const int qs32 = TC_Q * step;
             const float *w = pr.P.w + (size_t)t * SC;
             const int *mo = pr.P.mo + (size_t)t * SC;
             bool first = true;
@@ -715,7 +780,7 @@ __global__ void __launch_bounds__(tc_threads(VAR), 1) tc_persistent(const __grid
                     (var && !full) ? pr.P.pre2f + (size_t)ch * (N + 1) + u0 : nullptr;
                 const double *__restrict__ p1 =
                     (var && full) ? pr.P.pre1 + (size_t)ch * (N + 1) + u0 : nullptr;
-                const double inv_n = var ? 1.0 / (double)ntap : 0.0;
+                const double inv_n = (var && full) ? 1.0 / (double)ntap : 0.0;
                 float *oc = outp + ((size_t)t * n_corr + kb + (long long)TC_Q * a0) * SC + ch;
                 // statistics: all loads of a chunk issued together (indices clamped into the
                 // valid range) before any use; the first chunk before waiting for the accumulator
@@ -754,26 +819,29 @@ __global__ void __launch_bounds__(tc_threads(VAR), 1) tc_persistent(const __grid
                         // atanh(cc - 10 eps) * z into the network sum
                         auto var_value = [&](int i, float num, float ssd) {
                             const int a = c0 + i;
-                            // the threshold on sqrt(sst * ssd), as p * rsqrt(p); p = 0 gives NaN there
-                            const float p = sst * ssd, r = rsqrtf(p);
+                            // the threshold on sqrt(sst * ssd), as p * rsqrt(p); p = 0 gives
+                            // NaN there, and p below the normal range (flushed) cannot pass it
+                            const float p = sst * ssd, r = rsqrt_ftz(p);
                             const float cc = p * r > kThreshold ? num * r : 0.0f;
                             const float prev = first ? 0.0f : sv[i];
-                            sv[i] = (a >= a_lo && a < a_hi)
-                                        ? fmaf(atanhf(cc - 10.0f * FLT_EPSILON), zw, prev)
+                            sv[i] = (interior || (a >= a_lo && a < a_hi))
+                                        ? fmaf(fisher_atanh(cc - 10.0f * FLT_EPSILON), zw, prev)
                                         : prev;
                         };
+                        // element offsets of the windows (32-bit: at most NB * Q * step)
                         auto off = [&](int i) {
-                            return (long long)min(max(c0 + i, a_lo), a_hi - 1) * qs;
+                            return (interior ? c0 + i : min(max(c0 + i, a_lo), a_hi - 1)) * qs32;
                         };
                         if (!full) {  // hi + lo float prefix pairs: FP32 only
+                            const float2 *__restrict__ pf_hi = pf + ntap;
 #pragma unroll
                             for (int h = 0; h < CH; h += 4) {  // loads of 4 values, then their use
                                 float2 lo[4], hi[4];
 #pragma unroll
                                 for (int j = 0; j < 4; j++) {
-                                    const float2 *q = pf + off(h + j);
-                                    lo[j] = any ? q[0] : make_float2(0.0f, 0.0f);
-                                    hi[j] = any ? q[ntap] : make_float2(0.0f, 0.0f);
+                                    const int o = off(h + j);
+                                    lo[j] = any ? pf[o] : make_float2(0.0f, 0.0f);
+                                    hi[j] = any ? pf_hi[o] : make_float2(0.0f, 0.0f);
                                 }
 #pragma unroll
                                 for (int j = 0; j < 4; j++)

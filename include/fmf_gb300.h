@@ -297,6 +297,11 @@ FMF_API int fmf_device_errors(void);
  * and reported it as the library's kernels do; the device stays usable. */
 FMF_API int fmf_selftest_wait_timeout(unsigned ms);
 
+/* Accuracy check of the atanh used by the tensor-core form of the per-channel
+ * length search (no reference counterpart): out[i] = atanh(y[i]) as that
+ * epilogue computes it, for n device floats, asynchronous on `stream`. */
+FMF_API int fmf_eval_atanh(const float *y, float *out, size_t n, void *stream);
+
 /* Event timing (no reference counterpart; used by the benchmark).
  * fmf_timing_begin() makes every later call on this thread record CUDA
  * events on its stream around its preprocessing kernels and around its

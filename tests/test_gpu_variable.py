@@ -141,3 +141,33 @@ def test_variable_equal_lengths_match_fixed_length_coefficients(oracle_built):
     got = fmf.matched_filter(tp, mo, w, d, 1, n_samples_template=nt, check_zeros=False)
     ref = oracle_built.run_oracle_variable(tp, nt, mo, w, d, 1)
     _check(got, ref, 1.0)
+
+
+def test_fisher_atanh_accuracy():
+    """The atanh of the tensor-core Fisher-z epilogue (series for |y| <= 1/4,
+    logarithm reduction above) against FP64 atanh: within 4 ulp everywhere in
+    (-1, 1), +-inf at +-1, NaN beyond."""
+    torch = pytest.importorskip("torch")
+    from fast_matched_filter_gb300 import _lib
+    lib = _lib.load()
+    rng = np.random.default_rng(7)
+    y = np.concatenate([
+        rng.uniform(-1, 1, 2_000_000), rng.uniform(-0.3, 0.3, 1_000_000),
+        1 - np.logspace(-7.2, 0, 100_000), -(1 - np.logspace(-7.2, 0, 100_000)),
+        np.logspace(-40, -0.5, 100_000), np.nextafter(np.float32(0.25), np.float32([0, 1])),
+        np.float32([0.0, -0.0, 1e-45, 0.25, -0.25])]).astype(np.float32)
+    y = y[np.abs(y) < 1]
+    dy = torch.from_numpy(y).cuda()
+    out = torch.empty_like(dy)
+    _lib.check(lib.fmf_eval_atanh(dy.data_ptr(), out.data_ptr(), y.size, None), lib)
+    got = out.cpu().numpy().astype(np.float64)
+    exact = np.arctanh(y.astype(np.float64))
+    ulp = np.spacing(np.abs(exact).astype(np.float32)).astype(np.float64)
+    err = np.abs(got - exact) / ulp
+    assert err.max() <= 4.0, "max %.2f ulp at y=%r" % (err.max(), y[np.argmax(err)])
+    special = np.float32([1.0, -1.0, 1.0000001, -1.5, np.nan, np.inf])
+    ds = torch.from_numpy(special).cuda()
+    os_ = torch.empty_like(ds)
+    _lib.check(lib.fmf_eval_atanh(ds.data_ptr(), os_.data_ptr(), special.size, None), lib)
+    s = os_.cpu().numpy()
+    assert s[0] == np.inf and s[1] == -np.inf and np.isnan(s[2:]).all()
