@@ -86,12 +86,14 @@ def make_workload(name, rank=0, templates=0, samples=0):
         kw["n_samples"] = samples
     gen = {"config0": synthetic.config0, "config1": synthetic.config1,
            "config2": synthetic.config2, "config4": synthetic.config4,
-           "variable": synthetic.variable}[name]
+           "variable": synthetic.variable, "variable_full": synthetic.variable}[name]
+    if name == "variable_full":
+        kw["normalize"] = "full"
     if name == "config0":
         cfg = gen(seed=100 + 1000 * rank)
     else:
-        cfg = gen(seed={"config1": 101, "config2": 102, "config4": 104, "variable": 105}[name]
-                  + 1000 * rank, **kw)
+        cfg = gen(seed={"config1": 101, "config2": 102, "config4": 104, "variable": 105,
+                        "variable_full": 105}[name] + 1000 * rank, **kw)
     tp = cfg["templates"]
     cfg["sst"] = np.sum(tp ** 2, axis=-1).astype(np.float32)
     cfg["macs"] = synthetic.macs(tp.shape, cfg["data"].shape[-1], cfg["step"])
@@ -685,7 +687,8 @@ def run_variable(args):
     torch.cuda.set_device(0)
     lib = _lib.load()
     precision = "split_bf16" if args.precision == "auto" else args.precision
-    cfg = make_workload("variable", 0, args.templates, args.samples)
+    cfg = make_workload(args.workload, 0, args.templates, args.samples)
+    nz = 1 if cfg["normalize"] == "full" else 0
     T, S, C, L = cfg["templates"].shape
     N = cfg["data"].shape[-1]
     n_corr = cfg["n_corr"]
@@ -704,7 +707,7 @@ def run_variable(args):
             st = lib.fmf_matched_filter_variable_ex(
                 dev["templates"].data_ptr(), dev["sst"].data_ptr(), dev["moveouts"].data_ptr(),
                 dev["data"].data_ptr(), dev["weights"].data_ptr(), cfg["step"], dnt.data_ptr(), N,
-                T, S, C, n_corr, out.data_ptr(), 0, flags, stream.cuda_stream)
+                T, S, C, n_corr, out.data_ptr(), nz, flags, stream.cuda_stream)
             _lib.check(st, lib)
             return lib.fmf_last_launch_count()
 
@@ -775,7 +778,7 @@ def run_variable(args):
         st = lib.fmf_matched_filter_variable_ex(
             host["templates"].ctypes.data, host["sst"].ctypes.data, host["moveouts"].ctypes.data,
             host["data"].ctypes.data, host["weights"].ctypes.data, cfg["step"], nt.ctypes.data, N,
-            T, S, C, n_corr, cc.ctypes.data, 0, _lib.flag_precision(precision), None)
+            T, S, C, n_corr, cc.ctypes.data, nz, _lib.flag_precision(precision), None)
         _lib.check(st, lib)
 
     call_host()
@@ -872,7 +875,7 @@ def main(argv=None):
         return run_reference_arm(args)
     if args.workload == "config3":
         return run_batch(args)
-    if args.workload == "variable":
+    if args.workload in ("variable", "variable_full"):
         return run_variable(args)
     return run_ours(args)
 

@@ -271,6 +271,7 @@ int prepare_problem(const Args &a, Scratch &ws, cudaStream_t s, Problem *Pout, c
     P.pre2 = nullptr;
     P.pre1 = nullptr;
     P.pre2f = nullptr;
+    P.pre1f = nullptr;
     P.zweight = nullptr;
 
     if (!P.network_sum) {

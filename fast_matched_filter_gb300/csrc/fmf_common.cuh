@@ -40,11 +40,56 @@ struct Problem {
     int network_sum;      // 1 weighted sum over channels, 0 per channel
     // Per-channel template lengths (Fisher-z network sum), else null:
     const int *ntap;      // (T, SC) taps of each channel (templates zero-padded to L)
-    const double *pre2;   // (SC, N+1) FP64 prefix sums of centred d^2 (full), else null
-    const double *pre1;   // (SC, N+1) FP64 prefix sums of centred d (full), else null
-    const float2 *pre2f;  // (SC, N+1) prefix sums of d^2 as hi + lo floats (short), else null
+    const double *pre2;   // unused (FP64 prefix sums), null
+    const double *pre1;   // unused, null
+    const float2 *pre2f;  // (SC, N+1) prefix sums of d^2 (centred d for full) as hi + lo floats
+    const float2 *pre1f;  // (SC, N+1) prefix sums of centred d as hi + lo floats (full), else null
     const float *zweight; // (T, SC) Fisher-z weight of each channel
 };
+
+#ifdef __CUDACC__
+// Window sums of a per-channel length n from prefix sums stored as float
+// pairs P = hi + lo (hi = fl(P), lo = fl(P - hi), ~48 significant bits), in
+// FP32 arithmetic only.
+
+// a - b = s + e exactly (Knuth's TwoSum on a and -b).
+__device__ __forceinline__ float two_diff(float a, float b, float &e)
+{
+    const float s = a - b, bb = s - a;
+    e = (a - (s - bb)) - (b + bb);
+    return s;
+}
+
+// 'short': sum of d^2 over the window [a, b) = (hi_b - hi_a) + (lo_b - lo_a).
+__device__ __forceinline__ float window_energy(float2 pa, float2 pb)
+{
+    return (pb.x - pa.x) + (pb.y - pa.y);
+}
+
+// 'full': centred energy v = S2 - S1^2 / n and mean S1 / n of the window,
+// with S2, S1 and S1^2 / n carried as unevaluated float pairs (TwoSum, and
+// FMA for the exact square and division residuals), so that v keeps float
+// accuracy even when the window mean dominates (S2 / v large).
+__device__ __forceinline__ void window_centred(float2 a2, float2 b2, float2 a1, float2 b1, float nf,
+                                               float inv_n, float &v, float &mean)
+{
+    float e2, e1;
+    const float s2h = two_diff(b2.x, a2.x, e2);
+    const float s2l = e2 + (b2.y - a2.y);
+    const float s1h = two_diff(b1.x, a1.x, e1);
+    const float s1l = e1 + (b1.y - a1.y);
+    const float h = s1h + s1l, l = s1l - (h - s1h);  // S1 = h + l, |l| <= ulp(h) / 2
+    mean = h * inv_n;
+    const float p = h * h;
+    const float pe = fmaf(2.0f * h, l, fmaf(h, h, -p));  // S1^2 = p + pe (+ l^2)
+    const float qh = p * inv_n;
+    const float ql = (fmaf(-qh, nf, p) + pe) * inv_n;    // S1^2 / n = qh + ql
+    float ev;
+    const float vh = two_diff(s2h, qh, ev);
+    const float r = vh + ((ev + s2l) - ql);
+    v = r > 0.0f ? r : 0.0f;
+}
+#endif
 
 }  // namespace fmf
 

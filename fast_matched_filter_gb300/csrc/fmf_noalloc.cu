@@ -201,6 +201,7 @@ extern "C" int fmf_matched_filter_noalloc(const float *templates, const float *s
     P.pre2 = nullptr;
     P.pre1 = nullptr;
     P.pre2f = nullptr;
+    P.pre1f = nullptr;
     P.zweight = nullptr;
     for (int t0 = 0; t0 < T; t0 += 65535) {
         Problem Q = P;

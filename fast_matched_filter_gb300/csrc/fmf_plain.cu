@@ -214,9 +214,9 @@ plain_kernel(const Problem P, const PlainGeom g)
                 const float sst = P.sst[row], zw = P.zweight[row];
                 const float ts = P.normalize ? P.tsum[row] : 0.0f;
                 const int n = P.ntap[row];
-                const double *p2 = P.normalize ? P.pre2 + (size_t)ch * (P.N + 1) : nullptr;
-                const double *p1 = P.normalize ? P.pre1 + (size_t)ch * (P.N + 1) : nullptr;
-                const float2 *pf = P.normalize ? nullptr : P.pre2f + (size_t)ch * (P.N + 1);
+                const float nf = (float)n, inv_n = 1.0f / nf;
+                const float2 *p2 = P.pre2f + (size_t)ch * (P.N + 1);
+                const float2 *p1 = P.normalize ? P.pre1f + (size_t)ch * (P.N + 1) : nullptr;
 #pragma unroll
                 for (int r = 0; r < PL_R; r++) {
                     long long k = k0 + tid * PL_R + r;
@@ -224,14 +224,11 @@ plain_kernel(const Problem P, const PlainGeom g)
                         const long long u = k * P.step + mo[ch];
                         float num = acc[r], ssd;
                         if (P.normalize) {
-                            const double s2 = p2[u + n] - p2[u];
-                            const double s1 = p1[u + n] - p1[u];
-                            const double v = s2 - s1 * s1 / (double)n;
-                            num = fmaf(-(float)(s1 / (double)n), ts, num);
-                            ssd = (float)(v > 0.0 ? v : 0.0);
-                        } else {  // hi + lo float prefix pairs
-                            const float2 a = pf[u], b = pf[u + n];
-                            ssd = (b.x - a.x) + (b.y - a.y);
+                            float mean;
+                            window_centred(p2[u], p2[u + n], p1[u], p1[u + n], nf, inv_n, ssd, mean);
+                            num = fmaf(-mean, ts, num);
+                        } else {
+                            ssd = window_energy(p2[u], p2[u + n]);
                         }
                         const float den = sqrtf(sst * ssd);
                         const float cc = den > kThreshold ? num / den : 0.0f;

@@ -774,13 +774,10 @@ __global__ void __launch_bounds__(tc_threads(VAR), 1) tc_persistent(const __grid
                 const float *__restrict__ sm = (full && !var) ? stat_m + (size_t)ch * N + u0 : se;
                 const int ntap = var ? pr.P.ntap[row] : 0;
                 const float zw = var ? pr.P.zweight[row] : 0.0f;
-                const double *__restrict__ p2 =
-                    (var && full) ? pr.P.pre2 + (size_t)ch * (N + 1) + u0 : nullptr;
-                const float2 *__restrict__ pf =
-                    (var && !full) ? pr.P.pre2f + (size_t)ch * (N + 1) + u0 : nullptr;
-                const double *__restrict__ p1 =
-                    (var && full) ? pr.P.pre1 + (size_t)ch * (N + 1) + u0 : nullptr;
-                const double inv_n = (var && full) ? 1.0 / (double)ntap : 0.0;
+                const float2 *__restrict__ pf = var ? pr.P.pre2f + (size_t)ch * (N + 1) + u0 : nullptr;
+                const float2 *__restrict__ pg =
+                    (var && full) ? pr.P.pre1f + (size_t)ch * (N + 1) + u0 : nullptr;
+                const float nf = (float)ntap, inv_n = var ? 1.0f / nf : 0.0f;
                 float *oc = outp + ((size_t)t * n_corr + kb + (long long)TC_Q * a0) * SC + ch;
                 // statistics: all loads of a chunk issued together (indices clamped into the
                 // valid range) before any use; the first chunk before waiting for the accumulator
@@ -845,25 +842,26 @@ __global__ void __launch_bounds__(tc_threads(VAR), 1) tc_persistent(const __grid
                                 }
 #pragma unroll
                                 for (int j = 0; j < 4; j++)
-                                    var_value(h + j, x[h + j], (hi[j].x - lo[j].x) + (hi[j].y - lo[j].y));
+                                    var_value(h + j, x[h + j], window_energy(lo[j], hi[j]));
                             }
-                        } else {
+                        } else {  // centred windows: double-float FP32 arithmetic
 #pragma unroll
                             for (int h = 0; h < CH; h += 2) {
-                                double lo2[2], hi2[2], lo1[2], hi1[2];
+                                float2 lo2[2], hi2[2], lo1[2], hi1[2];
 #pragma unroll
                                 for (int j = 0; j < 2; j++) {
-                                    lo2[j] = any ? p2[off(h + j)] : 0.0;
-                                    hi2[j] = any ? p2[off(h + j) + ntap] : 0.0;
-                                    lo1[j] = any ? p1[off(h + j)] : 0.0;
-                                    hi1[j] = any ? p1[off(h + j) + ntap] : 0.0;
+                                    const int o = off(h + j);
+                                    const float2 z2 = make_float2(0.0f, 0.0f);
+                                    lo2[j] = any ? pf[o] : z2;
+                                    hi2[j] = any ? pf[o + ntap] : z2;
+                                    lo1[j] = any ? pg[o] : z2;
+                                    hi1[j] = any ? pg[o + ntap] : z2;
                                 }
 #pragma unroll
                                 for (int j = 0; j < 2; j++) {
-                                    const double s2 = hi2[j] - lo2[j], s1 = hi1[j] - lo1[j];
-                                    const double v = s2 - s1 * s1 * inv_n;
-                                    var_value(h + j, fmaf(-(float)(s1 * inv_n), ts, x[h + j]),
-                                              (float)(v > 0.0 ? v : 0.0));
+                                    float v, mean;
+                                    window_centred(lo2[j], hi2[j], lo1[j], hi1[j], nf, inv_n, v, mean);
+                                    var_value(h + j, fmaf(-mean, ts, x[h + j]), v);
                                 }
                             }
                         }

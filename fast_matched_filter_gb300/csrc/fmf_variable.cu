@@ -16,8 +16,9 @@
 // transform applies to every output (matched_filter.c:405-408).
 //
 // Kernels: metadata (one thread, the reference's float accumulation order),
-// masked/centred templates, FP64 prefix sums of d^2 and d (global, so that
-// any window length is two subtractions), the numerator kernel with its
+// masked/centred templates, FP64 prefix sums of d^2 and d stored as float
+// pairs (global, so that any window length is a few FP32 operations), the
+// numerator kernel with its
 // variable-length epilogue -- the plain FP32 kernel (fmf_plain.cu) or the
 // tensor-core kernel (fmf_tc.cu), whose issuers stop each channel's K range
 // at its own length -- and the final transform.
@@ -187,17 +188,16 @@ __global__ void prefix_offsets_kernel(double *bs2, double *bs1, int nblk, int SC
 }
 
 // Phase 3, grid (blocks, SC), 256 threads: inclusive scan of the block plus
-// its offset -> pre[ch][i + 1] = sum_{x <= i} d'^2 (pre[ch][0] = 0); for 'full'
-// also the centred data and its prefix sums.  With pre2f (short) the FP64
-// prefix P is stored as the float pair hi = fl(P), lo = fl(P - hi): about 48
-// significant bits, so that a window sum is three FP32 additions,
-// (hi_b - hi_a) + (lo_b - lo_a), exact to float rounding while the window
-// holds more than ~2^-24 of the channel's energy up to that point, with no
-// FP64 arithmetic (slow on this part) in the correlation epilogues.
+// its offset -> P2[ch][i + 1] = sum_{x <= i} d'^2 (P2[ch][0] = 0) and, for
+// 'full', P1 of d' and the centred data.  Each FP64 prefix P is stored as the
+// float pair hi = fl(P), lo = fl(P - hi): about 48 significant bits, so that
+// the correlation epilogues form window sums in FP32 arithmetic only (FP64 is
+// slow on this part), exact to float rounding while the window holds more
+// than ~2^-24 of the channel's energy up to that point.
 __global__ void prefix_write_kernel(const float *__restrict__ data, int N, const float *__restrict__ mu,
                                     const double *__restrict__ bs2, const double *__restrict__ bs1,
-                                    int nblk, double *__restrict__ pre2, double *__restrict__ pre1,
-                                    float2 *__restrict__ pre2f, float *__restrict__ dcen)
+                                    int nblk, float2 *__restrict__ pre2f, float2 *__restrict__ pre1f,
+                                    float *__restrict__ dcen)
 {
     __shared__ double part2[32], part1[32];
     const int ch = blockIdx.y, blk = blockIdx.x;
@@ -248,30 +248,24 @@ __global__ void prefix_write_kernel(const float *__restrict__ data, int N, const
     }
     __syncthreads();
     const double off2 = part2[wid] + (x2 - s2), off1 = part1[wid] + (x1 - s1);
-    double *p2 = pre2 ? pre2 + (size_t)ch * (N + 1) : nullptr;
-    double *p1 = pre1 ? pre1 + (size_t)ch * (N + 1) : nullptr;
-    float2 *pf = pre2f ? pre2f + (size_t)ch * (N + 1) : nullptr;
+    float2 *p2 = pre2f + (size_t)ch * (N + 1);
+    float2 *p1 = pre1f ? pre1f + (size_t)ch * (N + 1) : nullptr;
+    auto split = [](double v) {
+        const float hi = (float)v;
+        return make_float2(hi, (float)(v - (double)hi));
+    };
     if (blk == 0 && threadIdx.x == 0) {
-        if (p2)
-            p2[0] = 0.0;
+        p2[0] = make_float2(0.0f, 0.0f);
         if (p1)
-            p1[0] = 0.0;
-        if (pf)
-            pf[0] = make_float2(0.0f, 0.0f);
+            p1[0] = make_float2(0.0f, 0.0f);
     }
 #pragma unroll
     for (int e = 0; e < per; e++) {
         const int i = i0 + threadIdx.x * per + e;
         if (i < N) {
-            const double v = off2 + v2[e];
-            if (p2)
-                p2[i + 1] = v;
-            if (pf) {
-                const float hi = (float)v;
-                pf[i + 1] = make_float2(hi, (float)(v - (double)hi));
-            }
+            p2[i + 1] = split(off2 + v2[e]);
             if (p1)
-                p1[i + 1] = off1 + v1[e];
+                p1[i + 1] = split(off1 + v1[e]);
         }
     }
 }
@@ -305,23 +299,21 @@ static int variable_device(const VArgs &a, int L, cudaStream_t s)
     Scratch ws(s);
     int *k_lo;
     float *zweight, *consts, *tmask, *tsum = nullptr, *mu = nullptr, *dcen = nullptr;
-    double *pre2 = nullptr, *pre1 = nullptr, *bs2, *bs1;
-    float2 *pre2f = nullptr;
+    double *bs2, *bs1;
+    float2 *pre2f, *pre1f = nullptr;
     const int nblk = (N + kPrefixBlock - 1) / kPrefixBlock;
     if ((rc = ws.get(&k_lo, 2 * (size_t)T, "template ranges")) ||
         (rc = ws.get(&zweight, (size_t)T * SC, "Fisher-z weights")) ||
         (rc = ws.get(&consts, 3 * (size_t)T, "transform constants")) ||
         (rc = ws.get(&tmask, (size_t)T * SC * L, "masked templates")) ||
+        (rc = ws.get(&pre2f, (size_t)SC * (N + 1), "prefix sums")) ||
         (rc = ws.get(&bs2, 2 * (size_t)SC * nblk, "block sums")))
-        return rc;
-    if (!full && (rc = ws.get(&pre2f, (size_t)SC * (N + 1), "prefix sums")))
         return rc;
     bs1 = bs2 + (size_t)SC * nblk;
     if (full && ((rc = ws.get(&tsum, (size_t)T * SC, "template sums")) ||
                  (rc = ws.get(&mu, (size_t)SC, "channel means")) ||
                  (rc = ws.get(&dcen, (size_t)SC * N, "centred data")) ||
-                 (rc = ws.get(&pre2, (size_t)SC * (N + 1), "prefix sums")) ||
-                 (rc = ws.get(&pre1, (size_t)SC * (N + 1), "prefix sums of d"))))
+                 (rc = ws.get(&pre1f, (size_t)SC * (N + 1), "prefix sums of d"))))
         return rc;
     int *k_hi = k_lo + T;
     float *norm_sum = consts, *bias = consts + T, *scale = consts + 2 * T;
@@ -333,8 +325,7 @@ static int variable_device(const VArgs &a, int L, cudaStream_t s)
         channel_mean_kernel<<<SC, 256, 0, s>>>(a.data, N, mu);
     prefix_block_kernel<<<dim3(nblk, SC), 256, 0, s>>>(a.data, N, mu, bs2, bs1, nblk);
     prefix_offsets_kernel<<<(SC + 127) / 128, 128, 0, s>>>(bs2, bs1, nblk, SC);
-    prefix_write_kernel<<<dim3(nblk, SC), 256, 0, s>>>(a.data, N, mu, bs2, bs1, nblk, pre2, pre1, pre2f,
-                                                       dcen);
+    prefix_write_kernel<<<dim3(nblk, SC), 256, 0, s>>>(a.data, N, mu, bs2, bs1, nblk, pre2f, pre1f, dcen);
     count_launch(full ? 6 : 5);
     if ((rc = check_launch("variable-length preprocessing")))
         return rc;
@@ -360,9 +351,10 @@ static int variable_device(const VArgs &a, int L, cudaStream_t s)
     P.normalize = a.normalize;
     P.network_sum = 1;
     P.ntap = a.ntap;
-    P.pre2 = pre2;
-    P.pre1 = pre1;
+    P.pre2 = nullptr;
+    P.pre1 = nullptr;
     P.pre2f = pre2f;
+    P.pre1f = pre1f;
     P.zweight = zweight;
     const int precision = FMF_FLAG_PRECISION_OF(a.flags);
     if (precision != FMF_PREC_FP32) {

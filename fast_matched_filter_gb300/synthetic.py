@@ -155,11 +155,12 @@ def config4(seed=104, n_templates=500, n_samples=4320000):
                 network_sum=True)
 
 
-def variable(seed=105, n_templates=100, n_samples=1080000):
+def variable(seed=105, n_templates=100, n_samples=1080000, normalize="short"):
     """Per-channel template lengths (the reference's 'variable_precise'):
     data (20, 3, 1,080,000) N(0,1); 100 Hann-tapered templates whose channels
     keep U{400..800} samples (zero-padded to 800); moveouts U{0..1000}; uniform
-    weights; step 1, short; network sum (Fisher z)."""
+    weights; step 1; network sum (Fisher z).  normalize='full' adds a DC
+    offset U(-100, 100) per channel, which the window means remove."""
     rng = np.random.default_rng(seed)
     S, C, N, T, L = 20, 3, n_samples, n_templates, 800
     data = rng.standard_normal((S, C, N), dtype=np.float32)
@@ -172,9 +173,11 @@ def variable(seed=105, n_templates=100, n_samples=1080000):
     moveouts = rng.integers(0, 1001, (T, S, C)).astype(np.int32)
     _plant(rng, data, templates, moveouts, 1, 0.5)
     weights = np.full((T, S, C), 1.0 / (S * C), dtype=np.float32)
-    return dict(name="variable_S20C3N%d_T%dL400-800" % (N, T), templates=templates,
-                moveouts=moveouts, weights=weights, data=data, step=1, normalize="short",
-                network_sum=True, n_samples_template=nt)
+    if normalize == "full":
+        data += rng.uniform(-100.0, 100.0, (S, C, 1)).astype(np.float32)
+    return dict(name="variable_S20C3N%d_T%dL400-800%s" % (N, T, "_full" if normalize == "full" else ""),
+                templates=templates, moveouts=moveouts, weights=weights, data=data, step=1,
+                normalize=normalize, network_sum=True, n_samples_template=nt)
 
 
 def variable_macs(n_samples_template, n_samples, step):

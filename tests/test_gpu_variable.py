@@ -133,6 +133,26 @@ def test_variable_tensor_core_short_channels(oracle_built, step, normalize):
     _check(got, ref, float(np.sum(w)), TOL_TC)
 
 
+@pytest.mark.parametrize("precision", ["fp32", "split_bf16"])
+def test_variable_full_with_drift(oracle_built, precision):
+    """'full' on data whose window means dominate their spread (a DC offset
+    and a slow drift 50x the noise): the centred window energies
+    S2 - S1^2 / n are formed from float-pair prefix sums in double-float
+    arithmetic and must keep float accuracy despite the cancellation."""
+    rng = np.random.default_rng(44)
+    tp, mo, w, d = random_search(45, 3, 3, 2, 160, 9000, -20, 120, zero_weights=1)
+    i = np.arange(d.shape[-1])
+    d = (d + 300.0 + 50.0 * np.sin(2 * np.pi * i / 5000.0)).astype(np.float32)
+    nt = rng.integers(60, 161, mo.shape).astype(np.int32)
+    tp = np.ascontiguousarray(tp[..., :int(nt.max())])
+    for idx in np.ndindex(nt.shape):
+        tp[idx][nt[idx]:] = 0.0
+    got = fmf.matched_filter(tp, mo, w, d, 1, n_samples_template=nt, check_zeros=False,
+                             normalize="full", precision=precision)
+    ref = oracle_built.run_oracle_variable(tp, nt, mo, w, d, 1, "full")
+    _check(got, ref, float(np.sum(w)), _tol(precision))
+
+
 def test_variable_equal_lengths_match_fixed_length_coefficients(oracle_built):
     """With every length equal to L the per-channel coefficients are the
     precise ones: atanh/tanh of a single channel recovers its coefficient."""
