@@ -232,7 +232,7 @@ int prepare_problem(const Args &a, Scratch &ws, cudaStream_t s, Problem *Pout, c
     }
     if (full) {
         template_center_kernel<<<(unsigned)((size_t)T * SC), 128, 0, s>>>(a.tpl, L, tcen, tsum);
-        channel_mean_kernel<<<SC, 256, 0, s>>>(a.data, N, mu);
+        channel_mean_kernel<<<SC, 1024, 0, s>>>(a.data, N, mu);
         count_launch(2);
     }
     if ((rc = cuda_status(cudaFuncSetAttribute(window_stats_kernel,

@@ -160,7 +160,7 @@ extern "C" int fmf_matched_filter_noalloc(const float *templates, const float *s
                                                             k_lo, k_hi);
     if (full) {
         template_center_kernel<<<(unsigned)((size_t)T * SC), 128, 0, s>>>(templates, L, tcen, tsum);
-        channel_mean_kernel<<<SC, 256, 0, s>>>(data, N, mu);
+        channel_mean_kernel<<<SC, 1024, 0, s>>>(data, N, mu);
     }
     cudaError_t e = cudaFuncSetAttribute(window_stats_kernel,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)stat_smem);

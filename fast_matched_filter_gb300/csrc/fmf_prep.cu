@@ -7,20 +7,24 @@
 //    the FP64 sum of the centred values.  sum(t*(d-m)) equals
 //    sum((t-tbar)*(d-m)) exactly, so centring changes no result; it removes
 //    the template's DC term from the products the numerator sums.
-//  * channel_mean_kernel   : "full" only -- FP64 mean of each data channel,
+//  * channel_mean_kernel   : "full" only -- mean of each data channel (double-float sum),
 //    rounded to float; d - mu is exact in FP32 wherever mu/2 <= d <= 2 mu.
 //  * template_energy_kernel: the template energies sum(t^2) when the caller
 //    passes none, computed as the reference wrapper computes them for
 //    float32 templates (numpy.sum(templates**2, axis=-1),
 //    fast_matched_filter.py:256-261): float32 squares summed in numpy's
 //    pairwise order, so the values are bit-identical.
-//  * window_stats_kernel   : FP64 sliding-window statistics of every channel
-//    for windows of L samples starting at each sample index:
+//  * window_stats_kernel   : sliding-window statistics of every channel for
+//    windows of L samples starting at each sample index:
 //      short: E = sum d^2                      (matched_filter.c:622)
 //      full : m = sum d'/L, V = sum d'^2 - (sum d')^2/L   (d' = d - mu)
-//    computed from an FP64 prefix sum local to each block of windows, so the
+//    computed from a prefix sum local to each block of windows (so the
 //    differenced values are of the size of the block's energy, not of the
-//    whole trace's.
+//    whole trace's) held as double-float pairs in FP32 arithmetic: squares
+//    split exactly by FMA, TwoSum additions with the rounding errors carried
+//    in the low word, window differences by TwoSum; about 44 significant bits,
+//    the accuracy of an FP64 scan at FP32 speed (FP64 runs at ~2 operations
+//    per clock per SM on this part, which made this kernel FP64-bound).
 #include "fmf_common.cuh"
 
 namespace fmf {
@@ -198,57 +202,86 @@ __global__ void template_center_kernel(const float *__restrict__ tpl, int L,
         tsum[row] = (float)tot;
 }
 
-// grid = SC blocks of 256 threads
+// (h, l) += (xh, xl): TwoSum of the high words, every rounding error and the
+// low words accumulated in l.
+__device__ __forceinline__ void pair_add(float &h, float &l, float xh, float xl)
+{
+    const float s = h + xh, bb = s - h;
+    l += ((h - (s - bb)) + (xh - bb)) + xl;
+    h = s;
+}
+
+// grid = SC blocks of 1024 threads: the mean of each data channel, rounded
+// to float, from double-float sums (FP32 arithmetic, fixed order).
 __global__ void channel_mean_kernel(const float *__restrict__ data, int N,
                                     float *__restrict__ mu)
 {
-    __shared__ double red[33];
+    __shared__ float2 red[32];
     const float *src = data + (size_t)blockIdx.x * N;
-    double s = 0.0;
+    float h = 0.0f, l = 0.0f;
     for (int i = threadIdx.x; i < N; i += blockDim.x)
-        s += (double)src[i];
-    double tot = block_sum_f64(s, red);
-    if (threadIdx.x == 0)
-        mu[blockIdx.x] = (float)(tot / (double)N);
+        pair_add(h, l, src[i], 0.0f);
+    for (int o = 16; o > 0; o >>= 1) {
+        const float yh = __shfl_down_sync(0xffffffffu, h, o), yl = __shfl_down_sync(0xffffffffu, l, o);
+        pair_add(h, l, yh, yl);
+    }
+    if ((threadIdx.x & 31) == 0)
+        red[threadIdx.x >> 5] = make_float2(h, l);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float th = 0.0f, tl = 0.0f;
+        for (int i = 0; i < (int)(blockDim.x >> 5); i++)
+            pair_add(th, tl, red[i].x, red[i].y);
+        mu[blockIdx.x] = (float)(((double)th + (double)tl) / (double)N);
+    }
 }
 
-// Inclusive block scan of a[1..len] (a[0] = 0) held in shared memory.
-// Each thread scans a contiguous segment serially; segment totals are
-// combined with a warp-level exclusive scan.
-__device__ void block_scan_f64(double *a, int len, double *part)
+// In-place inclusive scan of a[1..len] (a[0] = 0) as double-float pairs, by the
+// block: a contiguous segment per thread, then the segment totals by warp
+// shuffles and one thread over the warps.
+__device__ void block_scan_pair(float2 *a, int len, float2 *part)
 {
     const int nt = blockDim.x;
     const int seg = (len + nt - 1) / nt;
     const int b = 1 + threadIdx.x * seg;
     const int e = min(len + 1, b + seg);
-    double s = 0.0;
+    float h = 0.0f, l = 0.0f;
     for (int i = b; i < e; i++) {
-        s += a[i];
-        a[i] = s;
+        const float2 x = a[i];
+        pair_add(h, l, x.x, x.y);
+        a[i] = make_float2(h, l);
     }
-    // exclusive scan of per-thread totals
-    int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    double x = s;
+    // inclusive warp scan of the segment totals
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    float xh = h, xl = l;
     for (int o = 1; o < 32; o <<= 1) {
-        double y = __shfl_up_sync(0xffffffffu, x, o);
+        const float yh = __shfl_up_sync(0xffffffffu, xh, o), yl = __shfl_up_sync(0xffffffffu, xl, o);
         if (lane >= o)
-            x += y;
+            pair_add(xh, xl, yh, yl);
     }
     if (lane == 31)
-        part[wid] = x;
+        part[wid] = make_float2(xh, xl);
+    // exclusive value of this thread within its warp
+    float eh = __shfl_up_sync(0xffffffffu, xh, 1), el = __shfl_up_sync(0xffffffffu, xl, 1);
+    if (lane == 0)
+        eh = el = 0.0f;
     __syncthreads();
     if (threadIdx.x == 0) {
-        double run = 0.0;
+        float rh = 0.0f, rl = 0.0f;
         for (int i = 0; i < (nt >> 5); i++) {
-            double v = part[i];
-            part[i] = run;
-            run += v;
+            const float2 v = part[i];
+            part[i] = make_float2(rh, rl);
+            pair_add(rh, rl, v.x, v.y);
         }
     }
     __syncthreads();
-    double off = part[wid] + (x - s);
-    for (int i = b; i < e; i++)
-        a[i] += off;
+    float oh = part[wid].x, ol = part[wid].y;
+    pair_add(oh, ol, eh, el);
+    for (int i = b; i < e; i++) {
+        float2 x = a[i];
+        pair_add(x.x, x.y, oh, ol);
+        a[i] = x;
+    }
     __syncthreads();
 }
 
@@ -259,45 +292,48 @@ __global__ void window_stats_kernel(const float *__restrict__ data, int N, int L
                                     float *__restrict__ stat_e,
                                     float *__restrict__ stat_m)
 {
-    extern __shared__ double sh[];
-    __shared__ double part[33];
+    extern __shared__ float2 shp[];
+    __shared__ float2 part[33];
     const int ch = blockIdx.y;
     const long long c0 = (long long)blockIdx.x * B;
     const int len = (int)min((long long)B + L, (long long)N - c0);
     const bool full = mu != nullptr;
-    double *P2 = sh;
-    double *P1 = sh + (B + L + 1);
+    float2 *P2 = shp;
+    float2 *P1 = shp + (B + L + 1);
     const float *src = data + (size_t)ch * N + c0;
     const float m = full ? mu[ch] : 0.0f;
     for (int i = threadIdx.x; i < len; i += blockDim.x) {
-        float v = src[i] - m;
+        const float v = src[i] - m;
         if (full && i < B)
             dcen[(size_t)ch * N + c0 + i] = v;
-        P2[i + 1] = (double)v * (double)v;
+        const float sq = v * v;
+        P2[i + 1] = make_float2(sq, fmaf(v, v, -sq));  // v^2 exactly
         if (full)
-            P1[i + 1] = (double)v;
+            P1[i + 1] = make_float2(v, 0.0f);
     }
     if (threadIdx.x == 0) {
-        P2[0] = 0.0;
+        P2[0] = make_float2(0.0f, 0.0f);
         if (full)
-            P1[0] = 0.0;
+            P1[0] = make_float2(0.0f, 0.0f);
     }
     __syncthreads();
-    block_scan_f64(P2, len, part);
+    block_scan_pair(P2, len, part);
     if (full)
-        block_scan_f64(P1, len, part);
+        block_scan_pair(P1, len, part);
     const int nwin = min(B, len - L + 1);
-    const double invL = 1.0 / (double)L;
+    const float Lf = (float)L, invL = 1.0f / Lf;
     for (int u = threadIdx.x; u < nwin; u += blockDim.x) {
-        double e2 = P2[u + L] - P2[u];
-        size_t o = (size_t)ch * N + c0 + u;
+        const size_t o = (size_t)ch * N + c0 + u;
         if (full) {
-            double e1 = P1[u + L] - P1[u];
-            double v = e2 - e1 * e1 * invL;
-            stat_e[o] = (float)(v > 0.0 ? v : 0.0);
-            stat_m[o] = (float)(e1 * invL);
+            float v, mean;
+            window_centred(P2[u], P2[u + L], P1[u], P1[u + L], Lf, invL, v, mean);
+            stat_e[o] = v;
+            stat_m[o] = mean;
         } else {
-            stat_e[o] = (float)e2;
+            float e;
+            const float2 a2 = P2[u], b2 = P2[u + L];
+            const float h = two_diff(b2.x, a2.x, e);
+            stat_e[o] = h + (e + (b2.y - a2.y));
         }
     }
 }

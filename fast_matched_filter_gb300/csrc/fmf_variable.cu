@@ -322,7 +322,7 @@ static int variable_device(const VArgs &a, int L, cudaStream_t s)
                                     zweight, norm_sum, bias, scale);
     vp_template_kernel<<<(unsigned)((size_t)T * SC), 128, 0, s>>>(a.tpl, a.ntap, L, full ? 1 : 0, tmask, tsum);
     if (full)
-        channel_mean_kernel<<<SC, 256, 0, s>>>(a.data, N, mu);
+        channel_mean_kernel<<<SC, 1024, 0, s>>>(a.data, N, mu);
     prefix_block_kernel<<<dim3(nblk, SC), 256, 0, s>>>(a.data, N, mu, bs2, bs1, nblk);
     prefix_offsets_kernel<<<(SC + 127) / 128, 128, 0, s>>>(bs2, bs1, nblk, SC);
     prefix_write_kernel<<<dim3(nblk, SC), 256, 0, s>>>(a.data, N, mu, bs2, bs1, nblk, pre2f, pre1f, dcen);
