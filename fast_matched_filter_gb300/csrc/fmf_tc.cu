@@ -660,7 +660,7 @@ __global__ void __launch_bounds__(tc_threads(VAR), 1) tc_persistent(const __grid
                         const int mu = pr.mu[meta];
                         const int sres = ((mu % TC_Q) + TC_Q) % TC_Q;
                         int lphi = (P.L - phi + step - 1) / step;
-                        if (VAR) {  // per-channel length: the taps past it are zeros, skip them
+                        if constexpr (VAR) {  // per-channel length: the taps past it are zeros, skip them
                             const int n = P.ntap[(size_t)t * SC + ch];
                             const int own = n > phi ? (n - phi + step - 1) / step : 0;
                             lphi = min(lphi, own);
@@ -739,8 +739,6 @@ __global__ void __launch_bounds__(tc_threads(VAR), 1) tc_persistent(const __grid
             const uint32_t s_cols = lane_base + (uint32_t)(TC_NACC * TC_NB_MAX + a0);
             const int SC = pr.P.SC, step = pr.P.step, n_corr = pr.P.n_corr, N = pr.P.N;
             const bool full = pr.P.normalize != 0, nsum = pr.P.network_sum != 0;
-            // per-channel template lengths: FP64 prefix sums and a Fisher-z network sum
-            constexpr bool var = VAR;
             const float *__restrict__ stat_e = pr.P.stat_e;
             const float *__restrict__ stat_m = pr.P.stat_m;
             const float *__restrict__ sstp = pr.P.sst;
@@ -770,14 +768,8 @@ __global__ void __launch_bounds__(tc_threads(VAR), 1) tc_persistent(const __grid
                 const float sst = sstp[row];
                 const float ts = full ? tsump[row] : 0.0f;
                 const long long u0 = (kb + (long long)TC_Q * a0) * step + mo[ch];
-                const float *__restrict__ se = var ? nullptr : stat_e + (size_t)ch * N + u0;
-                const float *__restrict__ sm = (full && !var) ? stat_m + (size_t)ch * N + u0 : se;
-                const int ntap = var ? pr.P.ntap[row] : 0;
-                const float zw = var ? pr.P.zweight[row] : 0.0f;
-                const float2 *__restrict__ pf = var ? pr.P.pre2f + (size_t)ch * (N + 1) + u0 : nullptr;
-                const float2 *__restrict__ pg =
-                    (var && full) ? pr.P.pre1f + (size_t)ch * (N + 1) + u0 : nullptr;
-                const float nf = (float)ntap, inv_n = var ? 1.0f / nf : 0.0f;
+                const float *__restrict__ se = VAR ? nullptr : stat_e + (size_t)ch * N + u0;
+                const float *__restrict__ sm = (VAR || !full) ? se : stat_m + (size_t)ch * N + u0;
                 float *oc = outp + ((size_t)t * n_corr + kb + (long long)TC_Q * a0) * SC + ch;
                 // statistics: all loads of a chunk issued together (indices clamped into the
                 // valid range) before any use; the first chunk before waiting for the accumulator
@@ -786,19 +778,35 @@ __global__ void __launch_bounds__(tc_threads(VAR), 1) tc_persistent(const __grid
 #pragma unroll
                     for (int i = 0; i < CH; i++) {
                         const int ac = min(max(c0 + i, a_lo), a_hi - 1);
-                        e[i] = (any && !var) ? __ldg(se + ac * qs) : 0.0f;
-                        mm[i] = (any && full && !var) ? __ldg(sm + ac * qs) : 0.0f;
+                        e[i] = any ? __ldg(se + ac * qs) : 0.0f;
+                        mm[i] = (any && full) ? __ldg(sm + ac * qs) : 0.0f;
                     }
                 };
-                load_chunk(0);
+                if constexpr (!VAR)
+                    load_chunk(0);
+                // per-channel lengths: the channel's own length and Fisher-z weight, its
+                // prefix-sum pairs (d^2, and d for full) at the first window of the thread
+                [[maybe_unused]] int ntap = 0;
+                [[maybe_unused]] float zw = 0.0f, nf = 0.0f, inv_n = 0.0f;
+                [[maybe_unused]] const float2 *pf = nullptr, *pg = nullptr;
+                if constexpr (VAR) {
+                    ntap = pr.P.ntap[row];
+                    zw = pr.P.zweight[row];
+                    pf = pr.P.pre2f + (size_t)ch * (N + 1) + u0;
+                    pg = full ? pr.P.pre1f + (size_t)ch * (N + 1) + u0 : nullptr;
+                    nf = (float)ntap;
+                    inv_n = 1.0f / nf;
+                }
                 if (!mbar_wait_warp(dfull0 + 8 * d, (c / TC_NACC) & 1, abort_flag, B.err, 16u))
                     goto epilogue_done;
                 tc_fence_after();
                 const uint32_t dcols = lane_base + (uint32_t)(d * TC_NB_MAX + a0);
 #pragma unroll 1
                 for (int c0 = 0; c0 < NC; c0 += CH) {
-                    if (c0 > 0)
-                        load_chunk(c0);
+                    if constexpr (!VAR) {
+                        if (c0 > 0)
+                            load_chunk(c0);
+                    }
                     float x[CH], sv[CH];
                     tmem_ldc<CH>(dcols + c0, x);
                     if (nsum && !first)
@@ -810,7 +818,7 @@ __global__ void __launch_bounds__(tc_threads(VAR), 1) tc_persistent(const __grid
                         if (lane == 0)
                             mbar_arrive(dempty0 + 8 * d);
                     }
-                    if (var) {
+                    if constexpr (VAR) {
                         // window sums of the channel's own length from the FP64 prefix sums,
                         // the 'precise' threshold on the square root, and
                         // atanh(cc - 10 eps) * z into the network sum
