@@ -48,6 +48,7 @@
 // Every wait is bounded (globaltimer); on timeout the CTA raises an error
 // word, stops issuing, waits for its own copies/MMAs (bounded) and frees TMEM.
 #include <cfloat>
+#include <type_traits>
 
 #include <cuda_bf16.h>
 
@@ -421,22 +422,23 @@ __device__ __forceinline__ float rsqrt_ftz(float x)
 //    with m in [sqrt(1/2), sqrt(2)) and ln(m) = 2 atanh(s), s = (m - 1) / (m + 1),
 //    |s| <= 0.1716, from the same series to s^9/9;
 //  |y| = 1 gives +-inf, |y| > 1 and NaN give NaN.
-__device__ __forceinline__ float fisher_atanh(float y)
+__device__ __forceinline__ float atanh_series(float y)
+{
+    const float z = y * y;
+    float p = fmaf(1.0f / 13.0f, z, 1.0f / 11.0f);
+    p = fmaf(p, z, 1.0f / 9.0f);
+    p = fmaf(p, z, 1.0f / 7.0f);
+    p = fmaf(p, z, 1.0f / 5.0f);
+    p = fmaf(p, z, 1.0f / 3.0f);
+    return fmaf(y * z, p, y);
+}
+
+__device__ __forceinline__ float atanh_reduced(float y)
 {
     const float a = fabsf(y);
-    float r;
-    if (a <= 0.25f) {
-        const float z = y * y;
-        float p = fmaf(1.0f / 13.0f, z, 1.0f / 11.0f);
-        p = fmaf(p, z, 1.0f / 9.0f);
-        p = fmaf(p, z, 1.0f / 7.0f);
-        p = fmaf(p, z, 1.0f / 5.0f);
-        p = fmaf(p, z, 1.0f / 3.0f);
-        return fmaf(y * z, p, y);
-    }
     if (!(a < 1.0f))  // 1, above 1, NaN
         return a == 1.0f ? copysignf(INFINITY, y) : __int_as_float(0x7fc00000);
-    const float q = __fdividef(1.0f + a, 1.0f - a);  // in (5/3, 2^25]
+    const float q = __fdividef(1.0f + a, 1.0f - a);  // in (5/3, 2^25] for a > 1/4
     const int bits = __float_as_int(q);
     const int k = (bits - 0x3f3504f3) >> 23;  // 0x3f3504f3 = sqrt(1/2)
     const float m = __int_as_float(bits - (k << 23));
@@ -445,17 +447,33 @@ __device__ __forceinline__ float fisher_atanh(float y)
     float p = fmaf(1.0f / 9.0f, z, 1.0f / 7.0f);
     p = fmaf(p, z, 1.0f / 5.0f);
     p = fmaf(p, z, 1.0f / 3.0f);
-    r = fmaf(s * z, p, s);                               // ln(m) / 2
+    float r = fmaf(s * z, p, s);                         // ln(m) / 2
     r = fmaf((float)k, 0.5f * 0.693145751953125f, r);    // + k ln2 / 2 (ln2 in two parts)
     r = fmaf((float)k, 0.5f * 1.4286068203094172e-06f, r);
     return copysignf(r, y);
 }
 
+// Called by all 32 lanes of a warp together: the series on every lane, the
+// reduction only when some lane of the warp needs it (no divergent branch;
+// the common case, every |y| <= 1/4, skips it).
+__device__ __forceinline__ float fisher_atanh(float y)
+{
+    const bool big = !(fabsf(y) <= 0.25f);  // NaN included
+    float r = atanh_series(y);
+    if (__any_sync(0xffffffffu, big)) {
+        const float g = atanh_reduced(y);
+        r = big ? g : r;
+    }
+    return r;
+}
+
+// every lane of every warp takes part (the tail reads a dummy value)
 __global__ void fisher_atanh_kernel(const float *__restrict__ y, float *__restrict__ out, long long n)
 {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const float r = fisher_atanh(i < n ? y[i] : 0.0f);
     if (i < n)
-        out[i] = fisher_atanh(y[i]);
+        out[i] = r;
 }
 
 int launch_fisher_atanh(const float *y, float *out, long long n, cudaStream_t s)
@@ -822,57 +840,66 @@ __global__ void __launch_bounds__(tc_threads(VAR), 1) tc_persistent(const __grid
                         // window sums of the channel's own length from the FP64 prefix sums,
                         // the 'precise' threshold on the square root, and
                         // atanh(cc - 10 eps) * z into the network sum
-                        auto var_value = [&](int i, float num, float ssd) {
-                            const int a = c0 + i;
-                            // the threshold on sqrt(sst * ssd), as p * rsqrt(p); p = 0 gives
-                            // NaN there, and p below the normal range (flushed) cannot pass it
-                            const float p = sst * ssd, r = rsqrt_ftz(p);
-                            const float cc = p * r > kThreshold ? num * r : 0.0f;
-                            const float prev = first ? 0.0f : sv[i];
-                            sv[i] = (interior || (a >= a_lo && a < a_hi))
-                                        ? fmaf(fisher_atanh(cc - 10.0f * FLT_EPSILON), zw, prev)
-                                        : prev;
-                        };
-                        // element offsets of the windows (32-bit: at most NB * Q * step)
-                        auto off = [&](int i) {
-                            return (interior ? c0 + i : min(max(c0 + i, a_lo), a_hi - 1)) * qs32;
-                        };
-                        if (!full) {  // hi + lo float prefix pairs: FP32 only
-                            const float2 *__restrict__ pf_hi = pf + ntap;
+                        // CHECK: some output of the warp lies outside the valid lags (clamped
+                        // indices, masked sums); otherwise every one is valid
+                        auto var_chunk = [&](auto check) {
+                            constexpr bool CHECK = decltype(check)::value;
+                            auto var_value = [&](int i, float num, float ssd) {
+                                const int a = c0 + i;
+                                // the threshold on sqrt(sst * ssd), as p * rsqrt(p); p = 0 gives
+                                // NaN there, and p below the normal range (flushed) cannot pass it
+                                const float p = sst * ssd, r = rsqrt_ftz(p);
+                                const float cc = p * r > kThreshold ? num * r : 0.0f;
+                                const float prev = first ? 0.0f : sv[i];
+                                const float z = fmaf(fisher_atanh(cc - 10.0f * FLT_EPSILON), zw, prev);
+                                sv[i] = (!CHECK || (a >= a_lo && a < a_hi)) ? z : prev;
+                            };
+                            // element offsets of the windows (32-bit: at most NB * Q * step)
+                            auto off = [&](int i) {
+                                return (CHECK ? min(max(c0 + i, a_lo), a_hi - 1) : c0 + i) * qs32;
+                            };
+                            const bool ld = !CHECK || any;
+                            const float2 z2 = make_float2(0.0f, 0.0f);
+                            if (!full) {  // hi + lo float prefix pairs: FP32 only
+                                const float2 *__restrict__ pf_hi = pf + ntap;
 #pragma unroll
-                            for (int h = 0; h < CH; h += 4) {  // loads of 4 values, then their use
-                                float2 lo[4], hi[4];
+                                for (int h = 0; h < CH; h += 4) {  // loads of 4 values, then their use
+                                    float2 lo[4], hi[4];
 #pragma unroll
-                                for (int j = 0; j < 4; j++) {
-                                    const int o = off(h + j);
-                                    lo[j] = any ? pf[o] : make_float2(0.0f, 0.0f);
-                                    hi[j] = any ? pf_hi[o] : make_float2(0.0f, 0.0f);
+                                    for (int j = 0; j < 4; j++) {
+                                        const int o = off(h + j);
+                                        lo[j] = ld ? pf[o] : z2;
+                                        hi[j] = ld ? pf_hi[o] : z2;
+                                    }
+#pragma unroll
+                                    for (int j = 0; j < 4; j++)
+                                        var_value(h + j, x[h + j], window_energy(lo[j], hi[j]));
                                 }
+                            } else {  // centred windows: double-float FP32 arithmetic
 #pragma unroll
-                                for (int j = 0; j < 4; j++)
-                                    var_value(h + j, x[h + j], window_energy(lo[j], hi[j]));
+                                for (int h = 0; h < CH; h += 2) {
+                                    float2 lo2[2], hi2[2], lo1[2], hi1[2];
+#pragma unroll
+                                    for (int j = 0; j < 2; j++) {
+                                        const int o = off(h + j);
+                                        lo2[j] = ld ? pf[o] : z2;
+                                        hi2[j] = ld ? pf[o + ntap] : z2;
+                                        lo1[j] = ld ? pg[o] : z2;
+                                        hi1[j] = ld ? pg[o + ntap] : z2;
+                                    }
+#pragma unroll
+                                    for (int j = 0; j < 2; j++) {
+                                        float v, mean;
+                                        window_centred(lo2[j], hi2[j], lo1[j], hi1[j], nf, inv_n, v, mean);
+                                        var_value(h + j, fmaf(-mean, ts, x[h + j]), v);
+                                    }
+                                }
                             }
-                        } else {  // centred windows: double-float FP32 arithmetic
-#pragma unroll
-                            for (int h = 0; h < CH; h += 2) {
-                                float2 lo2[2], hi2[2], lo1[2], hi1[2];
-#pragma unroll
-                                for (int j = 0; j < 2; j++) {
-                                    const int o = off(h + j);
-                                    const float2 z2 = make_float2(0.0f, 0.0f);
-                                    lo2[j] = any ? pf[o] : z2;
-                                    hi2[j] = any ? pf[o + ntap] : z2;
-                                    lo1[j] = any ? pg[o] : z2;
-                                    hi1[j] = any ? pg[o + ntap] : z2;
-                                }
-#pragma unroll
-                                for (int j = 0; j < 2; j++) {
-                                    float v, mean;
-                                    window_centred(lo2[j], hi2[j], lo1[j], hi1[j], nf, inv_n, v, mean);
-                                    var_value(h + j, fmaf(-mean, ts, x[h + j]), v);
-                                }
-                            }
-                        }
+                        };
+                        if (interior)
+                            var_chunk(std::false_type{});
+                        else
+                            var_chunk(std::true_type{});
                     } else if (nsum && interior) {
                         // every output of the warp is valid: no per-value range test
                         if (first) {
