@@ -44,6 +44,7 @@ static int clear_error()
 }
 
 void count_launch(int n) { g_launches += n; }
+void reset_launch_count() { g_launches = 0; }
 
 // ---------------------------------------------------------------- event timing
 // Opt-in (fmf_timing_begin/end): every call records CUDA events on its stream
@@ -273,6 +274,7 @@ int prepare_problem(const Args &a, Scratch &ws, cudaStream_t s, Problem *Pout, c
     P.pre2f = nullptr;
     P.pre1f = nullptr;
     P.zweight = nullptr;
+    P.vp_norm = P.vp_bias = P.vp_scale = nullptr;
 
     if (!P.network_sum) {
         size_t bytes = (size_t)T * a.n_corr * SC * sizeof(float);
@@ -951,6 +953,7 @@ int fmf_selftest_wait_timeout(unsigned ms)
 int fmf_eval_atanh(const float *y, float *out, size_t n, void *stream)
 {
     fmf::clear_error();
+    fmf::reset_launch_count();
     if (n > 0 && (!y || !out))
         return fmf::set_error(FMF_ERR_ARG, "null array argument");
     if (n > ((size_t)1 << 40))

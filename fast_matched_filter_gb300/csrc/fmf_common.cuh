@@ -45,6 +45,9 @@ struct Problem {
     const float2 *pre2f;  // (SC, N+1) prefix sums of d^2 (centred d for full) as hi + lo floats
     const float2 *pre1f;  // (SC, N+1) prefix sums of centred d as hi + lo floats (full), else null
     const float *zweight; // (T, SC) Fisher-z weight of each channel
+    // (T) each, or null: when set, the tensor-core kernel writes
+    // (tanh(x / vp_norm[t]) + vp_bias[t]) * vp_scale[t] for every output x
+    const float *vp_norm, *vp_bias, *vp_scale;
 };
 
 #ifdef __CUDACC__
@@ -98,6 +101,7 @@ __device__ __forceinline__ void window_centred(float2 a2, float2 b2, float2 a1, 
 namespace fmf {
 int set_error(int status, const char *fmt, ...);
 void count_launch(int n = 1);
+void reset_launch_count();  // at the start of every entry point (fmf_last_launch_count)
 int check_launch(const char *what);
 
 // Stream-ordered scratch allocations (cudaMallocAsync from the device's

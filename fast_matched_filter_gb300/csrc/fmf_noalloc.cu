@@ -112,6 +112,7 @@ extern "C" int fmf_matched_filter_noalloc(const float *templates, const float *s
 {
     using namespace fmf;
     set_error(FMF_OK, "");
+    reset_launch_count();
     if (!templates || !sum_square_templates || !moveouts || !data || !weights || !cc_out)
         return set_error(FMF_ERR_ARG, "noalloc: null array argument");
     if (step < 1 || n_samples_template < 1 || n_templates < 1 || n_stations < 1 ||
@@ -203,6 +204,7 @@ extern "C" int fmf_matched_filter_noalloc(const float *templates, const float *s
     P.pre2f = nullptr;
     P.pre1f = nullptr;
     P.zweight = nullptr;
+    P.vp_norm = P.vp_bias = P.vp_scale = nullptr;
     for (int t0 = 0; t0 < T; t0 += 65535) {
         Problem Q = P;
         const int nt = T - t0 < 65535 ? T - t0 : 65535;

@@ -952,11 +952,22 @@ __global__ void __launch_bounds__(tc_threads(VAR), 1) tc_persistent(const __grid
                         tmem_ldc<CH>(s_cols + c0, sv);
                         tmem_wait_ld();
                     }
+                    if constexpr (VAR) {  // the Fisher-z transform of every output, fused
+                        const float zn = pr.P.vp_norm[t], zb = pr.P.vp_bias[t], zs = pr.P.vp_scale[t];
 #pragma unroll
-                    for (int i = 0; i < CH; i++) {
-                        const int a = c0 + i;
-                        if ((long long)a * TC_Q < lim)
-                            o[(size_t)a * TC_Q] = (!first && a >= a_lo && a < a_hi) ? sv[i] : 0.0f;
+                        for (int i = 0; i < CH; i++) {
+                            const int a = c0 + i;
+                            const float x = (!first && a >= a_lo && a < a_hi) ? sv[i] : 0.0f;
+                            if ((long long)a * TC_Q < lim)
+                                o[(size_t)a * TC_Q] = (tanhf(x / zn) + zb) * zs;
+                        }
+                    } else {
+#pragma unroll
+                        for (int i = 0; i < CH; i++) {
+                            const int a = c0 + i;
+                            if ((long long)a * TC_Q < lim)
+                                o[(size_t)a * TC_Q] = (!first && a >= a_lo && a < a_hi) ? sv[i] : 0.0f;
+                        }
                     }
                 }
             }
@@ -1160,6 +1171,15 @@ void tc_subset(const TcProb *full, int t0, int nt, TcProb *out)
     q.P.w += o;
     q.P.k_lo += t0;
     q.P.k_hi += t0;
+    if (q.P.ntap)
+        q.P.ntap += o;
+    if (q.P.zweight)
+        q.P.zweight += o;
+    if (q.P.vp_norm) {
+        q.P.vp_norm += t0;
+        q.P.vp_bias += t0;
+        q.P.vp_scale += t0;
+    }
     q.P.out += (size_t)t0 * q.P.n_corr * (q.P.network_sum ? 1 : SC);
     q.P.T = nt;
     q.w_hi += o * step * q.NW * 64;

@@ -15,7 +15,9 @@
 // stop = N - L - max(0, max mo) - step (matched_filter.c:384-385); the final
 // transform applies to every output (matched_filter.c:405-408).
 //
-// Kernels: metadata (one thread, the reference's float accumulation order),
+// Kernels: metadata (Fisher-z weights per (t, ch), lag ranges and weight sums
+// per template, the cumulative scale in one thread, each in the reference's
+// float operation order),
 // masked/centred templates, FP64 prefix sums of d^2 and d stored as float
 // pairs (global, so that any window length is a few FP32 operations), the
 // numerator kernel with its
@@ -36,50 +38,79 @@ int launch_tc(const Problem &P, const float *data_for_tc, int precision, unsigne
               cudaStream_t s, int forced_nb, int template_group);
 int collect_device_errors();
 
-// One thread: lag range, Fisher-z weights and the transform constants of
-// every template, in the reference's order of float operations.
-__global__ void vp_meta_kernel(const int *__restrict__ mo, const float *__restrict__ w,
-                               const int *__restrict__ ntap, int T, int SC, int L, int N, int step,
-                               int n_corr, int *k_lo, int *k_hi, float *zweight, float *norm_sum,
-                               float *bias, float *scale)
+// Fisher-z weight of every (t, ch), one thread each, in the reference's mix
+// of float and double operations: z = sqrt(n - 3) * w as
+// 1 / sqrt(1 / (n - 3)) * w.
+__global__ void vp_zweight_kernel(const float *__restrict__ w, const int *__restrict__ ntap, long long n,
+                                  float *__restrict__ zweight)
 {
-    if (threadIdx.x != 0 || blockIdx.x != 0)
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n)
+        zweight[i] = (float)(1.0 / (double)sqrtf((float)(1.0 / (double)(ntap[i] - 3))) * (double)w[i]);
+}
+
+// One thread per template: lag range, sum of the Fisher-z weights (channel
+// order, float), used-channel bias.
+__global__ void vp_meta_kernel(const int *__restrict__ mo, const float *__restrict__ w,
+                               const float *__restrict__ zweight, int T, int SC, int L, int N, int step,
+                               int n_corr, int *k_lo, int *k_hi, float *norm_sum, float *bias)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= T)
         return;
+    const int *m = mo + (size_t)t * SC;
+    const float *wt = w + (size_t)t * SC;
+    const float *zt = zweight + (size_t)t * SC;
+    int lo = 0, hi = 0, used = 0;
+    float zs = 0.0f;
+    for (int ch = 0; ch < SC; ch++) {
+        lo = min(lo, m[ch]);
+        hi = max(hi, m[ch]);
+        if (wt[ch] != 0.0f)
+            used += 1;
+        zs += zt[ch];
+    }
+    const long long start = (long long)(int)ceilf((float)abs(lo) / (float)step) * step;
+    const long long stop = (long long)N - L - hi - step;
+    long long a = 0, b = 0;
+    if (stop > start) {
+        a = start / step;
+        b = (stop - 1) / step + 1;
+        if (b > n_corr)
+            b = n_corr;
+        if (a > b)
+            a = b;
+    }
+    k_lo[t] = (int)a;
+    k_hi[t] = (int)b;
+    norm_sum[t] = zs;
+    bias[t] = used * FLT_EPSILON * 10;
+}
+
+// scale[t] = the reference's max_cc after template t: one float sum of the
+// weights of templates 0..t in (t, ch) order (never reset,
+// matched_filter.c:329,365).  One block: the weights pass through shared
+// memory in chunks, thread 0 adds them in order.
+constexpr int kScaleChunk = 8192;
+__global__ void vp_scale_kernel(const float *__restrict__ w, int T, int SC, float *__restrict__ scale)
+{
+    __shared__ float buf[kScaleChunk];
+    const long long n = (long long)T * SC;
     float max_cc = 0.0f;
-    for (int t = 0; t < T; t++) {
-        const int *m = mo + (size_t)t * SC;
-        const float *wt = w + (size_t)t * SC;
-        const int *nt = ntap + (size_t)t * SC;
-        int lo = 0, hi = 0, used = 0;
-        for (int ch = 0; ch < SC; ch++) {
-            lo = min(lo, m[ch]);
-            hi = max(hi, m[ch]);
-            max_cc += wt[ch];
-            if (wt[ch] != 0.0f)
-                used += 1;
+    for (long long c0 = 0; c0 < n; c0 += kScaleChunk) {
+        const int len = (int)min((long long)kScaleChunk, n - c0);
+        __syncthreads();
+        for (int i = threadIdx.x; i < len; i += blockDim.x)
+            buf[i] = w[c0 + i];
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            for (int i = 0; i < len; i++) {
+                max_cc += buf[i];
+                const long long g = c0 + i;
+                if ((g + 1) % SC == 0)
+                    scale[g / SC] = max_cc;
+            }
         }
-        float zs = 0.0f;
-        for (int ch = 0; ch < SC; ch++) {
-            const float z = (float)(1.0 / (double)sqrtf((float)(1.0 / (double)(nt[ch] - 3))) * (double)wt[ch]);
-            zweight[(size_t)t * SC + ch] = z;
-            zs += z;
-        }
-        const long long start = (long long)(int)ceilf((float)abs(lo) / (float)step) * step;
-        const long long stop = (long long)N - L - hi - step;
-        long long a = 0, b = 0;
-        if (stop > start) {
-            a = start / step;
-            b = (stop - 1) / step + 1;
-            if (b > n_corr)
-                b = n_corr;
-            if (a > b)
-                a = b;
-        }
-        k_lo[t] = (int)a;
-        k_hi[t] = (int)b;
-        norm_sum[t] = zs;
-        bias[t] = used * FLT_EPSILON * 10;
-        scale[t] = max_cc;
     }
 }
 
@@ -318,15 +349,18 @@ static int variable_device(const VArgs &a, int L, cudaStream_t s)
     int *k_hi = k_lo + T;
     float *norm_sum = consts, *bias = consts + T, *scale = consts + 2 * T;
 
-    vp_meta_kernel<<<1, 32, 0, s>>>(a.mo, a.w, a.ntap, T, SC, L, N, (int)a.step, (int)a.n_corr, k_lo, k_hi,
-                                    zweight, norm_sum, bias, scale);
+    const long long n_tc = (long long)T * SC;
+    vp_zweight_kernel<<<(unsigned)((n_tc + 255) / 256), 256, 0, s>>>(a.w, a.ntap, n_tc, zweight);
+    vp_meta_kernel<<<(T + 127) / 128, 128, 0, s>>>(a.mo, a.w, zweight, T, SC, L, N, (int)a.step,
+                                                   (int)a.n_corr, k_lo, k_hi, norm_sum, bias);
+    vp_scale_kernel<<<1, 256, 0, s>>>(a.w, T, SC, scale);
     vp_template_kernel<<<(unsigned)((size_t)T * SC), 128, 0, s>>>(a.tpl, a.ntap, L, full ? 1 : 0, tmask, tsum);
     if (full)
         channel_mean_kernel<<<SC, 1024, 0, s>>>(a.data, N, mu);
     prefix_block_kernel<<<dim3(nblk, SC), 256, 0, s>>>(a.data, N, mu, bs2, bs1, nblk);
     prefix_offsets_kernel<<<(SC + 127) / 128, 128, 0, s>>>(bs2, bs1, nblk, SC);
     prefix_write_kernel<<<dim3(nblk, SC), 256, 0, s>>>(a.data, N, mu, bs2, bs1, nblk, pre2f, pre1f, dcen);
-    count_launch(full ? 6 : 5);
+    count_launch(full ? 8 : 7);
     if ((rc = check_launch("variable-length preprocessing")))
         return rc;
 
@@ -356,18 +390,23 @@ static int variable_device(const VArgs &a, int L, cudaStream_t s)
     P.pre2f = pre2f;
     P.pre1f = pre1f;
     P.zweight = zweight;
+    P.vp_norm = P.vp_bias = P.vp_scale = nullptr;
     const int precision = FMF_FLAG_PRECISION_OF(a.flags);
     if (precision != FMF_PREC_FP32) {
         unsigned *err = nullptr;
         const int forced = ((a.flags >> 8) & 0xff) * 16;
         if (forced != 0 && forced != 32 && forced != 64 && forced != 128)
             return set_error(FMF_ERR_ARG, "tensor-core tile of %d lag blocks (32, 64 or 128)", forced);
+        P.vp_norm = norm_sum;  // the final transform fused into the output write
+        P.vp_bias = bias;
+        P.vp_scale = scale;
         if ((rc = device_error_word(&err)) ||
             (rc = launch_tc(P, P.data, precision, err, ws, s, forced, (a.flags >> 16) & 0xff)))
             return rc;
-    } else if ((rc = launch_plain_all(P, s))) {
-        return rc;
+        return FMF_OK;
     }
+    if ((rc = launch_plain_all(P, s)))
+        return rc;
     const long long n = (long long)T * a.n_corr;
     vp_finalize_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(a.out, T, (int)a.n_corr, norm_sum, bias,
                                                                    scale);
@@ -378,6 +417,7 @@ static int variable_device(const VArgs &a, int L, cudaStream_t s)
 static int variable_entry(const VArgs &a, void *stream)
 {
     set_error(FMF_OK, "");
+    reset_launch_count();
     if (!a.tpl || !a.sst || !a.mo || !a.data || !a.w || !a.ntap || !a.out)
         return set_error(FMF_ERR_ARG, "null array argument");
     if (a.step < 1 || a.T < 1 || a.S < 1 || a.C < 1 || a.n_corr < 1 || a.N < 1)
