@@ -63,6 +63,22 @@ __device__ __forceinline__ float two_diff(float a, float b, float &e)
     return s;
 }
 
+// (h, l) += (xh, xl): TwoSum of the high words, every rounding error and the
+// low words accumulated in l (not renormalised).
+__device__ __forceinline__ void pair_add(float &h, float &l, float xh, float xl)
+{
+    const float s = h + xh, bb = s - h;
+    l += ((h - (s - bb)) + (xh - bb)) + xl;
+    h = s;
+}
+
+// The pair (h, l) as hi = fl(h + l), lo = the rest (|h| >= |l|).
+__device__ __forceinline__ float2 pair_normalise(float h, float l)
+{
+    const float hi = h + l;
+    return make_float2(hi, l - (hi - h));
+}
+
 // 'short': sum of d^2 over the window [a, b) = (hi_b - hi_a) + (lo_b - lo_a).
 __device__ __forceinline__ float window_energy(float2 pa, float2 pb)
 {

@@ -202,15 +202,6 @@ __global__ void template_center_kernel(const float *__restrict__ tpl, int L,
         tsum[row] = (float)tot;
 }
 
-// (h, l) += (xh, xl): TwoSum of the high words, every rounding error and the
-// low words accumulated in l.
-__device__ __forceinline__ void pair_add(float &h, float &l, float xh, float xl)
-{
-    const float s = h + xh, bb = s - h;
-    l += ((h - (s - bb)) + (xh - bb)) + xl;
-    h = s;
-}
-
 // grid = SC blocks of 1024 threads: the mean of each data channel, rounded
 // to float, from double-float sums (FP32 arithmetic, fixed order).
 __global__ void channel_mean_kernel(const float *__restrict__ data, int N,

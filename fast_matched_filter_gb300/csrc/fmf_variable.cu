@@ -168,76 +168,86 @@ __global__ void vp_template_kernel(const float *__restrict__ tpl, const int *__r
 
 constexpr int kPrefixBlock = 2048;
 
-// Phase 1, grid (blocks, SC): FP64 block sums of d'^2 and d' (d' = d - mu).
+// Prefix sums of d'^2 and d' (d' = d - mu) per channel in three phases, all in
+// double-float FP32 arithmetic (squares split exactly by FMA, TwoSum
+// additions; FP64 runs at ~2 operations per clock per SM on this part):
+// block sums, their exclusive scan per channel, then the scan inside each
+// block plus its offset.  Stored as normalised float pairs hi = fl(P),
+// lo = P - hi (~44-48 significant bits), so that the correlation epilogues
+// form window sums in FP32 arithmetic, exact to float rounding while the
+// window holds more than ~2^-24 of the channel's energy up to that point.
+
+// Phase 1, grid (blocks, SC), 256 threads: block sums.
 __global__ void prefix_block_kernel(const float *__restrict__ data, int N, const float *__restrict__ mu,
-                                    double *__restrict__ bs2, double *__restrict__ bs1, int nblk)
+                                    float2 *__restrict__ bs2, float2 *__restrict__ bs1, int nblk)
 {
-    __shared__ double r2[32], r1[32];
+    __shared__ float2 r2[32], r1[32];
     const int ch = blockIdx.y, blk = blockIdx.x;
     const float m = mu ? mu[ch] : 0.0f;
     const float *src = data + (size_t)ch * N;
-    double s2 = 0.0, s1 = 0.0;
+    float h2 = 0.0f, l2 = 0.0f, h1 = 0.0f, l1 = 0.0f;
     for (int i = blk * kPrefixBlock + threadIdx.x; i < min(N, (blk + 1) * kPrefixBlock); i += blockDim.x) {
-        const float v = src[i] - m;
-        s2 += (double)v * (double)v;
-        s1 += (double)v;
+        const float v = src[i] - m, sq = v * v;
+        pair_add(h2, l2, sq, fmaf(v, v, -sq));
+        pair_add(h1, l1, v, 0.0f);
     }
     for (int o = 16; o > 0; o >>= 1) {
-        s2 += __shfl_down_sync(0xffffffffu, s2, o);
-        s1 += __shfl_down_sync(0xffffffffu, s1, o);
+        const float a = __shfl_down_sync(0xffffffffu, h2, o), b = __shfl_down_sync(0xffffffffu, l2, o);
+        const float c = __shfl_down_sync(0xffffffffu, h1, o), d = __shfl_down_sync(0xffffffffu, l1, o);
+        pair_add(h2, l2, a, b);
+        pair_add(h1, l1, c, d);
     }
     if ((threadIdx.x & 31) == 0) {
-        r2[threadIdx.x >> 5] = s2;
-        r1[threadIdx.x >> 5] = s1;
+        r2[threadIdx.x >> 5] = make_float2(h2, l2);
+        r1[threadIdx.x >> 5] = make_float2(h1, l1);
     }
     __syncthreads();
     if (threadIdx.x == 0) {
-        double a = 0.0, b = 0.0;
+        float a = 0.0f, b = 0.0f, c = 0.0f, d = 0.0f;
         for (int i = 0; i < (int)(blockDim.x >> 5); i++) {
-            a += r2[i];
-            b += r1[i];
+            pair_add(a, b, r2[i].x, r2[i].y);
+            pair_add(c, d, r1[i].x, r1[i].y);
         }
-        bs2[(size_t)ch * nblk + blk] = a;
-        bs1[(size_t)ch * nblk + blk] = b;
+        bs2[(size_t)ch * nblk + blk] = pair_normalise(a, b);
+        bs1[(size_t)ch * nblk + blk] = pair_normalise(c, d);
     }
 }
 
-// Phase 2, one thread per channel: exclusive scan of the block sums.
-__global__ void prefix_offsets_kernel(double *bs2, double *bs1, int nblk, int SC)
+// Phase 2, one thread per channel: exclusive scan of the block sums
+// (renormalised at every step).
+__global__ void prefix_offsets_kernel(float2 *bs2, float2 *bs1, int nblk, int SC)
 {
     const int ch = blockIdx.x * blockDim.x + threadIdx.x;
     if (ch >= SC)
         return;
-    double a = 0.0, b = 0.0;
+    float2 a = make_float2(0.0f, 0.0f), b = make_float2(0.0f, 0.0f);
     for (int i = 0; i < nblk; i++) {
-        const double x = bs2[(size_t)ch * nblk + i], y = bs1[(size_t)ch * nblk + i];
+        const float2 x = bs2[(size_t)ch * nblk + i], y = bs1[(size_t)ch * nblk + i];
         bs2[(size_t)ch * nblk + i] = a;
         bs1[(size_t)ch * nblk + i] = b;
-        a += x;
-        b += y;
+        pair_add(a.x, a.y, x.x, x.y);
+        a = pair_normalise(a.x, a.y);
+        pair_add(b.x, b.y, y.x, y.y);
+        b = pair_normalise(b.x, b.y);
     }
 }
 
 // Phase 3, grid (blocks, SC), 256 threads: inclusive scan of the block plus
 // its offset -> P2[ch][i + 1] = sum_{x <= i} d'^2 (P2[ch][0] = 0) and, for
-// 'full', P1 of d' and the centred data.  Each FP64 prefix P is stored as the
-// float pair hi = fl(P), lo = fl(P - hi): about 48 significant bits, so that
-// the correlation epilogues form window sums in FP32 arithmetic only (FP64 is
-// slow on this part), exact to float rounding while the window holds more
-// than ~2^-24 of the channel's energy up to that point.
+// 'full', P1 of d' and the centred data.
 __global__ void prefix_write_kernel(const float *__restrict__ data, int N, const float *__restrict__ mu,
-                                    const double *__restrict__ bs2, const double *__restrict__ bs1,
+                                    const float2 *__restrict__ bs2, const float2 *__restrict__ bs1,
                                     int nblk, float2 *__restrict__ pre2f, float2 *__restrict__ pre1f,
                                     float *__restrict__ dcen)
 {
-    __shared__ double part2[32], part1[32];
+    __shared__ float2 part2[32], part1[32];
     const int ch = blockIdx.y, blk = blockIdx.x;
     const float m = mu ? mu[ch] : 0.0f;
     const float *src = data + (size_t)ch * N;
     const int i0 = blk * kPrefixBlock;
-    const int per = kPrefixBlock / 256;  // 8 consecutive samples per thread
-    double v2[kPrefixBlock / 256], v1[kPrefixBlock / 256];
-    double s2 = 0.0, s1 = 0.0;
+    constexpr int per = kPrefixBlock / 256;  // 8 consecutive samples per thread
+    float2 v2[per], v1[per];                 // running pairs of this thread
+    float h2 = 0.0f, l2 = 0.0f, h1 = 0.0f, l1 = 0.0f;
 #pragma unroll
     for (int e = 0; e < per; e++) {
         const int i = i0 + threadIdx.x * per + e;
@@ -247,44 +257,49 @@ __global__ void prefix_write_kernel(const float *__restrict__ data, int N, const
             if (dcen)
                 dcen[(size_t)ch * N + i] = v;
         }
-        s2 += (double)v * (double)v;
-        s1 += (double)v;
-        v2[e] = s2;
-        v1[e] = s1;
+        const float sq = v * v;
+        pair_add(h2, l2, sq, fmaf(v, v, -sq));
+        pair_add(h1, l1, v, 0.0f);
+        v2[e] = make_float2(h2, l2);
+        v1[e] = make_float2(h1, l1);
     }
-    // exclusive scan of the per-thread totals
+    // inclusive warp scan of the thread totals, then the exclusive value of this thread
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    double x2 = s2, x1 = s1;
+    float x2 = h2, y2 = l2, x1 = h1, y1 = l1;
     for (int o = 1; o < 32; o <<= 1) {
-        const double y2 = __shfl_up_sync(0xffffffffu, x2, o), y1 = __shfl_up_sync(0xffffffffu, x1, o);
+        const float a = __shfl_up_sync(0xffffffffu, x2, o), b = __shfl_up_sync(0xffffffffu, y2, o);
+        const float c = __shfl_up_sync(0xffffffffu, x1, o), d = __shfl_up_sync(0xffffffffu, y1, o);
         if (lane >= o) {
-            x2 += y2;
-            x1 += y1;
+            pair_add(x2, y2, a, b);
+            pair_add(x1, y1, c, d);
         }
     }
     if (lane == 31) {
-        part2[wid] = x2;
-        part1[wid] = x1;
+        part2[wid] = make_float2(x2, y2);
+        part1[wid] = make_float2(x1, y1);
     }
+    float e2h = __shfl_up_sync(0xffffffffu, x2, 1), e2l = __shfl_up_sync(0xffffffffu, y2, 1);
+    float e1h = __shfl_up_sync(0xffffffffu, x1, 1), e1l = __shfl_up_sync(0xffffffffu, y1, 1);
+    if (lane == 0)
+        e2h = e2l = e1h = e1l = 0.0f;
     __syncthreads();
-    if (threadIdx.x == 0) {
-        double a = bs2[(size_t)ch * nblk + blk], b = bs1[(size_t)ch * nblk + blk];
+    if (threadIdx.x == 0) {  // warp offsets, starting from the block's offset
+        const float2 o2 = bs2[(size_t)ch * nblk + blk], o1 = bs1[(size_t)ch * nblk + blk];
+        float a = o2.x, b = o2.y, c = o1.x, d = o1.y;
         for (int k = 0; k < (int)(blockDim.x >> 5); k++) {
-            const double p = part2[k], q = part1[k];
-            part2[k] = a;
-            part1[k] = b;
-            a += p;
-            b += q;
+            const float2 p = part2[k], q = part1[k];
+            part2[k] = make_float2(a, b);
+            part1[k] = make_float2(c, d);
+            pair_add(a, b, p.x, p.y);
+            pair_add(c, d, q.x, q.y);
         }
     }
     __syncthreads();
-    const double off2 = part2[wid] + (x2 - s2), off1 = part1[wid] + (x1 - s1);
+    float oh2 = part2[wid].x, ol2 = part2[wid].y, oh1 = part1[wid].x, ol1 = part1[wid].y;
+    pair_add(oh2, ol2, e2h, e2l);
+    pair_add(oh1, ol1, e1h, e1l);
     float2 *p2 = pre2f + (size_t)ch * (N + 1);
     float2 *p1 = pre1f ? pre1f + (size_t)ch * (N + 1) : nullptr;
-    auto split = [](double v) {
-        const float hi = (float)v;
-        return make_float2(hi, (float)(v - (double)hi));
-    };
     if (blk == 0 && threadIdx.x == 0) {
         p2[0] = make_float2(0.0f, 0.0f);
         if (p1)
@@ -294,9 +309,14 @@ __global__ void prefix_write_kernel(const float *__restrict__ data, int N, const
     for (int e = 0; e < per; e++) {
         const int i = i0 + threadIdx.x * per + e;
         if (i < N) {
-            p2[i + 1] = split(off2 + v2[e]);
-            if (p1)
-                p1[i + 1] = split(off1 + v1[e]);
+            float a = oh2, b = ol2;
+            pair_add(a, b, v2[e].x, v2[e].y);
+            p2[i + 1] = pair_normalise(a, b);
+            if (p1) {
+                float c = oh1, d = ol1;
+                pair_add(c, d, v1[e].x, v1[e].y);
+                p1[i + 1] = pair_normalise(c, d);
+            }
         }
     }
 }
@@ -330,7 +350,7 @@ static int variable_device(const VArgs &a, int L, cudaStream_t s)
     Scratch ws(s);
     int *k_lo;
     float *zweight, *consts, *tmask, *tsum = nullptr, *mu = nullptr, *dcen = nullptr;
-    double *bs2, *bs1;
+    float2 *bs2, *bs1;
     float2 *pre2f, *pre1f = nullptr;
     const int nblk = (N + kPrefixBlock - 1) / kPrefixBlock;
     if ((rc = ws.get(&k_lo, 2 * (size_t)T, "template ranges")) ||

@@ -191,3 +191,19 @@ def test_fisher_atanh_accuracy():
     _lib.check(lib.fmf_eval_atanh(ds.data_ptr(), os_.data_ptr(), special.size, None), lib)
     s = os_.cpu().numpy()
     assert s[0] == np.inf and s[1] == -np.inf and np.isnan(s[2:]).all()
+
+
+def test_variable_launch_count_per_call():
+    """fmf_last_launch_count reports the launches of the last call only
+    (the counter restarts at every entry point)."""
+    from fast_matched_filter_gb300 import _lib
+    lib = _lib.load()
+    tp, mo, w, d = random_search(12, 2, 2, 2, 80, 4000, 0, 50)
+    nt = np.full(mo.shape, 80, np.int32)
+    counts = []
+    for precision in ("fp32", "fp32", "split_bf16", "split_bf16"):
+        fmf.matched_filter(tp, mo, w, d, 1, n_samples_template=nt, check_zeros=False,
+                           precision=precision)
+        counts.append(lib.fmf_last_launch_count())
+    assert counts[0] == counts[1] and counts[2] == counts[3], counts
+    assert 0 < counts[0] <= 12 and 0 < counts[2] <= 12, counts
