@@ -187,6 +187,12 @@ int validate_args(const Args &a)
         return set_error(FMF_ERR_ARG, "normalize must be 0 (short) or 1 (full), got %d", a.normalize);
     if (a.precision < FMF_PREC_FP32 || a.precision > FMF_PREC_BF16)
         return set_error(FMF_ERR_ARG, "unknown precision %d", a.precision);
+    if (a.flags & FMF_FLAG_DEVICE_POINTERS) {  // the kernels load these in place: 4-byte elements
+        const void *ptrs[6] = {a.tpl, a.sst, a.mo, a.data, a.w, a.out};
+        for (const void *p : ptrs)
+            if ((uintptr_t)p & 3)
+                return set_error(FMF_ERR_ARG, "device array %p is not 4-byte aligned", p);
+    }
     return FMF_OK;
 }
 
@@ -839,6 +845,13 @@ int fmf_detect(const float *cc, size_t n_templates, size_t n_corr, const int *la
 {
     fmf::clear_error();
     fmf::g_launches = 0;
+    if (flags & FMF_FLAG_DEVICE_POINTERS) {  // read and written in place: 4-byte elements
+        const void *ptrs[9] = {cc, lag_begin, lag_end, median_out, mad_out, threshold_out,
+                               count_out, lag_out, value_out};
+        for (const void *p : ptrs)
+            if ((uintptr_t)p & 3)
+                return fmf::set_error(FMF_ERR_ARG, "device array %p is not 4-byte aligned", p);
+    }
     const fmf::DetectOut o{n_mad,      min_separation, max_detections, median_out, mad_out,
                            threshold_out, count_out,   lag_out,        value_out};
     return fmf::detect_entry(cc, n_templates, n_corr, lag_begin, lag_end, o, flags,

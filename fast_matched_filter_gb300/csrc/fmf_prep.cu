@@ -203,14 +203,36 @@ __global__ void template_center_kernel(const float *__restrict__ tpl, int L,
 }
 
 // grid = SC blocks of 1024 threads: the mean of each data channel, rounded
-// to float, from double-float sums (FP32 arithmetic, fixed order).
+// to float, from double-float sums (FP32 arithmetic, fixed order); each
+// thread keeps four 16-byte loads in flight.
 __global__ void channel_mean_kernel(const float *__restrict__ data, int N,
                                     float *__restrict__ mu)
 {
     __shared__ float2 red[32];
     const float *src = data + (size_t)blockIdx.x * N;
     float h = 0.0f, l = 0.0f;
-    for (int i = threadIdx.x; i < N; i += blockDim.x)
+    // the floats before the first 16-byte boundary of the row (any caller pointer), then
+    // float4 groups
+    const int head = (int)min((long long)N, (long long)(((16 - ((uintptr_t)src & 15)) & 15) >> 2));
+    for (int i = threadIdx.x; i < head; i += blockDim.x)
+        pair_add(h, l, src[i], 0.0f);
+    const float4 *v4 = reinterpret_cast<const float4 *>(src + head);
+    const int n4 = (N - head) >> 2;
+    constexpr int U = 4;
+    for (int i0 = threadIdx.x; i0 < n4; i0 += U * blockDim.x) {
+        float4 x[U];
+#pragma unroll
+        for (int u = 0; u < U; u++)
+            x[u] = i0 + u * (int)blockDim.x < n4 ? v4[i0 + u * blockDim.x] : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            pair_add(h, l, x[u].x, 0.0f);
+            pair_add(h, l, x[u].y, 0.0f);
+            pair_add(h, l, x[u].z, 0.0f);
+            pair_add(h, l, x[u].w, 0.0f);
+        }
+    }
+    for (int i = head + 4 * n4 + threadIdx.x; i < N; i += blockDim.x)
         pair_add(h, l, src[i], 0.0f);
     for (int o = 16; o > 0; o >>= 1) {
         const float yh = __shfl_down_sync(0xffffffffu, h, o), yl = __shfl_down_sync(0xffffffffu, l, o);

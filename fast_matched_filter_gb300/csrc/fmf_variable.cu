@@ -89,26 +89,36 @@ __global__ void vp_meta_kernel(const int *__restrict__ mo, const float *__restri
 
 // scale[t] = the reference's max_cc after template t: one float sum of the
 // weights of templates 0..t in (t, ch) order (never reset,
-// matched_filter.c:329,365).  One block: the weights pass through shared
-// memory in chunks, thread 0 adds them in order.
+// matched_filter.c:329,365).  One block: the weights of whole templates pass
+// through shared memory, thread 0 adds them in order.
 constexpr int kScaleChunk = 8192;
 __global__ void vp_scale_kernel(const float *__restrict__ w, int T, int SC, float *__restrict__ scale)
 {
     __shared__ float buf[kScaleChunk];
-    const long long n = (long long)T * SC;
+    const int per = SC <= kScaleChunk ? kScaleChunk / SC : 0;  // whole templates per chunk
     float max_cc = 0.0f;
-    for (long long c0 = 0; c0 < n; c0 += kScaleChunk) {
-        const int len = (int)min((long long)kScaleChunk, n - c0);
+    if (per == 0) {  // more channels than one chunk holds: straight from global memory
+        if (threadIdx.x == 0)
+            for (int t = 0; t < T; t++) {
+                for (int ch = 0; ch < SC; ch++)
+                    max_cc += w[(size_t)t * SC + ch];
+                scale[t] = max_cc;
+            }
+        return;
+    }
+    for (int t0 = 0; t0 < T; t0 += per) {
+        const int nt = min(per, T - t0);
         __syncthreads();
-        for (int i = threadIdx.x; i < len; i += blockDim.x)
-            buf[i] = w[c0 + i];
+        for (int i = threadIdx.x; i < nt * SC; i += blockDim.x)
+            buf[i] = w[(size_t)t0 * SC + i];
         __syncthreads();
         if (threadIdx.x == 0) {
-            for (int i = 0; i < len; i++) {
-                max_cc += buf[i];
-                const long long g = c0 + i;
-                if ((g + 1) % SC == 0)
-                    scale[g / SC] = max_cc;
+            for (int tt = 0; tt < nt; tt++) {
+                const float *b = buf + tt * SC;
+#pragma unroll 8
+                for (int ch = 0; ch < SC; ch++)
+                    max_cc += b[ch];
+                scale[t0 + tt] = max_cc;
             }
         }
     }
@@ -221,14 +231,26 @@ __global__ void prefix_offsets_kernel(float2 *bs2, float2 *bs1, int nblk, int SC
     if (ch >= SC)
         return;
     float2 a = make_float2(0.0f, 0.0f), b = make_float2(0.0f, 0.0f);
-    for (int i = 0; i < nblk; i++) {
-        const float2 x = bs2[(size_t)ch * nblk + i], y = bs1[(size_t)ch * nblk + i];
-        bs2[(size_t)ch * nblk + i] = a;
-        bs1[(size_t)ch * nblk + i] = b;
-        pair_add(a.x, a.y, x.x, x.y);
-        a = pair_normalise(a.x, a.y);
-        pair_add(b.x, b.y, y.x, y.y);
-        b = pair_normalise(b.x, b.y);
+    float2 *p2 = bs2 + (size_t)ch * nblk, *p1 = bs1 + (size_t)ch * nblk;
+    constexpr int G = 8;  // loads of a group issued before the dependent additions
+    for (int i0 = 0; i0 < nblk; i0 += G) {
+        float2 x[G], y[G];
+#pragma unroll
+        for (int j = 0; j < G; j++) {
+            x[j] = i0 + j < nblk ? p2[i0 + j] : make_float2(0.0f, 0.0f);
+            y[j] = i0 + j < nblk ? p1[i0 + j] : make_float2(0.0f, 0.0f);
+        }
+#pragma unroll
+        for (int j = 0; j < G; j++) {
+            if (i0 + j < nblk) {
+                p2[i0 + j] = a;
+                p1[i0 + j] = b;
+            }
+            pair_add(a.x, a.y, x[j].x, x[j].y);
+            a = pair_normalise(a.x, a.y);
+            pair_add(b.x, b.y, y[j].x, y[j].y);
+            b = pair_normalise(b.x, b.y);
+        }
     }
 }
 
@@ -450,6 +472,12 @@ static int variable_entry(const VArgs &a, void *stream)
     const int precision = FMF_FLAG_PRECISION_OF(a.flags);
     if (precision != FMF_PREC_FP32 && precision != FMF_PREC_SPLIT_BF16 && precision != FMF_PREC_BF16)
         return set_error(FMF_ERR_ARG, "unknown precision %d", precision);
+    if (a.flags & FMF_FLAG_DEVICE_POINTERS) {  // read in place: 4-byte elements
+        const void *ptrs[7] = {a.tpl, a.sst, a.mo, a.data, a.w, a.ntap, a.out};
+        for (const void *p : ptrs)
+            if ((uintptr_t)p & 3)
+                return set_error(FMF_ERR_ARG, "device array %p is not 4-byte aligned", p);
+    }
     cudaGetLastError();
     cudaStream_t s = (cudaStream_t)stream;
     const size_t n_meta = a.T * a.S * a.C;

@@ -77,6 +77,17 @@ def test_null_pointer_rejected(lib):
     assert lib.fmf_matched_filter(*args) == _lib.FMF_ERR_ARG
 
 
+def test_misaligned_device_array_rejected(lib):
+    """Device arrays are read in place: one off its element alignment is an
+    argument error, reported before any device work."""
+    args, keep = _args()
+    ex = [a if not hasattr(a, "contents") else ct.cast(a, ct.c_void_p).value for a in args]
+    ex[3] += 2  # data, 2 bytes off
+    st = lib.fmf_matched_filter_ex(*ex, 0, _lib.FLAG_DEVICE_POINTERS, None)
+    assert st == _lib.FMF_ERR_ARG
+    assert "aligned" in _lib.last_error(lib)[1]
+
+
 def test_unknown_precision_rejected(lib):
     args, keep = _args()
     ex = [a if not hasattr(a, "contents") else ct.cast(a, ct.c_void_p).value for a in args]
