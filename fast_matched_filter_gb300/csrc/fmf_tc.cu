@@ -82,6 +82,12 @@ struct TcProb {
     int n_tiles;                  // output tiles of nb*128 indices
     int tg;                       // templates interleaved per group of items
     int nb;                       // lag blocks per tile (MMA N): 32, 64 or 128
+    int parts;                    // k >= 1: the channels of a (tile, template) in k
+                                  // ranges [j SC / k, (j + 1) SC / k) on k CTAs (items
+                                  // j = 0..k-1 adjacent); their network sums go to
+                                  // part_out[j][t][lag] and are added in order j after
+                                  // the launch (a fixed order: deterministic results)
+    float *part_out;
 };
 
 struct TcBatch {
@@ -379,7 +385,9 @@ __global__ void tc_template_kernel(const float *__restrict__ tpl, const int *__r
 // ------------------------------------------------------------------ persistent kernel
 // Decodes a tile-queue item: search p, output tile, template t.  Items of one
 // search are ordered so that groups of `tg` templates sweep the tiles together.
-__device__ __forceinline__ void decode_item(const TcBatch &B, long long item, int &p, int &tile, int &t)
+template <bool PARTS>
+__device__ __forceinline__ void decode_item(const TcBatch &B, long long item, int &p, int &tile, int &t,
+                                            int &c_begin, int &c_end, int &part)
 {
     int lo = 0, hi = B.n_probs - 1;
     while (lo < hi) {
@@ -391,7 +399,17 @@ __device__ __forceinline__ void decode_item(const TcBatch &B, long long item, in
     }
     p = lo;
     const TcProb &pr = B.prob[p];
-    const long long local = item - pr.item_begin;
+    long long local = item - pr.item_begin;
+    c_begin = 0;
+    c_end = pr.P.SC;
+    part = 0;
+    if (PARTS) {  // the parts of a (tile, template) are adjacent items
+        const int k = pr.parts;
+        part = (int)(local % k);
+        local /= k;
+        c_begin = (int)((long long)part * pr.P.SC / k);
+        c_end = (int)((long long)(part + 1) * pr.P.SC / k);
+    }
     const long long per_group = (long long)pr.n_tiles * pr.tg;
     const int grp = (int)(local / per_group);
     const long long rem = local - (long long)grp * per_group;
@@ -487,8 +505,9 @@ int launch_fisher_atanh(const float *y, float *out, long long n, cudaStream_t s)
 
 // VAR: per-channel template lengths (Problem::ntap set in every search of the
 // batch), a separate instantiation so that the fixed-length epilogue keeps
-// its registers.
-template <bool VAR>
+// its registers.  PARTS: every search runs its items as channel parts
+// (TcProb::parts), a separate instantiation for the same reason.
+template <bool VAR, bool PARTS>
 __global__ void __launch_bounds__(tc_threads(VAR), 1) tc_persistent(const __grid_constant__ TcBatch B)
 {
     constexpr int TC_EPI_WARPS = tc_epi_warps(VAR);
@@ -555,8 +574,8 @@ __global__ void __launch_bounds__(tc_threads(VAR), 1) tc_persistent(const __grid
             item = __shfl_sync(0xffffffffu, item, 0);  // warp-uniform decision
             if (item >= total)
                 break;
-            int p, tile, t;
-            decode_item(B, item, p, tile, t);
+            int p, tile, t, c_begin, c_end, part;
+            decode_item<PARTS>(B, item, p, tile, t, c_begin, c_end, part);
             const TcProb &pr = B.prob[p];
             const Problem &P = pr.P;
             const int nb = pr.nb;
@@ -595,16 +614,16 @@ __global__ void __launch_bounds__(tc_threads(VAR), 1) tc_persistent(const __grid
                 return true;
             };
             auto next_active = [&](int ch) {
-                while (ch < SC && w[ch] == 0.0f)
+                while (ch < c_end && w[ch] == 0.0f)
                     ch++;
                 return ch;
             };
             // active channels in order; with step > 1 two consecutive channels
             // have their phases interleaved, so that both buffers stay fed
-            int ch = next_active(0);
-            while (ok && ch < SC) {
-                const int ch2 = step > 1 ? next_active(ch + 1) : SC;
-                const bool pair = ch2 < SC;
+            int ch = next_active(c_begin);
+            while (ok && ch < c_end) {
+                const int ch2 = step > 1 ? next_active(ch + 1) : c_end;
+                const bool pair = ch2 < c_end;
                 const int b = (int)(g & 1);
                 for (int phi = 0; ok && phi < step; phi++) {
                     ok = load_stage(ch, phi, b);
@@ -639,8 +658,8 @@ __global__ void __launch_bounds__(tc_threads(VAR), 1) tc_persistent(const __grid
                 mbar_arrive(iempty0 + 8 * slot);
                 if (item >= total)
                     break;
-                int p, tile, t;
-                decode_item(B, item, p, tile, t);
+                int p, tile, t, c_begin, c_end, part;
+                decode_item<PARTS>(B, item, p, tile, t, c_begin, c_end, part);
                 const TcProb &pr = B.prob[p];
                 const Problem &P = pr.P;
                 const int nb = pr.nb;
@@ -655,7 +674,7 @@ __global__ void __launch_bounds__(tc_threads(VAR), 1) tc_persistent(const __grid
                 const uint32_t w_off = (split ? 2u : 1u) * data_bytes;
                 const uint32_t lbo_b = (uint32_t)pr.R * 16;
                 const float *w = P.w + (size_t)t * SC;
-                for (int ch = 0; ch < SC; ch++) {
+                for (int ch = c_begin; ch < c_end; ch++) {
                     if (w[ch] == 0.0f)
                         continue;
                     if ((c & 1) != m) {  // the other issuer's channel
@@ -747,8 +766,8 @@ __global__ void __launch_bounds__(tc_threads(VAR), 1) tc_persistent(const __grid
             item = __shfl_sync(0xffffffffu, item, 0);
             if (item >= total)
                 break;
-            int p, tile, t;
-            decode_item(B, item, p, tile, t);
+            int p, tile, t, c_begin, c_end, part;
+            decode_item<PARTS>(B, item, p, tile, t, c_begin, c_end, part);
             const TcProb &pr = B.prob[p];
             // per-item fields, once, into registers
             const int nb = pr.nb;
@@ -777,7 +796,7 @@ __global__ void __launch_bounds__(tc_threads(VAR), 1) tc_persistent(const __grid
             const float *w = pr.P.w + (size_t)t * SC;
             const int *mo = pr.P.mo + (size_t)t * SC;
             bool first = true;
-            for (int ch = 0; busy && ch < SC; ch++) {
+            for (int ch = c_begin; busy && ch < c_end; ch++) {
                 const float wc = w[ch];
                 if (wc == 0.0f)
                     continue;
@@ -943,7 +962,9 @@ __global__ void __launch_bounds__(tc_threads(VAR), 1) tc_persistent(const __grid
                 c++;
             }
             if (nsum) {
-                float *o = outp + (size_t)t * n_corr + kb + (long long)TC_Q * a0;
+                // a channel part writes its partial sums to its own plane of part_out
+                float *o = (PARTS ? pr.part_out + (size_t)part * pr.P.T * n_corr : outp) +
+                           (size_t)t * n_corr + kb + (long long)TC_Q * a0;
                 const long long lim = n_corr - kb - (long long)TC_Q * a0;
 #pragma unroll 1
                 for (int c0 = 0; c0 < NC; c0 += CH) {
@@ -1064,6 +1085,8 @@ int tc_prepare(const Problem &P, const float *data_for_tc, int split, int nb, in
     pr.row_front = nb + 3;
     pr.rows_total = pr.row_front + (int)(((long long)P.N / step + 2) / TC_Q) + 2 + g.R + 1;
     pr.item_begin = 0;
+    pr.parts = 1;
+    pr.part_out = nullptr;
 
     const size_t g_elems = (size_t)P.SC * step * TC_CB * pr.rows_total * 8;
     const size_t w_elems = (size_t)P.T * P.SC * step * g.NW * 64;
@@ -1105,6 +1128,43 @@ static int n_sms()
     return n;
 }
 
+// out[i] = sum over parts j = 0..k-1 of part[j][i], in that order.
+__global__ void tc_parts_sum_kernel(const float *__restrict__ part, int k, long long m, float *__restrict__ out)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m)
+        return;
+    float v = part[i];
+    for (int j = 1; j < k; j++)
+        v += part[(size_t)j * m + i];
+    out[i] = v;
+}
+
+// Channel parts k (1..8, at most SC) for a search of `items` (tile, template)
+// items: the k that minimises the busiest SM's work, ceil(k items / SMs)
+// rounds of (1/k + 0.05) item each (0.05: an item's fixed pipeline fill and
+// output write); FMF_TC_PARTS=k forces a value.
+static int tc_choose_parts(long long items, int SC)
+{
+    const int sms = n_sms(), kmax = SC < 8 ? SC : 8;
+    if (const char *env = getenv("FMF_TC_PARTS")) {
+        const int k = atoi(env);
+        if (k >= 1)
+            return k < kmax ? k : kmax;
+    }
+    int best = 1;
+    double best_cost = 1e300;
+    for (int k = 1; k <= kmax; k++) {
+        const long long rounds = (k * items + sms - 1) / sms;
+        const double cost = (double)rounds * (1.0 / k + 0.05);
+        if (cost < best_cost - 1e-9) {
+            best_cost = cost;
+            best = k;
+        }
+    }
+    return best;
+}
+
 // One persistent launch over the tile queue of `n` prepared searches (n <= TC_MAX_PROBS).
 // `queue` is a device counter that this call zeroes on `s` before the launch.
 int tc_run(const TcProb *probs, int n, int split, unsigned long long *queue, unsigned *err, cudaStream_t s)
@@ -1115,10 +1175,26 @@ int tc_run(const TcProb *probs, int n, int split, unsigned long long *queue, uns
     TcBatch &B = Bh;
     long long items = 0;
     size_t stage = 0;
+    // A lone search with fewer (tile, template) items than SMs runs each item as k
+    // channel parts (network sum only; per-channel lengths need whole sums for
+    // their transform), k chosen to shorten the busiest SM's queue.  FMF_TC_PARTS=k
+    // overrides the choice where parts are allowed.
+    const Problem &P0 = probs[0].P;
+    const bool can_split = n == 1 && !P0.ntap && P0.network_sum && P0.SC >= 2;
+    const int parts = can_split ? tc_choose_parts((long long)probs[0].n_tiles * P0.T, P0.SC) : 1;
+    Scratch pws(s);
+    float *part_out = nullptr;
+    if (parts > 1) {
+        int rc = pws.get(&part_out, (size_t)parts * P0.T * P0.n_corr, "channel-part sums");
+        if (rc)
+            return rc;
+    }
     for (int i = 0; i < n; i++) {
         B.prob[i] = probs[i];
         B.prob[i].item_begin = items;
-        items += (long long)probs[i].n_tiles * probs[i].P.T;
+        B.prob[i].parts = parts;
+        B.prob[i].part_out = part_out;
+        items += (long long)probs[i].n_tiles * probs[i].P.T * parts;
         const size_t st = tc_shape(probs[i].P.L, probs[i].P.step, split, probs[i].nb).stage;
         stage = st > stage ? st : stage;
     }
@@ -1144,14 +1220,21 @@ int tc_run(const TcProb *probs, int n, int split, unsigned long long *queue, uns
         n_var += probs[i].P.ntap != nullptr;
     if (n_var != 0 && n_var != n)
         return set_error(FMF_ERR_ARG, "a persistent launch mixes per-channel and fixed template lengths");
-    void (*kern)(const TcBatch) = n_var ? tc_persistent<true> : tc_persistent<false>;
+    void (*kern)(const TcBatch) = n_var ? tc_persistent<true, false>
+                                  : (parts > 1 ? tc_persistent<false, true> : tc_persistent<false, false>);
     e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess)
         return set_error(FMF_ERR_CUDA, "tc_persistent shared memory (%zu bytes): %s", smem,
                          cudaGetErrorString(e));
     kern<<<grid, tc_threads(n_var != 0), smem, s>>>(B);
     count_launch();
-    return check_launch("tc_persistent");
+    int rc = check_launch("tc_persistent");
+    if (rc || parts == 1)
+        return rc;
+    const long long m = (long long)P0.T * P0.n_corr;
+    tc_parts_sum_kernel<<<(unsigned)((m + 255) / 256), 256, 0, s>>>(part_out, parts, m, P0.out);
+    count_launch();
+    return check_launch("tc_parts_sum_kernel");
 }
 
 size_t tc_prob_size() { return sizeof(TcProb); }

@@ -46,6 +46,32 @@ def test_split_bf16_per_channel(oracle_built, tile_lags, normalize):
     assert_parity(got, oracle_of(oracle_built, tp, mo, w, d, 2, normalize, False))
 
 
+@pytest.mark.parametrize("parts", ["1", "2", "5", "auto"])
+@pytest.mark.parametrize("S,C,step,normalize,zero", [(2, 1, 1, "short", 0), (3, 1, 2, "full", 1),
+                                                      (4, 3, 1, "short", 3), (1, 3, 3, "full", 0)])
+def test_split_bf16_channel_parts(oracle_built, monkeypatch, parts, S, C, step, normalize, zero):
+    """A lone search with fewer (tile, template) items than SMs runs each item
+    as k channel parts whose network sums are added in part order afterwards;
+    FMF_TC_PARTS forces k (at most the channel count).  Every k meets the parity
+    bar and agrees with the undivided form."""
+    tp, mo, w, d = random_search(70 + S * C + step, 3, S, C, 150, 30000, -20, 150,
+                                 dc=3.0 if normalize == "full" else 0.0, zero_weights=zero)
+    if zero == 3:  # one template with its whole first half of channels silent
+        w[1].reshape(-1)[: S * C // 2] = 0.0
+    if parts == "auto":
+        monkeypatch.delenv("FMF_TC_PARTS", raising=False)
+    else:
+        monkeypatch.setenv("FMF_TC_PARTS", parts)
+    got = fmf.matched_filter(tp, mo, w, d, step, check_zeros=False, normalize=normalize,
+                             precision="split_bf16")
+    assert_parity(got, oracle_of(oracle_built, tp, mo, w, d, step, normalize, True))
+    monkeypatch.setenv("FMF_TC_PARTS", "1")
+    other = fmf.matched_filter(tp, mo, w, d, step, check_zeros=False, normalize=normalize,
+                               precision="split_bf16")
+    assert np.array_equal(got == 0, other == 0)
+    assert np.abs(got - other).max() <= 1e-6
+
+
 def test_split_bf16_config0(oracle_built):
     cfg = synthetic.config0()
     args = (cfg["templates"], cfg["moveouts"], cfg["weights"], cfg["data"], cfg["step"])
