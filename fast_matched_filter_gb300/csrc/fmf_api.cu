@@ -465,27 +465,34 @@ static int run_streamed(const Args &d, float *host_out, cudaStream_t s)
     for (int i = 0; i <= n_chunks && e == cudaSuccess; i++)
         e = cudaEventCreateWithFlags(&ev[i], cudaEventDisableTiming);
     if (e == cudaSuccess) {
-        for (int c = 0; c < n_chunks && rc == FMF_OK; c++) {
+        // every chunk's kernels first, then the copies: a copy into pageable host memory
+        // returns only when it is done, and the kernels of the later chunks are queued by then
+        int launched = 0;
+        for (int c = 0; c < n_chunks && rc == FMF_OK && e == cudaSuccess; c++, launched++) {
+            const int t0 = bounds[c], nt = bounds[c + 1] - bounds[c];
+            if (nt > 0) {
+                if (!tcfull.empty()) {
+                    std::vector<unsigned char> sub(tc_prob_size());
+                    unsigned long long *queue;
+                    tc_subset(reinterpret_cast<const TcProb *>(tcfull.data()), t0, nt,
+                              reinterpret_cast<TcProb *>(sub.data()));
+                    if (!(rc = ws.get(&queue, 1, "tile queue")))
+                        rc = tc_run(reinterpret_cast<const TcProb *>(sub.data()), 1, split, queue, err, s);
+                } else {
+                    rc = launch_plain_all(problem_subset(P, t0, nt), s);
+                }
+                if (!rc && zc)
+                    rc = launch_zero_count(d, P.out, t0, nt, zc, s);
+            }
+            if (!rc)
+                e = cudaEventRecord(ev[c], s);
+        }
+        for (int c = 0; c < launched && rc == FMF_OK && e == cudaSuccess; c++) {
             const int t0 = bounds[c], nt = bounds[c + 1] - bounds[c];
             if (nt <= 0)
                 continue;
-            if (!tcfull.empty()) {
-                std::vector<unsigned char> sub(tc_prob_size());
-                unsigned long long *queue;
-                tc_subset(reinterpret_cast<const TcProb *>(tcfull.data()), t0, nt,
-                          reinterpret_cast<TcProb *>(sub.data()));
-                if (!(rc = ws.get(&queue, 1, "tile queue")))
-                    rc = tc_run(reinterpret_cast<const TcProb *>(sub.data()), 1, split, queue, err, s);
-            } else {
-                rc = launch_plain_all(problem_subset(P, t0, nt), s);
-            }
-            if (!rc && zc)
-                rc = launch_zero_count(d, P.out, t0, nt, zc, s);
-            if (rc)
-                break;
             const size_t off = (size_t)t0 * row, n = (size_t)nt * row * sizeof(float);
-            if ((e = cudaEventRecord(ev[c], s)) != cudaSuccess ||
-                (e = cudaStreamWaitEvent(s2, ev[c], 0)) != cudaSuccess ||
+            if ((e = cudaStreamWaitEvent(s2, ev[c], 0)) != cudaSuccess ||
                 (e = cudaMemcpyAsync(host_out + off, P.out + off, n, cudaMemcpyDeviceToHost, s2)) !=
                     cudaSuccess)
                 break;
