@@ -28,14 +28,13 @@
 #include <climits>
 #include <cmath>
 #include <cstdlib>
+#include <vector>
 
 #include "fmf_common.cuh"
 
 namespace fmf {
 
 __global__ void channel_mean_kernel(const float *, int, float *);
-int launch_tc(const Problem &P, const float *data_for_tc, int precision, unsigned *err, Scratch &ws,
-              cudaStream_t s, int forced_nb, int template_group);
 int collect_device_errors();
 
 // Fisher-z weight of every (t, ch), one thread each, in the reference's mix
@@ -364,7 +363,54 @@ struct VArgs {
     int normalize, flags;
 };
 
-static int variable_device(const VArgs &a, int L, cudaStream_t s)
+// Templates [t0, t0 + nt) of a prepared per-channel-length search.
+static Problem var_subset(const Problem &P, int t0, int nt)
+{
+    Problem Q = P;
+    const size_t o = (size_t)t0 * P.SC;
+    Q.tpl += o * P.L;
+    Q.sst += o;
+    if (Q.tsum)
+        Q.tsum += o;
+    Q.mo += o;
+    Q.w += o;
+    Q.ntap += o;
+    Q.zweight += o;
+    Q.k_lo += t0;
+    Q.k_hi += t0;
+    Q.out += (size_t)t0 * P.n_corr;
+    Q.T = nt;
+    return Q;
+}
+
+// A second stream and one event per template chunk, released on scope exit.
+struct CopyStream {
+    cudaStream_t s2 = nullptr;
+    cudaEvent_t ev[9] = {};
+    cudaError_t init(int n)
+    {
+        cudaError_t e = cudaStreamCreateWithFlags(&s2, cudaStreamNonBlocking);
+        for (int i = 0; i <= n && e == cudaSuccess; i++)
+            e = cudaEventCreateWithFlags(&ev[i], cudaEventDisableTiming);
+        return e;
+    }
+    ~CopyStream()
+    {
+        if (s2) {
+            cudaStreamSynchronize(s2);
+            cudaStreamDestroy(s2);
+        }
+        for (cudaEvent_t e : ev)
+            if (e)
+                cudaEventDestroy(e);
+    }
+};
+
+// With host_out, the result goes to host memory in template chunks of
+// tapering size (8,8,8,8,4,2,1,1 of 40 parts), each chunk's copy on a second
+// stream overlapping the later chunks' kernels (all of which are queued before
+// the first copy, which blocks the host when host_out is pageable).
+static int variable_device(const VArgs &a, int L, cudaStream_t s, float *host_out = nullptr)
 {
     int rc;
     const int T = (int)a.T, SC = (int)(a.S * a.C), N = (int)a.N;
@@ -434,26 +480,86 @@ static int variable_device(const VArgs &a, int L, cudaStream_t s)
     P.zweight = zweight;
     P.vp_norm = P.vp_bias = P.vp_scale = nullptr;
     const int precision = FMF_FLAG_PRECISION_OF(a.flags);
+    const size_t row_bytes = a.n_corr * sizeof(float);
+    const int n_chunks = (!host_out || (size_t)T * row_bytes < ((size_t)64 << 20)) ? 1 : (T < 8 ? T : 8);
+    int bounds[9];
+    {
+        static const int wts[8] = {8, 8, 8, 8, 4, 2, 1, 1};
+        const bool taper = n_chunks == 8 && T >= 40;
+        int acc = 0;
+        bounds[0] = 0;
+        for (int c = 0; c < n_chunks; c++) {
+            acc += taper ? wts[c] : 1;
+            bounds[c + 1] = (int)(((long long)T * acc) / (taper ? 40 : n_chunks));
+        }
+        bounds[n_chunks] = T;
+    }
+    unsigned *err = nullptr;
+    int split = 0;
+    std::vector<unsigned char> tcfull;
     if (precision != FMF_PREC_FP32) {
-        unsigned *err = nullptr;
         const int forced = ((a.flags >> 8) & 0xff) * 16;
         if (forced != 0 && forced != 32 && forced != 64 && forced != 128)
             return set_error(FMF_ERR_ARG, "tensor-core tile of %d lag blocks (32, 64 or 128)", forced);
         P.vp_norm = norm_sum;  // the final transform fused into the output write
         P.vp_bias = bias;
         P.vp_scale = scale;
+        split = precision == FMF_PREC_SPLIT_BF16;
+        const int nb = tc_choose_nb(L, (int)a.step, split, forced);
+        if (nb == 0)
+            return set_error(FMF_ERR_SMEM, "template length %d, step %zu: tensor-core tile does not fit "
+                                           "shared memory", L, a.step);
+        tcfull.resize(tc_prob_size());
         if ((rc = device_error_word(&err)) ||
-            (rc = launch_tc(P, P.data, precision, err, ws, s, forced, (a.flags >> 16) & 0xff)))
+            (rc = tc_prepare(P, P.data, split, nb, (a.flags >> 16) & 0xff, ws, s,
+                             reinterpret_cast<TcProb *>(tcfull.data()))))
             return rc;
-        return FMF_OK;
     }
-    if ((rc = launch_plain_all(P, s)))
-        return rc;
-    const long long n = (long long)T * a.n_corr;
-    vp_finalize_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(a.out, T, (int)a.n_corr, norm_sum, bias,
-                                                                   scale);
-    count_launch();
-    return check_launch("variable-length transform");
+    CopyStream cs;
+    cudaError_t e = host_out ? cs.init(n_chunks) : cudaSuccess;
+    if (e != cudaSuccess)
+        return set_error(FMF_ERR_CUDA, "copy stream: %s", cudaGetErrorString(e));
+    for (int c = 0; c < n_chunks; c++) {
+        const int t0 = bounds[c], nt = bounds[c + 1] - bounds[c];
+        if (nt > 0) {
+            if (!tcfull.empty()) {
+                std::vector<unsigned char> sub(tc_prob_size());
+                unsigned long long *queue;
+                tc_subset(reinterpret_cast<const TcProb *>(tcfull.data()), t0, nt,
+                          reinterpret_cast<TcProb *>(sub.data()));
+                if ((rc = ws.get(&queue, 1, "tile queue")) ||
+                    (rc = tc_run(reinterpret_cast<const TcProb *>(sub.data()), 1, split, queue, err, s)))
+                    return rc;
+            } else {
+                if ((rc = launch_plain_all(var_subset(P, t0, nt), s)))
+                    return rc;
+                const long long n = (long long)nt * a.n_corr;
+                vp_finalize_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(
+                    a.out + (size_t)t0 * a.n_corr, nt, (int)a.n_corr, norm_sum + t0, bias + t0, scale + t0);
+                count_launch();
+                if ((rc = check_launch("variable-length transform")))
+                    return rc;
+            }
+        }
+        if (host_out && (e = cudaEventRecord(cs.ev[c], s)) != cudaSuccess)
+            return set_error(FMF_ERR_CUDA, "chunk event: %s", cudaGetErrorString(e));
+    }
+    if (!host_out)
+        return FMF_OK;
+    for (int c = 0; c < n_chunks; c++) {
+        const int t0 = bounds[c], nt = bounds[c + 1] - bounds[c];
+        if (nt <= 0)
+            continue;
+        if ((e = cudaStreamWaitEvent(cs.s2, cs.ev[c], 0)) != cudaSuccess ||
+            (e = cudaMemcpyAsync(host_out + (size_t)t0 * a.n_corr, a.out + (size_t)t0 * a.n_corr,
+                                 (size_t)nt * row_bytes, cudaMemcpyDeviceToHost, cs.s2)) != cudaSuccess)
+            return set_error(FMF_ERR_CUDA, "copying the result: %s", cudaGetErrorString(e));
+    }
+    // the scratch is freed on s: s waits for the last copy
+    if ((e = cudaEventRecord(cs.ev[n_chunks], cs.s2)) != cudaSuccess ||
+        (e = cudaStreamWaitEvent(s, cs.ev[n_chunks], 0)) != cudaSuccess)
+        return set_error(FMF_ERR_CUDA, "copying the result: %s", cudaGetErrorString(e));
+    return FMF_OK;
 }
 
 static int variable_entry(const VArgs &a, void *stream)
@@ -532,11 +638,8 @@ static int variable_entry(const VArgs &a, void *stream)
         d.w = buf[4];
         d.ntap = reinterpret_cast<const int *>(buf[5]);
         d.out = buf[6];
-        if ((rc = variable_device(d, L, s)))
+        if ((rc = variable_device(d, L, s, a.out)))
             return rc;
-        cudaError_t e = cudaMemcpyAsync(a.out, d.out, cnt[6] * 4, cudaMemcpyDeviceToHost, s);
-        if (e != cudaSuccess)
-            return set_error(FMF_ERR_CUDA, "copying the result: %s", cudaGetErrorString(e));
     }
     cudaError_t e = cudaStreamSynchronize(s);
     if (e != cudaSuccess)

@@ -207,3 +207,37 @@ def test_variable_launch_count_per_call():
         counts.append(lib.fmf_last_launch_count())
     assert counts[0] == counts[1] and counts[2] == counts[3], counts
     assert 0 < counts[0] <= 12 and 0 < counts[2] <= 12, counts
+
+
+@pytest.mark.parametrize("precision", ["fp32", "split_bf16"])
+def test_variable_host_result_in_chunks_equals_device_result(precision):
+    """A result above 64 MB goes to host memory in template chunks whose copies
+    overlap the later chunks' kernels; it must equal, bit for bit, the same
+    search with device arrays (one launch, no chunks)."""
+    torch = pytest.importorskip("torch")
+    from fast_matched_filter_gb300 import _lib
+    lib = _lib.load()
+    rng = np.random.default_rng(31)
+    T, S, C, L, N = 20, 2, 1, 100, 1_050_000
+    tp, mo, w, d = random_search(31, T, S, C, L, N, 0, 80)
+    nt = rng.integers(20, L + 1, mo.shape).astype(np.int32)
+    nt[0, 0, 0] = L
+    for idx in np.ndindex(nt.shape):
+        tp[idx][nt[idx]:] = 0.0
+    host = fmf.matched_filter(tp, mo, w, d, 1, n_samples_template=nt, check_zeros=False,
+                              precision=precision)
+    assert host.nbytes > 64 << 20
+    sst = np.sum(tp.astype(np.float32) ** 2, axis=-1).astype(np.float32)
+    dev = [torch.from_numpy(np.ascontiguousarray(x)).cuda() for x in (tp, sst, mo, d, w, nt)]
+    out = torch.empty(host.shape, dtype=torch.float32, device="cuda")
+    st = lib.fmf_matched_filter_variable_ex(
+        dev[0].data_ptr(), dev[1].data_ptr(), dev[2].data_ptr(), dev[3].data_ptr(), dev[4].data_ptr(),
+        1, dev[5].data_ptr(), N, T, S, C, host.shape[1], out.data_ptr(), 0,
+        _lib.FLAG_DEVICE_POINTERS | _lib.flag_precision(precision), None)
+    _lib.check(st, lib)
+    torch.cuda.synchronize()
+    _lib.check(lib.fmf_device_errors(), lib)
+    got = out.cpu().numpy()
+    assert np.array_equal(np.isnan(got), np.isnan(host))
+    ok = ~np.isnan(host)
+    assert np.array_equal(got[ok], host[ok])
