@@ -40,6 +40,7 @@
 // detection run needs no host round trip and can be captured in a graph.
 #include <algorithm>
 #include <cmath>
+#include <type_traits>
 
 #include "fmf_common.cuh"
 
@@ -156,23 +157,55 @@ __device__ __forceinline__ void finish_select(DetState &s, int mode, float v, fl
     }
 }
 
-// Ascending bitonic sort of P (a power of two) 32-bit keys in shared memory.
-__device__ void bitonic_sort32(unsigned *a, int P)
+// The key of rank r (0-based, ascending) among the first P keys of sk, by the
+// block: three radix passes (11, 11 and 10 bits), each a shared-memory
+// histogram of the keys that match the bits chosen so far, then one warp
+// finding the bucket that holds the rank.  All threads of the block call it.
+__device__ unsigned block_select(const unsigned *sk, int P, int r, unsigned *hist, int *shared_pick)
 {
-    for (int k = 2; k <= P; k <<= 1)
-        for (int j = k >> 1; j > 0; j >>= 1) {
-            for (int i = threadIdx.x; i < P; i += blockDim.x) {
-                const int l = i ^ j;
-                if (l > i) {
-                    const unsigned x = a[i], y = a[l];
-                    if ((x > y) == ((i & k) == 0)) {
-                        a[i] = y;
-                        a[l] = x;
-                    }
-                }
-            }
-            __syncthreads();
+    unsigned prefix = 0u;
+    for (int pass = 0; pass < 3; pass++) {
+        const int shift = pass_shift(pass);
+        const unsigned bins = pass_bins(pass), high = pass_high_mask(pass);
+        for (int i = threadIdx.x; i < (int)bins; i += blockDim.x)
+            hist[i] = 0u;
+        __syncthreads();
+        for (int i = threadIdx.x; i < P; i += blockDim.x) {
+            const unsigned k = sk[i];
+            if ((k & high) == prefix)
+                atomicAdd(&hist[(k >> shift) & (bins - 1u)], 1u);
         }
+        __syncthreads();
+        if (threadIdx.x < 32) {
+            const int lane = threadIdx.x, per = (int)bins / 32;
+            unsigned sum = 0;
+            for (int i = 0; i < per; i++)
+                sum += hist[lane * per + i];
+            unsigned inc = sum;
+            for (int o = 1; o < 32; o <<= 1) {
+                const unsigned y = __shfl_up_sync(0xffffffffu, inc, o);
+                if (lane >= o)
+                    inc += y;
+            }
+            const unsigned exc = inc - sum;
+            if ((unsigned)r >= exc && (unsigned)r < inc) {
+                unsigned c = exc;
+                int i = 0;
+                for (; i < per - 1; i++) {
+                    if ((unsigned)r < c + hist[lane * per + i])
+                        break;
+                    c += hist[lane * per + i];
+                }
+                shared_pick[0] = lane * per + i;
+                shared_pick[1] = (int)c;
+            }
+        }
+        __syncthreads();
+        prefix |= (unsigned)shared_pick[0] << shift;
+        r -= shared_pick[1];
+        __syncthreads();
+    }
+    return prefix;
 }
 
 // Step 1 of the sample-select (one block per row): a strided sample of the
@@ -180,7 +213,7 @@ __device__ void bitonic_sort32(unsigned *a, int P)
 // sample) or the key window around the two middle ranks.
 __global__ void __launch_bounds__(1024)
 det_sample_kernel(const float *__restrict__ cc, size_t ld, DetState *__restrict__ st, int mode,
-                  float n_mad)
+                  float n_mad, float *__restrict__ saved)
 {
     extern __shared__ unsigned long long sample_smem[];
     unsigned *sk = reinterpret_cast<unsigned *>(sample_smem);  // kDetSample keys
@@ -194,27 +227,54 @@ det_sample_kernel(const float *__restrict__ cc, size_t ld, DetState *__restrict_
     int P = 1;
     while (P < m)
         P <<= 1;
-    for (int i = threadIdx.x; i < P; i += blockDim.x)
-        sk[i] = i < m ? sel_key(row[(long long)i * n / m], mode, s.med) : 0xffffffffu;
+    // sample positions floor(i * n / m) from a fixed-point step (no 64-bit division
+    // per sample); any spread of positions serves, the selection is exact.  The
+    // median pass gathers the sampled values from the row (scattered reads) and
+    // keeps them in `saved`; the MAD pass reads them back contiguously.
+    const unsigned long long stepq = ((unsigned long long)n << 20) / (unsigned long long)m;
+    float *sv = saved + (size_t)t * kDetSample;
+    for (int i = threadIdx.x; i < P; i += blockDim.x) {
+        unsigned key = 0xffffffffu;
+        if (i < m) {
+            float v;
+            if (mode == 0) {
+                long long pos = (long long)(((unsigned long long)i * stepq) >> 20);
+                v = row[pos < n ? pos : n - 1];
+                sv[i] = v;
+            } else {
+                v = sv[i];
+            }
+            key = sel_key(v, mode, s.med);
+        }
+        sk[i] = key;
+    }
     __syncthreads();
-    bitonic_sort32(sk, P);
+    // two order statistics of the sample (the padding keys, all ones, rank last):
+    // the exact middle values when the sample is the whole row; otherwise the keys
+    // bracketing the two middle ranks -- the sample position of rank r is about
+    // r*m/n, with a binomial standard deviation of at most sqrt(m)/2 = 64 positions:
+    // bracket by 6 of them
+    __shared__ unsigned hist[kDetBins];
+    __shared__ int pick[2];
+    const long long a = (n - 1) / 2, b = n / 2;
+    constexpr int kPad = 6 * 64 + 16;
+    const long long pa = a * m / n, pb = (b * m + n - 1) / n;
+    const int r0 = m == n ? (int)a : (int)(pa - kPad > 0 ? pa - kPad : 0);
+    const int r1 = m == n ? (int)b : (int)(pb + kPad < m - 1 ? pb + kPad : m - 1);
+    const unsigned k0 = block_select(sk, P, r0, hist, pick);
+    const unsigned k1 = r1 == r0 ? k0 : block_select(sk, P, r1, hist, pick);
     if (threadIdx.x != 0)
         return;
-    const long long a = (n - 1) / 2, b = n / 2;
     s.prefix[0] = s.prefix[1] = 0u;
     s.rank[0] = (int)a;
     s.rank[1] = (int)b;
     s.n_lt = s.n_in = 0;
-    if (m == n) {  // the whole row is sorted
-        finish_select(s, mode, middle_value(sk[a], sk[b], (int)n), n_mad);
+    if (m == n) {  // the whole row
+        finish_select(s, mode, middle_value(k0, k1, (int)n), n_mad);
         s.src = kSrcDone;
     } else {
-        // sample position of rank r is about r*m/n, with a binomial standard
-        // deviation of at most sqrt(m)/2 = 64 positions: bracket by 6 of them
-        constexpr int kPad = 6 * 64 + 16;
-        const long long pa = a * m / n, pb = (b * m + n - 1) / n;
-        s.klo = sk[pa - kPad > 0 ? pa - kPad : 0];
-        s.khi = sk[pb + kPad < m - 1 ? pb + kPad : m - 1];
+        s.klo = k0;
+        s.khi = k1;
         s.src = kSrcCand;
     }
     st[t] = s;
@@ -241,12 +301,15 @@ det_count_kernel(const float *__restrict__ cc, size_t ld, DetState *__restrict__
     // One warp step: each lane's up to 16 keys; the keys inside the window are
     // appended with one atomic per warp (a warp prefix sum places them).
     constexpr int kK = 16;
-    auto take = [&](const unsigned (&key)[kK], const bool (&ok)[kK]) {
+    const unsigned width = khi - klo;  // key - klo <= width  <=>  klo <= key <= khi
+    auto take = [&](const unsigned (&key)[kK], const bool (&ok)[kK], auto all_ok) {
+        constexpr bool ALL = decltype(all_ok)::value;  // every key of the step is in the row
         unsigned in_mask = 0;
 #pragma unroll
         for (int u = 0; u < kK; u++) {
-            lt += (ok[u] && key[u] < klo) ? 1u : 0u;
-            if (ok[u] && key[u] >= klo && key[u] <= khi)
+            const bool o = ALL || ok[u];
+            lt += (o && key[u] < klo) ? 1u : 0u;
+            if (o && key[u] - klo <= width)
                 in_mask |= 1u << u;
         }
         const int cnt = __popc(in_mask);
@@ -284,7 +347,7 @@ det_count_kernel(const float *__restrict__ cc, size_t ld, DetState *__restrict__
             ok[u] = false;
             key[u] = 0u;
         }
-        take(key, ok);
+        take(key, ok, std::false_type{});
     }
     const float4 *vrow = reinterpret_cast<const float4 *>(row + rs.head);
     const long long steps = (rs.nvec + 127) / 128;  // 128 float4s per warp step
@@ -316,7 +379,10 @@ det_count_kernel(const float *__restrict__ cc, size_t ld, DetState *__restrict__
             key[4 * u + 3] = sel_key(v[u].w, mode, med);
             ok[4 * u + 0] = ok[4 * u + 1] = ok[4 * u + 2] = ok[4 * u + 3] = okv;
         }
-        take(key, ok);
+        if (c * 128 + 128 <= rs.nvec)  // a whole step inside the row (warp-uniform)
+            take(key, ok, std::true_type{});
+        else
+            take(key, ok, std::false_type{});
     }
     for (int o = 16; o > 0; o >>= 1)
         lt += __shfl_down_sync(0xffffffffu, lt, o);
@@ -707,12 +773,14 @@ int detect_device(const float *cc, int T, int n_corr, size_t ld, const int *begi
     DetState *st;
     unsigned *hist, *keys;
     int2 *cand;
+    float *saved;
     // candidate keys per row: the sample window holds about 5 % of a row
     const long long key_cap = n_corr < 65536 ? n_corr : std::max(65536LL, (long long)n_corr / 8);
     if ((rc = ws.get(&st, (size_t)chunk, "detection state")) ||
         (rc = ws.get(&hist, (size_t)chunk * 2 * kDetBins, "detection histograms")) ||
         (rc = ws.get(&keys, (size_t)chunk * key_cap, "candidate keys")) ||
-        (rc = ws.get(&cand, (size_t)chunk * kDetCap, "candidate peaks")))
+        (rc = ws.get(&cand, (size_t)chunk * kDetCap, "candidate peaks")) ||
+        (rc = ws.get(&saved, (size_t)chunk * kDetSample, "sampled values")))
         return rc;
     cudaError_t e = cudaFuncSetAttribute(det_select_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)select_smem(kDetCap));
@@ -726,8 +794,9 @@ int detect_device(const float *cc, int T, int n_corr, size_t ld, const int *begi
     for (int t0 = 0; t0 < T; t0 += chunk) {
         const int nt = T - t0 < chunk ? T - t0 : chunk;
         const float *rows = cc + (size_t)t0 * ld;
-        // enough blocks per row to fill 152 SMs several times over
-        long long per_row = (152LL * 8 + nt - 1) / nt;
+        // enough blocks per row to fill the 152 SMs (8 resident blocks each) about eight
+        // times over, so that the last, partial wave of blocks costs little
+        long long per_row = (152LL * 8 * 8 + nt - 1) / nt;
         const long long row_cap = ((long long)n_corr + 1023) / 1024;
         if (per_row > row_cap)
             per_row = row_cap;
@@ -737,7 +806,8 @@ int detect_device(const float *cc, int T, int n_corr, size_t ld, const int *begi
         det_init_kernel<<<(nt + 127) / 128, 128, 0, s>>>(st, nt, n_corr, begin ? begin + t0 : nullptr,
                                                          end ? end + t0 : nullptr);
         for (int mode = 0; mode < 2; mode++) {
-            det_sample_kernel<<<nt, 1024, kDetSample * sizeof(unsigned), s>>>(rows, ld, st, mode, n_mad);
+            det_sample_kernel<<<nt, 1024, kDetSample * sizeof(unsigned), s>>>(rows, ld, st, mode, n_mad,
+                                                                               saved);
             det_count_kernel<<<grid, kDetThreads, 0, s>>>(rows, ld, st, keys, key_cap, mode);
             det_check_kernel<<<(nt + 127) / 128, 128, 0, s>>>(st, nt, key_cap);
             for (int pass = 0; pass < 3; pass++) {
