@@ -282,7 +282,7 @@ det_sample_kernel(const float *__restrict__ cc, size_t ld, DetState *__restrict_
 
 // Step 2: one pass over the row: keys below klo counted, keys inside
 // [klo, khi] appended to the row's candidate list (up to cap).
-__global__ void __launch_bounds__(kDetThreads)
+__global__ void __launch_bounds__(kDetThreads, 4)  // 32 warps per SM: enough loads in flight
 det_count_kernel(const float *__restrict__ cc, size_t ld, DetState *__restrict__ st,
                  unsigned *__restrict__ cand, long long cap, int mode)
 {
