@@ -612,7 +612,7 @@ def run_detection(cfg, dev_out, world, steps=3, warmup=1):
             "roofline": {"bound": "hbm", "achieved": gbs, "peak": peaks["hbm_gbs"],
                          "unit": "GB/s", "frac": gbs / peaks["hbm_gbs"],
                          "traffic": profiled_detect_traffic(rows),
-                         "traffic_source": "fmf_detect_64rows_day.md: DRAM bytes of one call's "
+                         "traffic_source": "fmf_detect_500rows_day.md: DRAM bytes of one call's "
                                            "launches per row byte, scaled to these rows",
                          "peak_source": "%s hbm_gbs (copy)" % peak_kind,
                          "kernel": "fmf_detect (det_hist x6, det_resolve x6, det_peaks, "
@@ -623,7 +623,7 @@ def profiled_detect_traffic(lags):
     """DRAM bytes of one detection call over `lags` row values, from the
     committed launch-list profile (bytes per row byte, which stays constant
     as the rows grow: every pass reads each row once)."""
-    path = os.path.join(HERE, "profiles", "fmf_detect_64rows_day.md")
+    path = os.path.join(HERE, "profiles", "fmf_detect_500rows_day.md")
     try:
         with open(path) as f:
             for line in f:
