@@ -973,7 +973,7 @@ __global__ void __launch_bounds__(tc_threads(VAR), 1) tc_persistent(const __grid
                         tmem_ldc<CH>(s_cols + c0, sv);
                         tmem_wait_ld();
                     }
-                    if constexpr (VAR) {  // the Fisher-z transform of every output, fused
+                    if constexpr (VAR && !PARTS) {  // the Fisher-z transform of every output, fused
                         const float zn = pr.P.vp_norm[t], zb = pr.P.vp_bias[t], zs = pr.P.vp_scale[t];
 #pragma unroll
                         for (int i = 0; i < CH; i++) {
@@ -1128,8 +1128,12 @@ static int n_sms()
     return n;
 }
 
-// out[i] = sum over parts j = 0..k-1 of part[j][i], in that order.
-__global__ void tc_parts_sum_kernel(const float *__restrict__ part, int k, long long m, float *__restrict__ out)
+// out[i] = sum over parts j = 0..k-1 of part[j][i], in that order; with
+// per-channel lengths (norm set) the Fisher-z transform of that sum,
+// (tanh(v / norm[t]) + bias[t]) * scale[t] for row t = i / n_corr.
+__global__ void tc_parts_sum_kernel(const float *__restrict__ part, int k, long long m, int n_corr,
+                                    const float *__restrict__ norm, const float *__restrict__ bias,
+                                    const float *__restrict__ scale, float *__restrict__ out)
 {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= m)
@@ -1137,6 +1141,10 @@ __global__ void tc_parts_sum_kernel(const float *__restrict__ part, int k, long 
     float v = part[i];
     for (int j = 1; j < k; j++)
         v += part[(size_t)j * m + i];
+    if (norm) {
+        const int t = (int)(i / n_corr);
+        v = (tanhf(v / norm[t]) + bias[t]) * scale[t];
+    }
     out[i] = v;
 }
 
@@ -1176,11 +1184,11 @@ int tc_run(const TcProb *probs, int n, int split, unsigned long long *queue, uns
     long long items = 0;
     size_t stage = 0;
     // A lone search with fewer (tile, template) items than SMs runs each item as k
-    // channel parts (network sum only; per-channel lengths need whole sums for
-    // their transform), k chosen to shorten the busiest SM's queue.  FMF_TC_PARTS=k
-    // overrides the choice where parts are allowed.
+    // channel parts (network sum only; with per-channel lengths the parts add raw
+    // Fisher-z sums and the transform follows the addition), k chosen to shorten the
+    // busiest SM's queue.  FMF_TC_PARTS=k overrides the choice where parts are allowed.
     const Problem &P0 = probs[0].P;
-    const bool can_split = n == 1 && !P0.ntap && P0.network_sum && P0.SC >= 2;
+    const bool can_split = n == 1 && P0.network_sum && P0.SC >= 2;
     const int parts = can_split ? tc_choose_parts((long long)probs[0].n_tiles * P0.T, P0.SC) : 1;
     Scratch pws(s);
     float *part_out = nullptr;
@@ -1220,8 +1228,9 @@ int tc_run(const TcProb *probs, int n, int split, unsigned long long *queue, uns
         n_var += probs[i].P.ntap != nullptr;
     if (n_var != 0 && n_var != n)
         return set_error(FMF_ERR_ARG, "a persistent launch mixes per-channel and fixed template lengths");
-    void (*kern)(const TcBatch) = n_var ? tc_persistent<true, false>
-                                  : (parts > 1 ? tc_persistent<false, true> : tc_persistent<false, false>);
+    void (*kern)(const TcBatch) =
+        n_var ? (parts > 1 ? tc_persistent<true, true> : tc_persistent<true, false>)
+              : (parts > 1 ? tc_persistent<false, true> : tc_persistent<false, false>);
     e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess)
         return set_error(FMF_ERR_CUDA, "tc_persistent shared memory (%zu bytes): %s", smem,
@@ -1232,7 +1241,9 @@ int tc_run(const TcProb *probs, int n, int split, unsigned long long *queue, uns
     if (rc || parts == 1)
         return rc;
     const long long m = (long long)P0.T * P0.n_corr;
-    tc_parts_sum_kernel<<<(unsigned)((m + 255) / 256), 256, 0, s>>>(part_out, parts, m, P0.out);
+    tc_parts_sum_kernel<<<(unsigned)((m + 255) / 256), 256, 0, s>>>(part_out, parts, m, P0.n_corr,
+                                                                     P0.ntap ? P0.vp_norm : nullptr,
+                                                                     P0.vp_bias, P0.vp_scale, P0.out);
     count_launch();
     return check_launch("tc_parts_sum_kernel");
 }

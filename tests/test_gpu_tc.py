@@ -114,3 +114,22 @@ def test_precision_stress_vs_fp64():
 def test_no_device_errors_after_tc_runs():
     from fast_matched_filter_gb300 import _lib
     assert _lib.load().fmf_device_errors() == 0
+
+
+@pytest.mark.parametrize("precision", ["fp32", "split_bf16"])
+def test_host_result_in_chunks_equals_device_result(monkeypatch, precision):
+    """A result above 64 MB goes to host memory in template chunks: every chunk's
+    kernels are queued first, then the copies (which block the host for numpy
+    arrays).  The result must equal, bit for bit, the same search on device
+    arrays in one launch."""
+    torch = pytest.importorskip("torch")
+    monkeypatch.setenv("FMF_TC_PARTS", "1")  # chunking only; channel parts change the sums
+    tp, mo, w, d = random_search(77, 20, 2, 1, 120, 1_050_000, 0, 60)
+    host = fmf.matched_filter(tp, mo, w, d, 1, check_zeros=False, precision=precision)
+    assert host.nbytes > 64 << 20
+    g = [torch.from_numpy(np.ascontiguousarray(x)).cuda() for x in
+         (tp, np.sum(tp ** 2, axis=-1).astype(np.float32), mo, w, d)]
+    out = torch.empty(host.shape, dtype=torch.float32, device="cuda")
+    fmf.matched_filter_device(*g, 1, out, precision=precision)
+    torch.cuda.synchronize()
+    assert np.array_equal(out.cpu().numpy(), host)

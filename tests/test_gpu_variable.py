@@ -210,11 +210,12 @@ def test_variable_launch_count_per_call():
 
 
 @pytest.mark.parametrize("precision", ["fp32", "split_bf16"])
-def test_variable_host_result_in_chunks_equals_device_result(precision):
+def test_variable_host_result_in_chunks_equals_device_result(monkeypatch, precision):
     """A result above 64 MB goes to host memory in template chunks whose copies
     overlap the later chunks' kernels; it must equal, bit for bit, the same
     search with device arrays (one launch, no chunks)."""
     torch = pytest.importorskip("torch")
+    monkeypatch.setenv("FMF_TC_PARTS", "1")  # chunking only; channel parts change the sums
     from fast_matched_filter_gb300 import _lib
     lib = _lib.load()
     rng = np.random.default_rng(31)
@@ -241,3 +242,28 @@ def test_variable_host_result_in_chunks_equals_device_result(precision):
     assert np.array_equal(np.isnan(got), np.isnan(host))
     ok = ~np.isnan(host)
     assert np.array_equal(got[ok], host[ok])
+
+
+@pytest.mark.parametrize("normalize", ["short", "full"])
+def test_variable_channel_parts(oracle_built, monkeypatch, normalize):
+    """A small per-channel-length search runs its tile items as channel parts:
+    the parts add raw Fisher-z sums and the transform follows the addition.
+    Forced k = 1, 3 and the automatic choice all meet the bar and agree."""
+    rng = np.random.default_rng(81)
+    tp, mo, w, d = random_search(82, 3, 3, 2, 140, 9000, -20, 120,
+                                 dc=2.0 if normalize == "full" else 0.0, zero_weights=2)
+    nt = rng.integers(40, 141, mo.shape).astype(np.int32)
+    nt[0, 0, 0] = 140
+    for idx in np.ndindex(nt.shape):
+        tp[idx][nt[idx]:] = 0.0
+    ref = oracle_built.run_oracle_variable(tp, nt, mo, w, d, 1, normalize)
+    got = {}
+    for k in ("1", "3", None):
+        if k is None:
+            monkeypatch.delenv("FMF_TC_PARTS", raising=False)
+        else:
+            monkeypatch.setenv("FMF_TC_PARTS", k)
+        got[k] = fmf.matched_filter(tp, mo, w, d, 1, n_samples_template=nt, check_zeros=False,
+                                    normalize=normalize, precision="split_bf16")
+        _check(got[k], ref, float(np.sum(w)), TOL_TC)
+    assert np.abs(got["1"] - got["3"]).max() <= 1e-5 * float(np.sum(w))
