@@ -133,3 +133,32 @@ def test_host_result_in_chunks_equals_device_result(monkeypatch, precision):
     fmf.matched_filter_device(*g, 1, out, precision=precision)
     torch.cuda.synchronize()
     assert np.array_equal(out.cpu().numpy(), host)
+
+
+def test_concurrent_calls_from_host_threads():
+    """The C ABI is reentrant: calls from several host threads at once (ctypes
+    drops the GIL; error state and launch bookkeeping are thread-local, the
+    device error word is allocated under a lock) give the results of the same
+    calls made one after another."""
+    import threading
+    cases = [random_search(900 + i, 3, 2, 2, 90 + 10 * i, 30000, 0, 100) for i in range(4)]
+    precs = ["fp32", "split_bf16", "split_bf16", "fp32"]
+    serial = [fmf.matched_filter(*c, 1, check_zeros=False, precision=p) for c, p in zip(cases, precs)]
+    results = [None] * len(cases)
+    errors = []
+
+    def work(i):
+        try:
+            for _ in range(3):
+                results[i] = fmf.matched_filter(*cases[i], 1, check_zeros=False, precision=precs[i])
+        except Exception as e:  # reported below
+            errors.append(e)
+
+    threads = [threading.Thread(target=work, args=(i,)) for i in range(len(cases))]
+    for th in threads:
+        th.start()
+    for th in threads:
+        th.join()
+    assert not errors, errors
+    for a, b in zip(serial, results):
+        assert np.array_equal(a, b)
