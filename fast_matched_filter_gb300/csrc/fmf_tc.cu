@@ -43,8 +43,13 @@
 //               issuing thread cannot keep the tensor pipe busy);
 //   warp 1      also allocates the TMEM (two accumulators + the network sum);
 //   warps 4-11  epilogue: tcgen05.ld of the accumulator, normalisation by the
-//               FP64 window statistics, threshold, weighted network sum in
-//               TMEM (channel order, fused multiply-add), outputs.
+//               window statistics, threshold, weighted network sum in TMEM
+//               (channel order, fused multiply-add), outputs.
+// Instantiations: tc_persistent<VAR, PARTS>.  VAR: per-channel template
+// lengths (the issuers cut each channel's K range at its own taps; 16 epilogue
+// warps, warps 4-19, form window sums from float-pair prefix sums and add
+// atanh(cc) * z).  PARTS: the items of a small search are split into channel
+// parts whose partial sums a second kernel adds in order.
 // Every wait is bounded (globaltimer); on timeout the CTA raises an error
 // word, stops issuing, waits for its own copies/MMAs (bounded) and frees TMEM.
 #include <cfloat>
