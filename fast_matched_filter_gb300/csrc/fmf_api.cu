@@ -275,8 +275,6 @@ int prepare_problem(const Args &a, Scratch &ws, cudaStream_t s, Problem *Pout, c
     P.normalize = a.normalize;
     P.network_sum = a.sum_mode != 0;
     P.ntap = nullptr;
-    P.pre2 = nullptr;
-    P.pre1 = nullptr;
     P.pre2f = nullptr;
     P.pre1f = nullptr;
     P.zweight = nullptr;

@@ -40,8 +40,6 @@ struct Problem {
     int network_sum;      // 1 weighted sum over channels, 0 per channel
     // Per-channel template lengths (Fisher-z network sum), else null:
     const int *ntap;      // (T, SC) taps of each channel (templates zero-padded to L)
-    const double *pre2;   // unused (FP64 prefix sums), null
-    const double *pre1;   // unused, null
     const float2 *pre2f;  // (SC, N+1) prefix sums of d^2 (centred d for full) as hi + lo floats
     const float2 *pre1f;  // (SC, N+1) prefix sums of centred d as hi + lo floats (full), else null
     const float *zweight; // (T, SC) Fisher-z weight of each channel

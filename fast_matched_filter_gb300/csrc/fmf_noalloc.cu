@@ -199,8 +199,6 @@ extern "C" int fmf_matched_filter_noalloc(const float *templates, const float *s
     P.normalize = normalize;
     P.network_sum = sum_cc_mode != 0;
     P.ntap = nullptr;
-    P.pre2 = nullptr;
-    P.pre1 = nullptr;
     P.pre2f = nullptr;
     P.pre1f = nullptr;
     P.zweight = nullptr;

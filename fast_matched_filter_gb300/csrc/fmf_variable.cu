@@ -473,8 +473,6 @@ static int variable_device(const VArgs &a, int L, cudaStream_t s, float *host_ou
     P.normalize = a.normalize;
     P.network_sum = 1;
     P.ntap = a.ntap;
-    P.pre2 = nullptr;
-    P.pre1 = nullptr;
     P.pre2f = pre2f;
     P.pre1f = pre1f;
     P.zweight = zweight;
