@@ -806,8 +806,8 @@ def run_batch(args):
     import fast_matched_filter_gb300 as fmf
     from fast_matched_filter_gb300 import synthetic
     torch.cuda.set_device(0)
-    shapes = synthetic.config3_shapes(max_templates=args.templates or 100,
-                                      max_samples=args.samples or 400000)
+    shapes = synthetic.config3_shapes(max_templates=args.templates or 500,
+                                      max_samples=args.samples or 4320000)
     probs, total_macs = [], 0
     for sh in shapes:
         cfg = synthetic.config3_problem(sh)
@@ -853,8 +853,8 @@ def run_batch(args):
             "warmup": args.warmup, "ms_per_step": ms_batch, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "bf16x3", "data": "synthetic",
             "config": {"workload": "config3_64_uneven_searches", "searches": len(shapes),
-                       "templates_max": args.templates or 100,
-                       "samples_max": args.samples or 400000,
+                       "templates_max": args.templates or 500,
+                       "samples_max": args.samples or 4320000,
                        "total_macs": total_macs, "shapes_seed": 103,
                        "form": "one CUDA graph: per-search preprocessing + persistent "
                                "tile-queue tensor-core launch"},
