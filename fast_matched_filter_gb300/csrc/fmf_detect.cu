@@ -302,6 +302,9 @@ det_count_kernel(const float *__restrict__ cc, size_t ld, DetState *__restrict__
     // appended with one atomic per warp (a warp prefix sum places them).
     constexpr int kK = 16;
     const unsigned width = khi - klo;  // key - klo <= width  <=>  klo <= key <= khi
+    // a lane's keys inside the window wait here (its own column), so that only
+    // the few candidates are written out, in a loop over the set bits
+    __shared__ unsigned stash[kWarps][kK][32];
     auto take = [&](const unsigned (&key)[kK], const bool (&ok)[kK], auto all_ok) {
         constexpr bool ALL = decltype(all_ok)::value;  // every key of the step is in the row
         unsigned in_mask = 0;
@@ -309,8 +312,10 @@ det_count_kernel(const float *__restrict__ cc, size_t ld, DetState *__restrict__
         for (int u = 0; u < kK; u++) {
             const bool o = ALL || ok[u];
             lt += (o && key[u] < klo) ? 1u : 0u;
-            if (o && key[u] - klo <= width)
+            if (o && key[u] - klo <= width) {
                 in_mask |= 1u << u;
+                stash[warp][u][lane] = key[u];
+            }
         }
         const int cnt = __popc(in_mask);
         int inc = cnt;
@@ -327,13 +332,9 @@ det_count_kernel(const float *__restrict__ cc, size_t ld, DetState *__restrict__
             base = atomicAdd(&st[t].n_in, total);
         base = __shfl_sync(0xffffffffu, base, 31);
         long long pos = (long long)base + inc - cnt;
-#pragma unroll
-        for (int u = 0; u < kK; u++)
-            if (in_mask & (1u << u)) {
-                if (pos < cap)
-                    list[pos] = key[u];
-                pos++;
-            }
+        for (unsigned m = in_mask; m; m &= m - 1u, pos++)
+            if (pos < cap)
+                list[pos] = stash[warp][__ffs(m) - 1][lane];
     };
     const RowSplit rs = split_row(row, n);
     if (blockIdx.x == 0 && warp == 0) {
