@@ -415,20 +415,30 @@ __global__ void det_check_kernel(DetState *__restrict__ st, int T, long long cap
 
 // Histogram update by a whole warp: every lane calls it (lanes whose value
 // does not count pass ok = false); lanes with the same digit add once.
+// With `aggregate` (the first pass, whose keys share few digits) lanes with
+// the same digit add once; otherwise (later passes, digits spread) each lane
+// adds its own count.
 __device__ __forceinline__ void hist_add(unsigned *h, float v, bool ok, int mode, float med, int shift,
                                          unsigned dmask, unsigned high, unsigned p0, unsigned p1,
-                                         bool two, int lane)
+                                         bool two, int lane, bool aggregate)
 {
     const unsigned key = mode == 2 ? __float_as_uint(v) : sel_key(v, mode, med);
     const unsigned dig = (key >> shift) & dmask;
     const bool m0 = ok && (key & high) == p0;
+    const bool m1 = two && ok && (key & high) == p1;
+    if (!aggregate) {
+        if (m0)
+            atomicAdd(&h[dig], 1u);
+        if (m1)
+            atomicAdd(&h[kDetBins + dig], 1u);
+        return;
+    }
     if (__any_sync(0xffffffffu, m0)) {
         const unsigned g = __match_any_sync(0xffffffffu, m0 ? dig : 0xffffffffu);
         if (m0 && (__ffs(g) - 1) == lane)
             atomicAdd(&h[dig], __popc(g));
     }
     if (two) {
-        const bool m1 = ok && (key & high) == p1;
         if (__any_sync(0xffffffffu, m1)) {
             const unsigned g = __match_any_sync(0xffffffffu, m1 ? dig : 0xffffffffu);
             if (m1 && (__ffs(g) - 1) == lane)
@@ -475,7 +485,7 @@ det_hist_kernel(const float *__restrict__ cc, size_t ld, const DetState *__restr
         const long long i = lane < rs.head ? lane : rs.head + 4 * rs.nvec + (lane - rs.head);
         const bool ok = lane < rs.head + rs.tail;
         const float v = ok ? row[i] : 0.f;
-        hist_add(h, v, ok, kmode, med, shift, dmask, high, p0, p1, two, lane);
+        hist_add(h, v, ok, kmode, med, shift, dmask, high, p0, p1, two, lane, pass == 0);
     }
     const float4 *vrow = reinterpret_cast<const float4 *>(row + rs.head);
     const long long steps = (rs.nvec + 63) / 64;  // 64 float4s per warp step
@@ -490,10 +500,10 @@ det_hist_kernel(const float *__restrict__ cc, size_t ld, const DetState *__restr
         }
 #pragma unroll
         for (int u = 0; u < 2; u++) {
-            hist_add(h, v[u].x, ok[u], kmode, med, shift, dmask, high, p0, p1, two, lane);
-            hist_add(h, v[u].y, ok[u], kmode, med, shift, dmask, high, p0, p1, two, lane);
-            hist_add(h, v[u].z, ok[u], kmode, med, shift, dmask, high, p0, p1, two, lane);
-            hist_add(h, v[u].w, ok[u], kmode, med, shift, dmask, high, p0, p1, two, lane);
+            hist_add(h, v[u].x, ok[u], kmode, med, shift, dmask, high, p0, p1, two, lane, pass == 0);
+            hist_add(h, v[u].y, ok[u], kmode, med, shift, dmask, high, p0, p1, two, lane, pass == 0);
+            hist_add(h, v[u].z, ok[u], kmode, med, shift, dmask, high, p0, p1, two, lane, pass == 0);
+            hist_add(h, v[u].w, ok[u], kmode, med, shift, dmask, high, p0, p1, two, lane, pass == 0);
         }
     }
     __syncthreads();
