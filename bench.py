@@ -1,8 +1,8 @@
 """Benchmark of the matched-filter hot path on GB300.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload config4|config1|config2|config0|config3|variable]
-                    [--precision ...]
+                    [--workload config4|config1|config2|config0|config3|variable|variable_full]
+                    [--precision ...] [--templates T] [--samples N]
 
 One *step* is one complete search of the workload (every template against
 every channel and output index: preprocessing kernels + correlation
@@ -18,6 +18,11 @@ kernel).  Metric: template*lag*channel multiply-accumulates per second
   roofline  the correlation kernel, event-timed inside the timed region.
   cpu_baseline  the oracle's C port of the reference CPU algorithm (OpenMP,
             all host cores) on a bounded sample of the same workload.
+
+Workloads: config4 the full-day search (default); config1 a continuous record;
+config2 DC offsets with 'full' normalisation and step 2; config0 the small case;
+config3 64 uneven searches in one batched launch; variable / variable_full
+per-channel template lengths with the Fisher-z network sum.
 
 --impl reference times that CPU algorithm alone (rank 0; other ranks exit).
 Under torchrun each rank searches its own template set against the same
