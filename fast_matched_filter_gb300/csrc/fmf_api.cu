@@ -103,8 +103,7 @@ __global__ void template_center_kernel(const float *, int, float *, float *);
 __global__ void template_energy_kernel(const float *, int, int, float *);
 __global__ void channel_mean_kernel(const float *, int, float *);
 __global__ void zero_count_kernel(const float *, long long, long long, long long, unsigned long long *);
-__global__ void window_stats_kernel(const float *, int, int, int, const float *, float *,
-                                    float *, float *);
+__global__ void window_stats_kernel(const float *, int, int, int, const float *, float *, float *);
 int launch_tc(const Problem &P, const float *data_for_tc, int precision, unsigned *err, Scratch &ws,
               cudaStream_t s, int forced_nb, int template_group);
 int launch_wait_selftest(unsigned *err, unsigned ms, cudaStream_t s);
@@ -209,15 +208,14 @@ int prepare_problem(const Args &a, Scratch &ws, cudaStream_t s, Problem *Pout, c
         return set_error(FMF_ERR_SMEM, "template length %d too long for the window-statistics kernel", L);
 
     int *k_lo, *k_hi;
-    float *stat_e, *stat_m = nullptr, *mu = nullptr, *dcen = nullptr, *tcen = nullptr, *tsum = nullptr;
+    float *stat_e, *mu = nullptr, *dcen = nullptr, *tcen = nullptr, *tsum = nullptr;
     if ((rc = ws.get(&k_lo, 2 * (size_t)T, "template ranges")))
         return rc;
     k_hi = k_lo + T;
-    if ((rc = ws.get(&stat_e, (size_t)SC * N, "window energies")))
+    if ((rc = ws.get(&stat_e, (size_t)SC * N * (full ? 2 : 1), "window statistics")))
         return rc;
     if (full) {
-        if ((rc = ws.get(&stat_m, (size_t)SC * N, "window means")) ||
-            (rc = ws.get(&mu, (size_t)SC, "channel means")) ||
+        if ((rc = ws.get(&mu, (size_t)SC, "channel means")) ||
             (rc = ws.get(&dcen, (size_t)SC * N, "centred data")) ||
             (rc = ws.get(&tcen, (size_t)T * SC * L, "centred templates")) ||
             (rc = ws.get(&tsum, (size_t)T * SC, "template sums")))
@@ -248,8 +246,7 @@ int prepare_problem(const Args &a, Scratch &ws, cudaStream_t s, Problem *Pout, c
                           "window statistics shared memory")))
         return rc;
     dim3 sgrid((N + kStatBlock - 1) / kStatBlock, SC);
-    window_stats_kernel<<<sgrid, 256, stat_smem, s>>>(a.data, N, L, kStatBlock, mu, dcen, stat_e,
-                                                      stat_m);
+    window_stats_kernel<<<sgrid, 256, stat_smem, s>>>(a.data, N, L, kStatBlock, mu, dcen, stat_e);
     count_launch();
     if ((rc = check_launch("preprocessing kernels")))
         return rc;
@@ -262,7 +259,6 @@ int prepare_problem(const Args &a, Scratch &ws, cudaStream_t s, Problem *Pout, c
     P.w = a.w;
     P.data = full ? dcen : a.data;
     P.stat_e = stat_e;
-    P.stat_m = stat_m;
     P.k_lo = k_lo;
     P.k_hi = k_hi;
     P.out = a.out;

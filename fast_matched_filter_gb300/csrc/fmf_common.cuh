@@ -30,8 +30,8 @@ struct Problem {
     const int *mo;        // (T, SC) moveouts
     const float *w;       // (T, SC) weights
     const float *data;    // (SC, N) data; centred per channel for "full"
-    const float *stat_e;  // (SC, N) window energy (short) / centred ssd (full), window starts at the index
-    const float *stat_m;  // (SC, N) centred window mean ("full"), else null
+    const float *stat_e;  // short: (SC, N) window energy; full: (SC, N) float pairs (centred
+                          // energy, centred mean), one 8-byte load per lag; window starts at the index
     const int *k_lo;      // (T) first valid output index
     const int *k_hi;      // (T) one past the last valid output index (<= n_corr)
     float *out;           // (T, n_corr) or (T, n_corr, SC)

@@ -38,8 +38,7 @@ namespace fmf {
 __global__ void template_range_kernel(const int *, int, int, int, int, int, int, int *, int *);
 __global__ void template_center_kernel(const float *, int, float *, float *);
 __global__ void channel_mean_kernel(const float *, int, float *);
-__global__ void window_stats_kernel(const float *, int, int, int, const float *, float *,
-                                    float *, float *);
+__global__ void window_stats_kernel(const float *, int, int, int, const float *, float *, float *);
 int launch_plain(const Problem &P, cudaStream_t stream);
 
 // The only working memory of fmf_matched_filter_noalloc.  In host code this
@@ -92,9 +91,12 @@ struct Carve {
 size_t scratch_bytes(size_t T, size_t SC, size_t L, size_t N, bool full)
 {
     auto al = [](size_t b) { return (b + 255) & ~size_t(255); };
-    size_t b = al(2 * T * sizeof(int)) + al(SC * N * sizeof(float));
+    // the carve of fmf_matched_filter_noalloc: ranges, window statistics (full:
+    // (energy, mean) pairs), then for full the centred data, channel means,
+    // centred templates and their sums
+    size_t b = al(2 * T * sizeof(int)) + al(SC * N * sizeof(float) * (full ? 2 : 1));
     if (full)
-        b += 2 * al(SC * N * sizeof(float)) + al(SC * sizeof(float)) + al(T * SC * L * sizeof(float)) +
+        b += al(SC * N * sizeof(float)) + al(SC * sizeof(float)) + al(T * SC * L * sizeof(float)) +
              al(T * SC * sizeof(float));
     return b;
 }
@@ -146,10 +148,9 @@ extern "C" int fmf_matched_filter_noalloc(const float *templates, const float *s
     Carve cv{base};
     int *k_lo = cv.take<int>(2 * (size_t)T);
     int *k_hi = k_lo + T;
-    float *stat_e = cv.take<float>((size_t)SC * N);
-    float *stat_m = nullptr, *dcen = nullptr, *mu = nullptr, *tcen = nullptr, *tsum = nullptr;
+    float *stat_e = cv.take<float>((size_t)SC * N * (full ? 2 : 1));
+    float *dcen = nullptr, *mu = nullptr, *tcen = nullptr, *tsum = nullptr;
     if (full) {
-        stat_m = cv.take<float>((size_t)SC * N);
         dcen = cv.take<float>((size_t)SC * N);
         mu = cv.take<float>((size_t)SC);
         tcen = cv.take<float>((size_t)T * SC * L);
@@ -168,8 +169,7 @@ extern "C" int fmf_matched_filter_noalloc(const float *templates, const float *s
     if (e != cudaSuccess)
         return set_error(FMF_ERR_CUDA, "noalloc: statistics shared memory: %s", cudaGetErrorString(e));
     dim3 sgrid((N + kNoallocStatBlock - 1) / kNoallocStatBlock, SC);
-    window_stats_kernel<<<sgrid, 256, stat_smem, s>>>(data, N, L, kNoallocStatBlock, mu, dcen, stat_e,
-                                                      stat_m);
+    window_stats_kernel<<<sgrid, 256, stat_smem, s>>>(data, N, L, kNoallocStatBlock, mu, dcen, stat_e);
     if ((e = cudaGetLastError()) != cudaSuccess)
         return set_error(FMF_ERR_CUDA, "noalloc: preprocessing launch: %s", cudaGetErrorString(e));
     if (!sum_cc_mode) {
@@ -186,7 +186,6 @@ extern "C" int fmf_matched_filter_noalloc(const float *templates, const float *s
     P.w = weights;
     P.data = full ? dcen : data;
     P.stat_e = stat_e;
-    P.stat_m = stat_m;
     P.k_lo = k_lo;
     P.k_hi = k_hi;
     P.out = cc_out;

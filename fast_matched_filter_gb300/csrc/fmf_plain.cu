@@ -243,16 +243,21 @@ plain_kernel(const Problem P, const PlainGeom g)
                 const float sst = P.sst[row], wc = w[ch];
                 const float ts = P.normalize ? P.tsum[row] : 0.0f;
                 const float *se = P.stat_e + (size_t)ch * P.N;
-                const float *sm = P.normalize ? P.stat_m + (size_t)ch * P.N : nullptr;
+                const float2 *sem = reinterpret_cast<const float2 *>(P.stat_e) + (size_t)ch * P.N;
 #pragma unroll
                 for (int r = 0; r < PL_R; r++) {
                     long long k = k0 + tid * PL_R + r;
                     if (k >= klo && k < khi) {
                         long long u = k * P.step + mo[ch];
-                        float num = acc[r];
-                        if (P.normalize)
-                            num = fmaf(-sm[u], ts, num);
-                        float den = sst * se[u];
+                        float num = acc[r], energy;
+                        if (P.normalize) {  // (centred energy, mean) pairs
+                            const float2 em = sem[u];
+                            num = fmaf(-em.y, ts, num);
+                            energy = em.x;
+                        } else {
+                            energy = se[u];
+                        }
+                        float den = sst * energy;
                         float cc = den > kThreshold ? num / sqrtf(den) : 0.0f;
                         if (P.network_sum)
                             net[r * PL_THREADS + tid] = fmaf(cc, wc, net[r * PL_THREADS + tid]);

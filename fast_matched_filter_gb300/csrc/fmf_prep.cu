@@ -302,8 +302,7 @@ __device__ void block_scan_pair(float2 *a, int len, float2 *part)
 __global__ void window_stats_kernel(const float *__restrict__ data, int N, int L,
                                     int B, const float *__restrict__ mu,
                                     float *__restrict__ dcen,
-                                    float *__restrict__ stat_e,
-                                    float *__restrict__ stat_m)
+                                    float *__restrict__ stat_e)
 {
     extern __shared__ float2 shp[];
     __shared__ float2 part[33];
@@ -340,8 +339,7 @@ __global__ void window_stats_kernel(const float *__restrict__ data, int N, int L
         if (full) {
             float v, mean;
             window_centred(P2[u], P2[u + L], P1[u], P1[u + L], Lf, invL, v, mean);
-            stat_e[o] = v;
-            stat_m[o] = mean;
+            reinterpret_cast<float2 *>(stat_e)[o] = make_float2(v, mean);
         } else {
             float e;
             const float2 a2 = P2[u], b2 = P2[u + L];

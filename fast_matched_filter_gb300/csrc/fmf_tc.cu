@@ -782,7 +782,6 @@ __global__ void __launch_bounds__(tc_threads(VAR), 1) tc_persistent(const __grid
             const int SC = pr.P.SC, step = pr.P.step, n_corr = pr.P.n_corr, N = pr.P.N;
             const bool full = pr.P.normalize != 0, nsum = pr.P.network_sum != 0;
             const float *__restrict__ stat_e = pr.P.stat_e;
-            const float *__restrict__ stat_m = pr.P.stat_m;
             const float *__restrict__ sstp = pr.P.sst;
             const float *__restrict__ tsump = pr.P.tsum;
             float *outp = pr.P.out;
@@ -810,8 +809,10 @@ __global__ void __launch_bounds__(tc_threads(VAR), 1) tc_persistent(const __grid
                 const float sst = sstp[row];
                 const float ts = full ? tsump[row] : 0.0f;
                 const long long u0 = (kb + (long long)TC_Q * a0) * step + mo[ch];
+                // short: window energies; full: (centred energy, mean) pairs
                 const float *__restrict__ se = VAR ? nullptr : stat_e + (size_t)ch * N + u0;
-                const float *__restrict__ sm = (VAR || !full) ? se : stat_m + (size_t)ch * N + u0;
+                const float2 *__restrict__ sem =
+                    VAR ? nullptr : reinterpret_cast<const float2 *>(stat_e) + (size_t)ch * N + u0;
                 float *oc = outp + ((size_t)t * n_corr + kb + (long long)TC_Q * a0) * SC + ch;
                 // statistics: all loads of a chunk issued together (indices clamped into the
                 // valid range) before any use; the first chunk before waiting for the accumulator
@@ -820,8 +821,14 @@ __global__ void __launch_bounds__(tc_threads(VAR), 1) tc_persistent(const __grid
 #pragma unroll
                     for (int i = 0; i < CH; i++) {
                         const int ac = min(max(c0 + i, a_lo), a_hi - 1);
-                        e[i] = any ? __ldg(se + ac * qs) : 0.0f;
-                        mm[i] = (any && full) ? __ldg(sm + ac * qs) : 0.0f;
+                        if (full) {
+                            const float2 em = any ? __ldg(sem + ac * qs) : make_float2(0.0f, 0.0f);
+                            e[i] = em.x;
+                            mm[i] = em.y;
+                        } else {
+                            e[i] = any ? __ldg(se + ac * qs) : 0.0f;
+                            mm[i] = 0.0f;
+                        }
                     }
                 };
                 if constexpr (!VAR)

@@ -460,7 +460,6 @@ static int variable_device(const VArgs &a, int L, cudaStream_t s, float *host_ou
     P.w = a.w;
     P.data = full ? dcen : a.data;
     P.stat_e = nullptr;
-    P.stat_m = nullptr;
     P.k_lo = k_lo;
     P.k_hi = k_hi;
     P.out = a.out;
