@@ -511,8 +511,10 @@ int launch_fisher_atanh(const float *y, float *out, long long n, cudaStream_t s)
 // VAR: per-channel template lengths (Problem::ntap set in every search of the
 // batch), a separate instantiation so that the fixed-length epilogue keeps
 // its registers.  PARTS: every search runs its items as channel parts
-// (TcProb::parts), a separate instantiation for the same reason.
-template <bool VAR, bool PARTS>
+// (TcProb::parts), a separate instantiation for the same reason.  NORM: 0 every
+// search 'short', 1 every search 'full', -1 each search's own (a batch mixing
+// both); the fixed modes drop the other mode's epilogue code.
+template <bool VAR, bool PARTS, int NORM>
 __global__ void __launch_bounds__(tc_threads(VAR), 1) tc_persistent(const __grid_constant__ TcBatch B)
 {
     constexpr int TC_EPI_WARPS = tc_epi_warps(VAR);
@@ -780,7 +782,8 @@ __global__ void __launch_bounds__(tc_threads(VAR), 1) tc_persistent(const __grid
             const int a0 = cgroup * NC;
             const uint32_t s_cols = lane_base + (uint32_t)(TC_NACC * TC_NB_MAX + a0);
             const int SC = pr.P.SC, step = pr.P.step, n_corr = pr.P.n_corr, N = pr.P.N;
-            const bool full = pr.P.normalize != 0, nsum = pr.P.network_sum != 0;
+            const bool full = NORM >= 0 ? NORM == 1 : pr.P.normalize != 0;
+            const bool nsum = pr.P.network_sum != 0;
             const float *__restrict__ stat_e = pr.P.stat_e;
             const float *__restrict__ sstp = pr.P.sst;
             const float *__restrict__ tsump = pr.P.tsum;
@@ -1240,9 +1243,19 @@ int tc_run(const TcProb *probs, int n, int split, unsigned long long *queue, uns
         n_var += probs[i].P.ntap != nullptr;
     if (n_var != 0 && n_var != n)
         return set_error(FMF_ERR_ARG, "a persistent launch mixes per-channel and fixed template lengths");
-    void (*kern)(const TcBatch) =
-        n_var ? (parts > 1 ? tc_persistent<true, true> : tc_persistent<true, false>)
-              : (parts > 1 ? tc_persistent<false, true> : tc_persistent<false, false>);
+    int n_full = 0;
+    for (int i = 0; i < n; i++)
+        n_full += probs[i].P.normalize != 0;
+    const int norm = n_full == 0 ? 0 : (n_full == n ? 1 : -1);
+    void (*kern)(const TcBatch);
+    if (n_var)
+        kern = parts > 1 ? tc_persistent<true, true, -1> : tc_persistent<true, false, -1>;
+    else if (parts > 1)
+        kern = norm == 0 ? tc_persistent<false, true, 0>
+                         : (norm == 1 ? tc_persistent<false, true, 1> : tc_persistent<false, true, -1>);
+    else
+        kern = norm == 0 ? tc_persistent<false, false, 0>
+                         : (norm == 1 ? tc_persistent<false, false, 1> : tc_persistent<false, false, -1>);
     e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess)
         return set_error(FMF_ERR_CUDA, "tc_persistent shared memory (%zu bytes): %s", smem,
