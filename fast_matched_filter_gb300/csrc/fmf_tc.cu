@@ -1248,7 +1248,10 @@ int tc_run(const TcProb *probs, int n, int split, unsigned long long *queue, uns
         n_full += probs[i].P.normalize != 0;
     const int norm = n_full == 0 ? 0 : (n_full == n ? 1 : -1);
     void (*kern)(const TcBatch);
-    if (n_var)
+    if (n_var && norm >= 0)  // per-channel lengths: always one search, one normalisation
+        kern = parts > 1 ? (norm == 0 ? tc_persistent<true, true, 0> : tc_persistent<true, true, 1>)
+                         : (norm == 0 ? tc_persistent<true, false, 0> : tc_persistent<true, false, 1>);
+    else if (n_var)
         kern = parts > 1 ? tc_persistent<true, true, -1> : tc_persistent<true, false, -1>;
     else if (parts > 1)
         kern = norm == 0 ? tc_persistent<false, true, 0>
