@@ -151,7 +151,7 @@ struct Scratch {
 };
 
 // Preprocessing shared by every form: per-template lag ranges, 'full'
-// centring, FP64 window statistics (fmf_api.cu).  Fills the epilogue fields of
+// centring, double-float window statistics (fmf_api.cu).  Fills the epilogue fields of
 // *P and the data the numerator kernels read (centred for 'full').
 struct Args {
     const float *tpl, *sst, *data, *w;

@@ -28,7 +28,7 @@
 // issues almost nothing but loads and FMAs.
 //
 // Epilogue per channel (fused): numerator of "full" minus m*sum(t'),
-// den = sst * E (E and m from the FP64 window statistics), threshold 1e-6 on
+// den = sst * E (E and m from the double-float window statistics), threshold 1e-6 on
 // den, cc = num / sqrt(den), network sum acc = fma(cc, w, acc) in channel
 // order (the reference's accumulation, matched_filter.c:450).  Outputs
 // outside [k_lo, k_hi) are written as 0.
@@ -207,7 +207,8 @@ plain_kernel(const Problem P, const PlainGeom g)
             }
             compute_phase(smem + b * g.stage_floats, g, taps, acc);
             if (phi == P.step - 1 && P.ntap) {
-                // per-channel template length: FP64 window sums of that length,
+                // per-channel template length: window sums of that length from the
+                // float-pair prefix sums,
                 // the 'precise' threshold (on the square root, matched_filter.c:650-652)
                 // and a Fisher-z network sum (matched_filter.c:596-601)
                 const size_t row = (size_t)t * P.SC + ch;

@@ -871,7 +871,7 @@ __global__ void __launch_bounds__(tc_threads(VAR), 1) tc_persistent(const __grid
                             mbar_arrive(dempty0 + 8 * d);
                     }
                     if constexpr (VAR) {
-                        // window sums of the channel's own length from the FP64 prefix sums,
+                        // window sums of the channel's own length from the float-pair prefix sums,
                         // the 'precise' threshold on the square root, and
                         // atanh(cc - 10 eps) * z into the network sum
                         // CHECK: some output of the warp lies outside the valid lags (clamped

@@ -18,7 +18,7 @@
 // Kernels: metadata (Fisher-z weights per (t, ch), lag ranges and weight sums
 // per template, the cumulative scale in one thread, each in the reference's
 // float operation order),
-// masked/centred templates, FP64 prefix sums of d^2 and d stored as float
+// masked/centred templates, double-float prefix sums of d^2 and d stored as float
 // pairs (global, so that any window length is a few FP32 operations), the
 // numerator kernel with its
 // variable-length epilogue -- the plain FP32 kernel (fmf_plain.cu) or the
