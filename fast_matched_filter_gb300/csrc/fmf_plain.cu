@@ -157,6 +157,9 @@ __device__ __forceinline__ void compute_phase(const float *buf, const PlainGeom 
     }
 }
 
+// FULL: 'full' normalisation; VAR: per-channel template lengths (Problem::ntap)
+// -- one instantiation per mode, so that each keeps only its own epilogue code.
+template <bool FULL, bool VAR>
 __global__ void __launch_bounds__(PL_THREADS, 2)
 plain_kernel(const Problem P, const PlainGeom g)
 {
@@ -200,31 +203,31 @@ plain_kernel(const Problem P, const PlainGeom g)
             // per-channel template lengths: the taps past the channel's own length are
             // zeros, so the phase stops after its own taps (rounded up to PL_U)
             int taps = g.lq_pad;
-            if (P.ntap) {
+            if constexpr (VAR) {
                 const int n = P.ntap[(size_t)t * P.SC + ch];
                 const int own = n > phi ? (n - phi + P.step - 1) / P.step : 0;
                 taps = min(g.lq_pad, (own + PL_U - 1) / PL_U * PL_U);
             }
             compute_phase(smem + b * g.stage_floats, g, taps, acc);
-            if (phi == P.step - 1 && P.ntap) {
+            if (VAR && phi == P.step - 1) {
                 // per-channel template length: window sums of that length from the
                 // float-pair prefix sums,
                 // the 'precise' threshold (on the square root, matched_filter.c:650-652)
                 // and a Fisher-z network sum (matched_filter.c:596-601)
                 const size_t row = (size_t)t * P.SC + ch;
                 const float sst = P.sst[row], zw = P.zweight[row];
-                const float ts = P.normalize ? P.tsum[row] : 0.0f;
+                const float ts = FULL ? P.tsum[row] : 0.0f;
                 const int n = P.ntap[row];
                 const float nf = (float)n, inv_n = 1.0f / nf;
                 const float2 *p2 = P.pre2f + (size_t)ch * (P.N + 1);
-                const float2 *p1 = P.normalize ? P.pre1f + (size_t)ch * (P.N + 1) : nullptr;
+                const float2 *p1 = FULL ? P.pre1f + (size_t)ch * (P.N + 1) : nullptr;
 #pragma unroll
                 for (int r = 0; r < PL_R; r++) {
                     long long k = k0 + tid * PL_R + r;
                     if (k >= klo && k < khi) {
                         const long long u = k * P.step + mo[ch];
                         float num = acc[r], ssd;
-                        if (P.normalize) {
+                        if (FULL) {
                             float mean;
                             window_centred(p2[u], p2[u + n], p1[u], p1[u + n], nf, inv_n, ssd, mean);
                             num = fmaf(-mean, ts, num);
@@ -242,7 +245,7 @@ plain_kernel(const Problem P, const PlainGeom g)
                 // fused epilogue of channel ch
                 const size_t row = (size_t)t * P.SC + ch;
                 const float sst = P.sst[row], wc = w[ch];
-                const float ts = P.normalize ? P.tsum[row] : 0.0f;
+                const float ts = FULL ? P.tsum[row] : 0.0f;
                 const float *se = P.stat_e + (size_t)ch * P.N;
                 const float2 *sem = reinterpret_cast<const float2 *>(P.stat_e) + (size_t)ch * P.N;
 #pragma unroll
@@ -251,7 +254,7 @@ plain_kernel(const Problem P, const PlainGeom g)
                     if (k >= klo && k < khi) {
                         long long u = k * P.step + mo[ch];
                         float num = acc[r], energy;
-                        if (P.normalize) {  // (centred energy, mean) pairs
+                        if (FULL) {  // (centred energy, mean) pairs
                             const float2 em = sem[u];
                             num = fmaf(-em.y, ts, num);
                             energy = em.x;
@@ -293,15 +296,17 @@ int launch_plain(const Problem &P, cudaStream_t stream)
         return set_error(FMF_ERR_SMEM,
                          "template length %d with step %d needs %zu bytes of shared memory (max 232448)",
                          P.L, P.step, g.smem);
-    cudaError_t e = cudaFuncSetAttribute(plain_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)g.smem);
+    void (*kern)(const Problem, const PlainGeom) =
+        P.ntap ? (P.normalize ? plain_kernel<true, true> : plain_kernel<false, true>)
+               : (P.normalize ? plain_kernel<true, false> : plain_kernel<false, false>);
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)g.smem);
     if (e != cudaSuccess)
         return set_error(FMF_ERR_CUDA, "plain kernel shared memory (%zu bytes): %s", g.smem,
                          cudaGetErrorString(e));
     const long long n_tiles = (P.n_corr + PL_TILE - 1) / PL_TILE;
     if (n_tiles * P.T > 0x7fffffffLL)
         return set_error(FMF_ERR_ARG, "too many (template, tile) pairs for one launch");
-    plain_kernel<<<(unsigned)(n_tiles * P.T), PL_THREADS, g.smem, stream>>>(P, g);
+    kern<<<(unsigned)(n_tiles * P.T), PL_THREADS, g.smem, stream>>>(P, g);
     count_launch();
     return check_launch("plain_kernel");
 }
