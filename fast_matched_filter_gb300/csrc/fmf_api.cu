@@ -152,7 +152,9 @@ int collect_device_errors()
     return FMF_OK;
 }
 
-static void keep_pool_cached()
+// The device's default pool keeps the memory that calls free (release threshold
+// at its maximum), so that the next call reuses it instead of mapping it again.
+void keep_pool_cached()
 {
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess)

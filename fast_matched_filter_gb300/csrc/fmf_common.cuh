@@ -116,6 +116,7 @@ namespace fmf {
 int set_error(int status, const char *fmt, ...);
 void count_launch(int n = 1);
 void reset_launch_count();  // at the start of every entry point (fmf_last_launch_count)
+void keep_pool_cached();    // at the start of every entry point that allocates scratch
 int check_launch(const char *what);
 
 // Stream-ordered scratch allocations (cudaMallocAsync from the device's

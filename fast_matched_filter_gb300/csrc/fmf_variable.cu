@@ -581,6 +581,7 @@ static int variable_entry(const VArgs &a, void *stream)
             if ((uintptr_t)p & 3)
                 return set_error(FMF_ERR_ARG, "device array %p is not 4-byte aligned", p);
     }
+    keep_pool_cached();
     cudaGetLastError();
     cudaStream_t s = (cudaStream_t)stream;
     const size_t n_meta = a.T * a.S * a.C;
