@@ -2,7 +2,7 @@
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
                     [--workload config4|config1|config2|config0|config3|variable|variable_full]
-                    [--precision ...] [--templates T] [--samples N]
+                    [--precision ...] [--templates T] [--samples N] [--frontend]
 
 One *step* is one complete search of the workload (every template against
 every channel and output index: preprocessing kernels + correlation
@@ -16,6 +16,8 @@ kernel).  Metric: template*lag*channel multiply-accumulates per second
             pinned host buffers: H2D of every input and D2H of the whole
             output inside each timed step.
   roofline  the correlation kernel, event-timed inside the timed region.
+  frontend_numpy  (--frontend) the drop-in Python call on the workload's
+            numpy arrays (pageable host memory), wall clock per call.
   cpu_baseline  the oracle's C port of the reference CPU algorithm (OpenMP,
             all host cores) on a bounded sample of the same workload.
 
@@ -67,6 +69,8 @@ def parse_args(argv=None):
                    help="skip the FP64 error report on a subset")
     p.add_argument("--no-detect", action="store_true",
                    help="skip the detection leg (threshold + peaks on the search output)")
+    p.add_argument("--frontend", action="store_true",
+                   help="also time the drop-in Python call on numpy (pageable) arrays")
     p.add_argument("--templates", type=int, default=0, help="override T (smaller runs)")
     p.add_argument("--samples", type=int, default=0, help="override N (smaller runs)")
     return p.parse_args(argv)
@@ -403,6 +407,8 @@ def run_ours(args):
             line["e2e_search_detect"] = run_e2e_detect(cfg, precision, args, world, lib)
     del out
     torch.cuda.empty_cache()
+    if args.frontend and world == 1:
+        line["frontend_numpy"] = run_frontend(cfg, precision, args)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(cfg)
     if rank == 0:
@@ -544,6 +550,29 @@ def precision_report(cfg, n_templates=2, n_lags=50000):
                                                                                    ref.shape[1])
     torch.cuda.synchronize()
     return out
+
+
+def run_frontend(cfg, precision, args):
+    """The drop-in call as a user of the reference makes it: fmf.matched_filter
+    on the workload's numpy arrays (pageable host memory, a fresh numpy output
+    per call, check_zeros='first' as the reference's default), wall clock per
+    call after one untimed call."""
+    import torch
+    import fast_matched_filter_gb300 as fmf
+    secs, got = [], None
+    for i in range(1 + args.steps):
+        got = None  # free the previous output first
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        got = fmf.matched_filter(cfg["templates"], cfg["moveouts"], cfg["weights"], cfg["data"],
+                                 cfg["step"], arch="gpu", check_zeros="first",
+                                 normalize=cfg["normalize"], network_sum=cfg["network_sum"],
+                                 precision=precision)
+        secs.append(time.perf_counter() - t)
+    med = float(np.median(secs[1:]))
+    return {"value": cfg["macs"] / med / 1e12, "unit": UNIT, "seconds": secs[1:],
+            "first_call_s": secs[0], "output_shape": list(got.shape),
+            "api": "fmf.matched_filter(..., arch='gpu') on numpy arrays (pageable host memory)"}
 
 
 def run_e2e(cfg, dev_out, precision, args, world, lib):
