@@ -178,7 +178,7 @@ def _addr(a):
 
 def matched_filter(templates, moveouts, weights, data, step,
                    n_samples_template=None, arch="gpu", check_zeros="first",
-                   normalize="short", network_sum=True, precision="fp32"):
+                   normalize="short", network_sum=True, precision="fp32", out=None):
     """Correlation coefficients between ``templates`` and ``data``
     (reference: fast_matched_filter.py:66-362).
 
@@ -192,6 +192,10 @@ def matched_filter(templates, moveouts, weights, data, step,
     normalize : 'short' or 'full' (window mean removed).
     network_sum : True -> (T, n_corr) weighted sums; False -> (T, n_corr, S, C).
     precision : 'fp32' | 'split_bf16' | 'bf16' (numerator arithmetic).
+    out : optional writable, C-contiguous float32 array of the output's shape;
+        every element is written and ``out`` is returned.  Reusing one array
+        (or a page-locked one) across calls saves allocating and faulting in
+        a fresh output per call.
     """
     assert normalize in ("short", "full"), "Only know short or full normalization methods"
     if normalize == "full":
@@ -202,7 +206,7 @@ def matched_filter(templates, moveouts, weights, data, step,
             return None
         return _matched_filter_variable(templates, moveouts, weights, data, step,
                                         n_samples_template, check_zeros, normalize,
-                                        network_sum, precision)
+                                        network_sum, precision, out)
     if arch.lower() != "gpu":
         print("Compiled library for {} not loaded; exiting!".format(arch))
         return None
@@ -214,8 +218,7 @@ def matched_filter(templates, moveouts, weights, data, step,
         print("Template and data dimensions are not compatible!")
         return None
     T, S, C, n_corr = pp["T"], pp["S"], pp["C"], pp["n_corr"]
-    n_out = T * n_corr * (1 if network_sum else S * C)
-    cc = np.zeros(n_out, dtype=np.float32)
+    cc = _output_array(out, (T, n_corr) if network_sum else (T, n_corr, S, C))
     args = (_ptr(pp["templates"], ct.c_float), _ptr(pp["sst"], ct.c_float),
             _ptr(pp["moveouts"], ct.c_int), _ptr(pp["data"], ct.c_float),
             _ptr(pp["weights"], ct.c_float), pp["step"], pp["L"], pp["N"], T, S, C,
@@ -240,11 +243,23 @@ def matched_filter(templates, moveouts, weights, data, step,
     cc = cc.reshape(T, n_corr) if network_sum else cc.reshape(T, n_corr, S, C)
     _zero_report(cc, pp["moveouts"], pp["weights"], T, n_corr, pp["step"],
                  network_sum, check_zeros, counts)
-    return cc
+    return cc if out is None else out
+
+
+def _output_array(out, shape):
+    """The flat float32 output: a new zeroed array, or a view of ``out``
+    after checking that the library may write it in place."""
+    if out is None:
+        return np.zeros(int(np.prod(shape)), dtype=np.float32)
+    if not (isinstance(out, np.ndarray) and out.dtype == np.float32 and out.flags.c_contiguous
+            and out.flags.writeable and out.shape == tuple(shape)):
+        raise ValueError("out must be a writable C-contiguous float32 array of shape %s"
+                         % (tuple(shape),))
+    return out.reshape(-1)
 
 
 def _matched_filter_variable(templates, moveouts, weights, data, step, n_samples_template,
-                             check_zeros, normalize, network_sum, precision="fp32"):
+                             check_zeros, normalize, network_sum, precision="fp32", out=None):
     """Per-channel template lengths (the reference's arch 'variable_precise',
     fast_matched_filter.py:216-229, 307-313) on the GPU library; ``precision``
     selects the plain FP32 or the tensor-core numerators."""
@@ -267,7 +282,7 @@ def _matched_filter_variable(templates, moveouts, weights, data, step, n_samples
     pp = prepare(templates, moveouts, weights, data, step, normalize)
     n_corr = int((pp["N"] - max_len) / pp["step"] + 1)
     nt = np.ascontiguousarray(n_samples_template.flatten(), dtype=np.int32)
-    cc = np.zeros(T * n_corr, dtype=np.float32)
+    cc = _output_array(out, (T, n_corr))
     st = lib.fmf_matched_filter_variable_ex(
         pp["templates"].ctypes.data, pp["sst"].ctypes.data, pp["moveouts"].ctypes.data,
         pp["data"].ctypes.data, pp["weights"].ctypes.data, pp["step"], nt.ctypes.data,
@@ -276,7 +291,7 @@ def _matched_filter_variable(templates, moveouts, weights, data, step, n_samples
     _lib.check(st, lib)
     cc = cc.reshape(T, n_corr)
     _zero_report(cc, pp["moveouts"], pp["weights"], T, n_corr, pp["step"], True, check_zeros)
-    return cc
+    return cc if out is None else out
 
 
 def matched_filter_device(templates, sum_square_templates, moveouts, weights, data,

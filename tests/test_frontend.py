@@ -107,3 +107,23 @@ def test_variable_lengths_without_network_sum_not_implemented():
                            np.ones((1, 1, 1)), np.zeros((1, 1, 100), np.float32), 1,
                            n_samples_template=np.full((1, 1, 1), 8), arch="variable_precise",
                            network_sum=False)
+
+
+@pytest.mark.parametrize("bad", ["dtype", "shape", "order", "readonly"])
+@pytest.mark.parametrize("variable", [False, True])
+def test_out_must_match_the_output(bad, variable):
+    T, S, C, L, N = 2, 2, 3, 8, 100
+    tp = np.zeros((T, S, C, L), np.float32)
+    mo = np.zeros((T, S, C), np.int32)
+    w = np.ones((T, S, C), np.float32)
+    d = np.zeros((S, C, N), np.float32)
+    n_corr = N - L + 1
+    out = {"dtype": np.zeros((T, n_corr), np.float64),
+           "shape": np.zeros((T, n_corr + 1), np.float32),
+           "order": np.zeros((n_corr, T), np.float32).T,
+           "readonly": np.zeros((T, n_corr), np.float32)}[bad]
+    if bad == "readonly":
+        out.flags.writeable = False
+    kw = {"n_samples_template": np.full((T, S, C), L)} if variable else {}
+    with pytest.raises(ValueError, match="out must be"):
+        fmf.matched_filter(tp, mo, w, d, 1, out=out, **kw)

@@ -67,3 +67,28 @@ def test_template_longer_than_data_rejected():
     with pytest.raises(ValueError):
         fmf.matched_filter(np.ones((1, 1, 1, 100), np.float32), np.zeros((1, 1, 1), np.int32),
                            np.ones((1, 1, 1), np.float32), np.ones((1, 1, 50), np.float32), 1)
+
+
+@pytest.mark.parametrize("precision", PRECISIONS)
+@pytest.mark.parametrize("mode", ["sum", "no_sum", "variable"])
+def test_out_is_written_in_full_and_returned(precision, mode):
+    # a caller-owned output full of NaN: every element is overwritten (the
+    # zeros outside the valid lags included) and the same array comes back
+    rng = np.random.default_rng(7)
+    T, S, C, L, N = 3, 4, 3, 50, 2000
+    tp = rng.standard_normal((T, S, C, L)).astype(np.float32)
+    d = rng.standard_normal((S, C, N)).astype(np.float32)
+    mo = rng.integers(0, 40, (T, S, C)).astype(np.int32)
+    w = rng.random((T, S, C)).astype(np.float32)
+    kw = {"precision": precision, "check_zeros": False}
+    if mode == "no_sum":
+        kw["network_sum"] = False
+    if mode == "variable":
+        n = rng.integers(20, L + 1, (T, S, C))
+        n[0, 0, 0] = L  # the template array's length is the longest
+        kw["n_samples_template"] = n
+    fresh = fmf.matched_filter(tp, mo, w, d, 1, **kw)
+    out = np.full(fresh.shape, np.nan, np.float32)
+    got = fmf.matched_filter(tp, mo, w, d, 1, out=out, **kw)
+    assert got is out
+    np.testing.assert_array_equal(out, fresh)
