@@ -11,9 +11,10 @@
 // device's stream-ordered pool; this one does not allocate at all.
 //
 // What it does: the plain FP32 form (the same kernels as fmf_matched_filter),
-// with every working array (per-template lag ranges, window statistics, and
-// for 'full' the centred data and templates) carved out of ONE file-scope
-// device array of FMF_NOALLOC_SCRATCH_BYTES bytes.  That array belongs to the
+// with every working array (per-template lag ranges, window statistics, the
+// template energies when the caller passes none, and for 'full' the centred
+// data and templates) carved out of ONE file-scope device array of
+// FMF_NOALLOC_SCRATCH_BYTES bytes.  That array belongs to the
 // module, so every GPU that loads this library holds it until the process
 // exits.  Inputs and outputs are the caller's device pointers.
 //
@@ -26,8 +27,9 @@
 //    and corrupt each other's results: serialise them.  Nothing read from the
 //    array is assumed to start at zero -- each call writes every element it
 //    later reads -- so the previous call's leftovers do no harm.
-//  * Searches that need more scratch than the array holds are rejected with
-//    FMF_ERR_ARG and a message giving both sizes, before any work is queued.
+//  * Searches that need more scratch than the array holds, and device arrays
+//    that are not 4-byte aligned, are rejected with FMF_ERR_ARG before any
+//    work is queued.
 #include <cstdio>
 #include <mutex>
 
@@ -36,10 +38,10 @@
 namespace fmf {
 
 __global__ void template_range_kernel(const int *, int, int, int, int, int, int, int *, int *);
+__global__ void template_energy_kernel(const float *, int, int, float *);
 __global__ void template_center_kernel(const float *, int, float *, float *);
 __global__ void channel_mean_kernel(const float *, int, float *);
 __global__ void window_stats_kernel(const float *, int, int, int, const float *, float *, float *);
-int launch_plain(const Problem &P, cudaStream_t stream);
 
 // The only working memory of fmf_matched_filter_noalloc.  In host code this
 // name is a host-side stand-in, not a device address: host code uses the
@@ -88,13 +90,23 @@ struct Carve {
     }
 };
 
-size_t scratch_bytes(size_t T, size_t SC, size_t L, size_t N, bool full)
+// Bytes of the carve of fmf_matched_filter_noalloc, or SIZE_MAX when the
+// search cannot fit (so that no product below can wrap): lag ranges, window
+// statistics ('full': (energy, mean) pairs), the template energies when the
+// caller passes none, then for 'full' the centred data, channel means,
+// centred templates and their sums.
+size_t scratch_bytes(size_t T, size_t SC, size_t L, size_t N, bool full, bool energies)
 {
+    const size_t cap = FMF_NOALLOC_SCRATCH_BYTES;
+    // every factor pair below is bounded before it is multiplied: each part
+    // must fit the array on its own
+    if (T > cap / 8 || SC > cap / 4 || N > cap / 4 || L > cap / 4 || SC > cap / 4 / N ||
+        T > cap / 4 / SC || T * SC > cap / 4 / (L + 1))
+        return SIZE_MAX;
     auto al = [](size_t b) { return (b + 255) & ~size_t(255); };
-    // the carve of fmf_matched_filter_noalloc: ranges, window statistics (full:
-    // (energy, mean) pairs), then for full the centred data, channel means,
-    // centred templates and their sums
     size_t b = al(2 * T * sizeof(int)) + al(SC * N * sizeof(float) * (full ? 2 : 1));
+    if (energies)
+        b += al(T * SC * sizeof(float));
     if (full)
         b += al(SC * N * sizeof(float)) + al(SC * sizeof(float)) + al(T * SC * L * sizeof(float)) +
              al(T * SC * sizeof(float));
@@ -115,25 +127,41 @@ extern "C" int fmf_matched_filter_noalloc(const float *templates, const float *s
     using namespace fmf;
     set_error(FMF_OK, "");
     reset_launch_count();
-    if (!templates || !sum_square_templates || !moveouts || !data || !weights || !cc_out)
+    if (!templates || !moveouts || !data || !weights || !cc_out)
         return set_error(FMF_ERR_ARG, "noalloc: null array argument");
+    {  // the kernels load these in place as 4-byte elements
+        const void *ptrs[6] = {templates, sum_square_templates, moveouts, data, weights, cc_out};
+        for (const void *p : ptrs)
+            if ((uintptr_t)p & 3)
+                return set_error(FMF_ERR_ARG, "noalloc: device array %p is not 4-byte aligned", p);
+    }
     if (step < 1 || n_samples_template < 1 || n_templates < 1 || n_stations < 1 ||
         n_components < 1 || n_corr < 1 || n_samples_data < n_samples_template)
         return set_error(FMF_ERR_ARG, "noalloc: invalid sizes");
     if (normalize != 0 && normalize != 1)
         return set_error(FMF_ERR_ARG, "noalloc: normalize must be 0 or 1");
+    if (n_stations > (size_t)INT_MAX || n_components > (size_t)INT_MAX)
+        return set_error(FMF_ERR_ARG, "noalloc: sizes out of range");
     const size_t SCz = n_stations * n_components;
     if (n_samples_data > (size_t)INT_MAX / 2 || n_corr > (size_t)INT_MAX || SCz > (size_t)INT_MAX ||
         n_templates > (size_t)INT_MAX || step > (size_t)INT_MAX / 2 ||
         n_corr > (n_samples_data - n_samples_template) / step + 1)
         return set_error(FMF_ERR_ARG, "noalloc: sizes out of range");
     const bool full = normalize == 1;
-    const size_t need = scratch_bytes(n_templates, SCz, n_samples_template, n_samples_data, full);
-    if (need > (size_t)FMF_NOALLOC_SCRATCH_BYTES)
+    const bool energies = sum_square_templates == nullptr;
+    const size_t need =
+        scratch_bytes(n_templates, SCz, n_samples_template, n_samples_data, full, energies);
+    if (need > (size_t)FMF_NOALLOC_SCRATCH_BYTES) {
+        if (need == SIZE_MAX)
+            return set_error(FMF_ERR_ARG,
+                             "noalloc: this search needs more scratch than the %zu bytes the "
+                             "allocation-free entry point has (use fmf_matched_filter_ex)",
+                             (size_t)FMF_NOALLOC_SCRATCH_BYTES);
         return set_error(FMF_ERR_ARG,
                          "noalloc: this search needs %zu bytes of scratch; the allocation-free entry "
                          "point has %zu (use fmf_matched_filter_ex)",
                          need, (size_t)FMF_NOALLOC_SCRATCH_BYTES);
+    }
     const int T = (int)n_templates, SC = (int)SCz, L = (int)n_samples_template,
               N = (int)n_samples_data;
     const size_t stat_smem = (size_t)(kNoallocStatBlock + L + 1) * sizeof(double) * (full ? 2 : 1);
@@ -149,6 +177,7 @@ extern "C" int fmf_matched_filter_noalloc(const float *templates, const float *s
     int *k_lo = cv.take<int>(2 * (size_t)T);
     int *k_hi = k_lo + T;
     float *stat_e = cv.take<float>((size_t)SC * N * (full ? 2 : 1));
+    float *sst = energies ? cv.take<float>((size_t)T * SC) : nullptr;
     float *dcen = nullptr, *mu = nullptr, *tcen = nullptr, *tsum = nullptr;
     if (full) {
         dcen = cv.take<float>((size_t)SC * N);
@@ -160,9 +189,15 @@ extern "C" int fmf_matched_filter_noalloc(const float *templates, const float *s
     cudaGetLastError();
     template_range_kernel<<<(T + 127) / 128, 128, 0, s>>>(moveouts, T, SC, L, N, (int)step, (int)n_corr,
                                                             k_lo, k_hi);
+    count_launch();
+    if (energies) {  // as numpy sums float32 templates**2: bit-identical energies
+        template_energy_kernel<<<(T * SC + 127) / 128, 128, 0, s>>>(templates, T * SC, L, sst);
+        count_launch();
+    }
     if (full) {
         template_center_kernel<<<(unsigned)((size_t)T * SC), 128, 0, s>>>(templates, L, tcen, tsum);
         channel_mean_kernel<<<SC, 1024, 0, s>>>(data, N, mu);
+        count_launch(2);
     }
     cudaError_t e = cudaFuncSetAttribute(window_stats_kernel,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)stat_smem);
@@ -170,6 +205,7 @@ extern "C" int fmf_matched_filter_noalloc(const float *templates, const float *s
         return set_error(FMF_ERR_CUDA, "noalloc: statistics shared memory: %s", cudaGetErrorString(e));
     dim3 sgrid((N + kNoallocStatBlock - 1) / kNoallocStatBlock, SC);
     window_stats_kernel<<<sgrid, 256, stat_smem, s>>>(data, N, L, kNoallocStatBlock, mu, dcen, stat_e);
+    count_launch();
     if ((e = cudaGetLastError()) != cudaSuccess)
         return set_error(FMF_ERR_CUDA, "noalloc: preprocessing launch: %s", cudaGetErrorString(e));
     if (!sum_cc_mode) {
@@ -180,7 +216,7 @@ extern "C" int fmf_matched_filter_noalloc(const float *templates, const float *s
 
     Problem P;
     P.tpl = full ? tcen : templates;
-    P.sst = sum_square_templates;
+    P.sst = energies ? sst : sum_square_templates;
     P.tsum = tsum;
     P.mo = moveouts;
     P.w = weights;
@@ -202,22 +238,7 @@ extern "C" int fmf_matched_filter_noalloc(const float *templates, const float *s
     P.pre1f = nullptr;
     P.zweight = nullptr;
     P.vp_norm = P.vp_bias = P.vp_scale = nullptr;
-    for (int t0 = 0; t0 < T; t0 += 65535) {
-        Problem Q = P;
-        const int nt = T - t0 < 65535 ? T - t0 : 65535;
-        const size_t o = (size_t)t0 * SC;
-        Q.tpl += o * L;
-        Q.sst += o;
-        if (Q.tsum)
-            Q.tsum += o;
-        Q.mo += o;
-        Q.w += o;
-        Q.k_lo += t0;
-        Q.k_hi += t0;
-        Q.out += (size_t)t0 * n_corr * (P.network_sum ? 1 : SC);
-        Q.T = nt;
-        if ((rc = launch_plain(Q, s)))
-            return rc;
-    }
+    if ((rc = launch_plain_all(P, s)))
+        return rc;
     return FMF_OK;
 }

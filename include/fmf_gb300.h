@@ -138,13 +138,16 @@ FMF_API int fmf_matched_filter_check_zeros(const float *templates, const float *
  * allocations by this library would fail or fragment.
  *
  * Same arguments as fmf_matched_filter plus a stream; every array argument is
- * a device pointer; plain FP32 form; asynchronous on `stream`.  It allocates
- * nothing: its working arrays live in one file-scope device array of
- * FMF_NOALLOC_SCRATCH_BYTES that every GPU loading this library holds until
- * the process exits.  The scratch needed is 4*S*C*N + 8*T bytes for
- * normalize=0 and 12*S*C*N + 4*T*S*C*(L+1) + 4*S*C + 8*T bytes for
- * normalize=1 (each part rounded up to 256 bytes); larger searches are
- * rejected with FMF_ERR_ARG.  The first call on a device looks up the array's
+ * a 4-byte-aligned device pointer (a misaligned one is rejected with
+ * FMF_ERR_ARG); plain FP32 form; asynchronous on `stream`.  As in
+ * fmf_matched_filter, sum_square_templates may be NULL and is then computed on
+ * the device.  It allocates nothing: its working arrays live in one
+ * file-scope device array of FMF_NOALLOC_SCRATCH_BYTES that every GPU loading
+ * this library holds until the process exits.  The scratch needed is
+ * 4*S*C*N + 8*T bytes for normalize=0 and 12*S*C*N + 4*T*S*C*(L+1) + 4*S*C +
+ * 8*T bytes for normalize=1, plus 4*T*S*C when sum_square_templates is NULL
+ * (each part rounded up to 256 bytes); larger searches are rejected with
+ * FMF_ERR_ARG.  The first call on a device looks up the array's
  * device address with that device current: make it before any stream
  * capture.  All calls share the array, so calls that overlap on the GPU race
  * and must be serialised by the caller.

@@ -120,3 +120,39 @@ def test_python_layer_raises_on_status(lib):
     with pytest.raises(_lib.FMFError) as e:
         _lib.check(_lib.FMF_ERR_ARG, lib)
     assert "BAD_ARG" in str(e.value)
+
+
+def _noalloc(lib):
+    f = lib.fmf_matched_filter_noalloc
+    f.argtypes = [ct.c_void_p] * 5 + [ct.c_size_t] * 7 + [ct.c_void_p, ct.c_int, ct.c_int,
+                                                          ct.c_void_p]
+    f.restype = ct.c_int
+    return f
+
+
+def test_noalloc_rejects_misaligned_array_before_device_work(lib):
+    """The allocation-free entry point checks element alignment of every array
+    before it touches the device, like the device-pointer path of
+    fmf_matched_filter_ex."""
+    args, keep = _args()
+    ex = [a if not hasattr(a, "contents") else ct.cast(a, ct.c_void_p).value for a in args]
+    for k in (0, 1, 2, 3, 4, 12):
+        bad = list(ex)
+        bad[k] += 2
+        st = _noalloc(lib)(*bad[:13], 0, 1, None)
+        assert st == _lib.FMF_ERR_ARG, k
+        assert "aligned" in _lib.last_error(lib)[1]
+
+
+@pytest.mark.parametrize("T,S,C,L,N", [
+    (1, 20, 3, 50, 200000),                 # 48 MB of window energies
+    (2 ** 31 - 1, 1, 1, 8, 2 ** 30 - 1),    # products that would wrap unguarded
+    (1 << 20, 1 << 11, 1, 1 << 10, 1 << 29),
+])
+def test_noalloc_rejects_searches_beyond_its_scratch(lib, T, S, C, L, N):
+    args, keep = _args()
+    ex = [a if not hasattr(a, "contents") else ct.cast(a, ct.c_void_p).value for a in args]
+    ex[5:12] = [1, L, N, T, S, C, N - L + 1]
+    st = _noalloc(lib)(*ex[:13], 1, 1, None)
+    assert st == _lib.FMF_ERR_ARG
+    assert "scratch" in _lib.last_error(lib)[1]
