@@ -38,6 +38,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 
 import numpy as np
@@ -137,13 +138,13 @@ class ClockSampler:
         self.dev = device_index
         self.proc = None
         self.off = device_index < 0
-        self.path = os.path.join(HERE, "gpurun_out", "clocks_bench_%d.csv" % device_index)
+        self.path = os.path.join(tempfile.gettempdir(),
+                                 "fmf_bench_clocks_%d_%d.csv" % (os.getpid(), device_index))
 
     def __enter__(self):
         if self.off:
             return self
         try:
-            os.makedirs(os.path.dirname(self.path), exist_ok=True)
             self.f = open(self.path, "w")
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.dev), "--query-gpu=" + self.Q,
@@ -175,6 +176,8 @@ class ClockSampler:
                     rows.append((float(parts[1]), float(parts[2]), float(parts[3]), parts[5:9]))
                 except ValueError:
                     continue
+        with contextlib.suppress(OSError):
+            os.remove(self.path)
         if not rows:
             return None
         loaded = [r for r in rows if r[2] > 200.0] or rows
@@ -498,17 +501,21 @@ def roofline(cfg, precision, kern_ms, prep_ms):
                 "peak_source": "nominal FP32 FMA rate: 152 SMs x 128 lanes x %.0f MHz (%s max "
                                "SM clock); no measured FP32 peak exists" % (mhz, src)}
     else:
-        peak = float(peaks.get("bf16_tflops_sustained", peaks["bf16_tflops"]))
+        bf16 = float(peaks.get("bf16_tflops_sustained", peaks["bf16_tflops"]))
         products = 3 if precision == "split_bf16" else 1
+        # the bound in algorithmic FLOP/s: each multiply-accumulate costs `products`
+        # bf16 tensor-core products
+        peak = bf16 / products
         ex, nb = tc_executed_macs(cfg)
         executed = 2.0 * ex * products / (kern_ms / 1e3) / 1e12
         traffic, tsrc = profiled_traffic("tc_persistent", cfg)
         roof = {"bound": "tensor", "achieved": algo_tflops, "peak": peak, "unit": "TFLOP/s",
                 "frac": algo_tflops / peak, "traffic": traffic, "traffic_source": tsrc,
                 "kernel": "tc_persistent (nb=%d)" % nb,
-                "peak_source": "%s bf16_tflops_sustained (cuBLAS bf16 GEMM, seconds-long loop)"
-                               % src,
-                "executed_tflops": executed, "executed_frac": executed / peak,
+                "peak_source": "%s bf16_tflops_sustained (cuBLAS bf16 GEMM, seconds-long loop) "
+                               "/ %d bf16 products per multiply-accumulate" % (src, products),
+                "bf16_peak": bf16,
+                "executed_tflops": executed, "executed_frac": executed / bf16,
                 "executed_over_algorithmic": ex * products / cfg["macs"]}
     roof["kernel_ms_avg"] = kern_ms
     roof["prep_ms_avg"] = prep_ms
@@ -776,16 +783,18 @@ def run_variable(args):
                                "no measured FP32 peak exists"}
 
     def tc_roofline(ms):
-        peak = peaks.get("bf16_tflops_sustained", FALLBACK_PEAKS["bf16_tflops_sustained"])
+        bf16 = peaks.get("bf16_tflops_sustained", FALLBACK_PEAKS["bf16_tflops_sustained"])
         achieved = 2 * cfg["macs"] / (ms / 1e3) / 1e12
         executed, nb = tc_executed_macs(cfg)
         n_prod = 3 if precision == "split_bf16" else 1
+        peak = bf16 / n_prod  # algorithmic FLOP/s bound: n_prod bf16 products per MAC
         ex = 2 * executed * n_prod / (ms / 1e3) / 1e12
         return {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                 "frac": achieved / peak, "traffic": None,
                 "kernel": "tc_persistent (nb=%d, per-channel K ranges)" % nb,
-                "peak_source": "%s bf16_tflops_sustained (cuBLAS bf16 GEMM, seconds-long loop)" % kind,
-                "executed_tflops": ex, "executed_frac": ex / peak,
+                "peak_source": "%s bf16_tflops_sustained (cuBLAS bf16 GEMM, seconds-long loop) "
+                               "/ %d bf16 products per multiply-accumulate" % (kind, n_prod),
+                "bf16_peak": bf16, "executed_tflops": ex, "executed_frac": ex / bf16,
                 "executed_over_algorithmic": executed * n_prod / cfg["macs"]}
 
     ms, launches, clocks = timed(precision, args.steps, args.warmup, True)

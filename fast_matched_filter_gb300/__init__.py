@@ -9,12 +9,12 @@ The exported names mirror the reference package's
 from .fast_matched_filter import (  # noqa: F401
     Batch,
     CPU_LOADED,
-    GPU_LOADED,
     matched_filter,
     matched_filter_device,
     test_matched_filter,
 )
 from ._lib import FMFError  # noqa: F401
+from .sharding import matched_filter_sharded, template_block  # noqa: F401
 from .detection import (  # noqa: F401
     Detections,
     detect,
@@ -23,3 +23,11 @@ from .detection import (  # noqa: F401
 )
 
 __version__ = "0.1.0"
+
+
+def __getattr__(name):
+    # GPU_LOADED loads the library on first read (importing maps no native code)
+    if name == "GPU_LOADED":
+        from . import fast_matched_filter
+        return fast_matched_filter.GPU_LOADED
+    raise AttributeError("module %r has no attribute %r" % (__name__, name))

@@ -23,17 +23,29 @@ import numpy as np
 from . import _lib, autotune
 
 CPU_LOADED = False
-_LIB, _LIB_ERROR = _lib.try_load()
-GPU_LOADED = _LIB is not None
+# The library is loaded by the first call that needs it (or the first read of
+# GPU_LOADED), not at import: importing the package for its generators or
+# its shape handling maps no native code.
+_LIB, _LIB_ERROR = None, "not loaded yet"
+
+
+def __getattr__(name):
+    """GPU_LOADED: whether libfmf_gb300.so loads (the reference's flag,
+    fast_matched_filter.py:52-63), evaluated on first use."""
+    if name == "GPU_LOADED":
+        global _LIB, _LIB_ERROR
+        if _LIB is None:
+            _LIB, _LIB_ERROR = _lib.try_load()
+        return _LIB is not None
+    raise AttributeError("module %r has no attribute %r" % (__name__, name))
 
 
 def _require_lib():
-    """The loaded library; retried here when it was built after import.
-    Raises RuntimeError when it cannot be loaded (no CPU fallback)."""
-    global _LIB, _LIB_ERROR, GPU_LOADED
+    """The loaded library, loaded on first use.  Raises RuntimeError when it
+    cannot be loaded (no CPU fallback)."""
+    global _LIB, _LIB_ERROR
     if _LIB is None:
         _LIB, _LIB_ERROR = _lib.try_load()
-        GPU_LOADED = _LIB is not None
     if _LIB is None:
         raise RuntimeError(
             "fast_matched_filter_gb300: libfmf_gb300.so is not loadable (%s); "
@@ -340,7 +352,11 @@ def test_matched_filter(n_templates=1, n_stations=1, n_components=1,
     uniform-noise data (mean removed per channel), templates cut from the data
     at random times with random moveouts of 0-10 s, unit weights, so that the
     maximum coefficient of every template is 1.  Returns (templates,
-    moveouts, data, step, cc_sums, run_time)."""
+    moveouts, data, step, cc_sums, run_time); with arch='variable_precise'
+    every station of every template keeps a random length of 1/2 to 1 times
+    the template duration (fast_matched_filter.py:512-531), and the returned
+    tuple carries those lengths before run_time (as the reference's,
+    fast_matched_filter.py:566-567)."""
     from time import time as clock
 
     starts = np.random.random_sample(n_templates) * (data_duration / 2)
@@ -371,14 +387,26 @@ def test_matched_filter(n_templates=1, n_stations=1, n_components=1,
                 a = int(first + moveouts[t, s, c])
                 templates[t, s, c, :] = data[s, c, a:a + n_tp]
     weights = np.ones((n_templates, n_stations, n_components), dtype=np.float32)
+    lengths = None
+    if arch == "variable_precise":
+        lengths = np.zeros(moveouts.shape, dtype=np.int32)
+        for t in range(n_templates):
+            for s in range(n_stations):
+                lengths[t, s, :] = np.int32(np.round(np.random.random_sample() * n_tp / 2
+                                                     + n_tp / 2))
+        templates = templates[:, :, :, :np.max(lengths)]
+        for idx in np.ndindex(lengths.shape):
+            templates[idx][lengths[idx]:] = 0.0
     t0 = clock()
     cc_sum = matched_filter(templates, moveouts, weights, data, step, arch=arch,
-                            check_zeros=check_zeros, normalize=normalize,
-                            network_sum=network_sum, precision=precision)
+                            n_samples_template=lengths, check_zeros=check_zeros,
+                            normalize=normalize, network_sum=network_sum, precision=precision)
     run_time = clock() - t0
     print("Matched filter ({}) for {} templates on {} stations/{} components over "
           "{} samples ({} step) ran in {:.3f}s".format(
               arch, n_templates, n_stations, n_components, n_data, step, run_time))
+    if lengths is not None:
+        return templates, moveouts, data, step, cc_sum, lengths, run_time
     return templates, moveouts, data, step, cc_sum, run_time
 
 

@@ -30,11 +30,22 @@ _REF_ARGS = [_fp, _fp, _ip, _fp, _fp, _sz, _sz, _sz, _sz, _sz, _sz, _sz, _fp]
 _oracle = None
 _ref = None
 
+# Where the reference checkout is read from (its CPU library source, its test
+# data): $FMF_REFERENCE_ROOT, else the checkout this build recipe was written
+# against.  Where neither exists, only the restatement is built and the tests
+# that need the reference skip.
+DEFAULT_REFERENCE_ROOT = "/root/reference"
+
+
+def reference_root():
+    return os.environ.get("FMF_REFERENCE_ROOT") or DEFAULT_REFERENCE_ROOT
+
 
 def build(ref_src=None):
     """Compile the restatement (always) and the reference (when its source exists)."""
     subprocess.check_call(["make", "-s", "-C", HERE], stdout=subprocess.DEVNULL)
-    src = ref_src or "/root/reference/fast_matched_filter/src/matched_filter.c"
+    src = ref_src or os.path.join(reference_root(), "fast_matched_filter", "src",
+                                  "matched_filter.c")
     if os.path.exists(src):
         subprocess.check_call(["make", "-s", "-C", HERE, "ref", "REF_SRC=" + src],
                               stdout=subprocess.DEVNULL)

@@ -17,6 +17,10 @@ def pytest_configure(config):
     subprocess.run([sys.executable, "-c",
                     "from fast_matched_filter_gb300 import build; build.build()"],
                    cwd=REPO, check=False)
+    # The checker libraries too, before collection: tests that pin the oracle
+    # against the reference library are skipped when that library is absent.
+    subprocess.run([sys.executable, "-c", "from oracle import cpu; cpu.build()"],
+                   cwd=REPO, check=False)
 
 
 @pytest.fixture(scope="session")

@@ -145,7 +145,8 @@ def reference_data_cases(ref_root):
              dict(arch="cpu", normalize="short", network_sum=True))]
 
 
-def main(ref_root="/root/reference"):
+def main(ref_root=None):
+    ref_root = ref_root or cpu.reference_root()
     cpu.build(os.path.join(ref_root, "fast_matched_filter", "src", "matched_filter.c"))
     ref = load_reference_wrapper(ref_root)
     for name, inputs, opts in cases() + reference_data_cases(ref_root):

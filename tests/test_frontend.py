@@ -15,6 +15,22 @@ def test_reference_names_exported():
     assert fmf.CPU_LOADED is False
 
 
+def test_import_maps_no_native_code():
+    """Importing the package and its generators loads no library; the first
+    read of GPU_LOADED (or the first call) does."""
+    import subprocess
+    import sys
+    code = ("import fast_matched_filter_gb300 as f, fast_matched_filter_gb300.synthetic\n"
+            "maps = lambda: open('/proc/self/maps').read()\n"
+            "assert 'libfmf_gb300' not in maps()\n"
+            "loaded = f.GPU_LOADED\n"
+            "assert loaded == ('libfmf_gb300' in maps())\n")
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True,
+                       cwd=__import__("os").path.dirname(__import__("os").path.dirname(
+                           __import__("os").path.abspath(__file__))))
+    assert r.returncode == 0, r.stderr
+
+
 @pytest.mark.parametrize("arch", ["cpu", "precise"])
 def test_cpu_architectures_reported_not_loaded(arch, capsys):
     tp = np.zeros((1, 1, 1, 8), np.float32)

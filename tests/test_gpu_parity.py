@@ -178,6 +178,25 @@ def test_synthetic_self_test_finds_templates():
     assert np.all(np.abs(cc.max(axis=1) - 6.0) < 1e-4)
 
 
+def test_synthetic_self_test_variable_lengths():
+    """The self-test's 'variable_precise' branch (fast_matched_filter.py:512-531):
+    per-station lengths of 1/2 to 1 template duration, returned before the run
+    time.  Each template correlates to 1 on every channel at its origin, so
+    its Fisher-z network sum peaks at the reference's scale, the weights of
+    templates 0..t (6 per template here, matched_filter.c:329,365)."""
+    np.random.seed(8)
+    out = fmf.test_matched_filter(n_templates=3, n_stations=2, n_components=3,
+                                  template_duration=4, data_duration=600, sampling_rate=50,
+                                  arch="variable_precise")
+    assert len(out) == 7
+    templates, lengths, cc = out[0], out[5], out[4]
+    assert lengths.shape == (3, 2, 3) and lengths.max() == templates.shape[-1]
+    assert np.all((lengths >= 100) & (lengths <= 200))
+    assert np.all(lengths == lengths[:, :, :1])  # one length per station
+    scale = 6.0 * np.arange(1, 4)
+    assert np.all(np.abs(cc.max(axis=1) - scale) < 1e-4 * scale)
+
+
 @pytest.mark.parametrize("precision", ["fp32", "split_bf16"])
 def test_reference_noisy_dataset_peak(precision):
     """The reference test suite's 'noisy' dataset (cropped to 80,000-90,000 in the

@@ -12,10 +12,11 @@ import os
 import numpy as np
 import pytest
 
+from oracle import cpu
 from tests._cases import (canonical, golden_names, golden_names_fixed, golden_names_variable,
                           load_golden, random_search)
 
-REF_DATA = "/root/reference/fast_matched_filter/tests/data"
+REF_DATA = os.path.join(cpu.reference_root(), "fast_matched_filter", "tests", "data")
 
 
 @pytest.mark.parametrize("name", golden_names_fixed())
