@@ -601,17 +601,36 @@ def run_e2e(cfg, dev_out, precision, args, world, lib):
             int(cfg["network_sum"]), prec, 0, None)
         _lib.check(st, lib)
 
-    call()  # warm-up (pool growth)
+    import ctypes as ct
+    for _ in range(2):  # warm-up (pool growth)
+        call()
     barrier(world)
-    n = max(1, min(args.steps, 3))
+    n = max(5, args.steps)
+    per_step = []
+    lib.fmf_timing_begin()
     t0 = time.perf_counter()
     for _ in range(n):
+        t = time.perf_counter()
         call()
+        per_step.append(time.perf_counter() - t)
     secs = dist_max(time.perf_counter() - t0, world)
+    ms = (ct.c_double * 5)()
+    calls = ct.c_int()
+    lib.fmf_timing_end_ex(ms, 5, ct.byref(calls))
     h2d = sum(int(v.numel() * v.element_size()) for v in pinned.values())
     d2h = int(host_out.numel() * 4)
+    wall_ms = 1e3 * secs / n
+    parts = {k: ms[i] / n for i, k in enumerate(("preprocessing_ms", "kernel_ms", "input_copies_ms",
+                                                 "output_copies_ms", "output_tail_ms"))}
+    parts["host_and_other_ms"] = wall_ms - (parts["input_copies_ms"] + parts["preprocessing_ms"]
+                                            + parts["kernel_ms"] + parts["output_tail_ms"])
     return {"value": cfg["macs"] * n * world / secs / 1e12, "unit": UNIT,
             "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "steps": n,
+            "ms_per_step": wall_ms, "step_ms": [round(1e3 * x, 2) for x in per_step],
+            "breakdown_per_step": parts,
+            "h2d_gbs": h2d / (parts["input_copies_ms"] / 1e3) / 1e9 if parts["input_copies_ms"] else None,
+            "d2h_window_gbs": d2h / (parts["output_copies_ms"] / 1e3) / 1e9
+            if parts["output_copies_ms"] else None,
             "api": "fmf_matched_filter_ex (C ABI, host pointers, pinned)"}
 
 

@@ -9,6 +9,7 @@ The exported names mirror the reference package's
 from .fast_matched_filter import (  # noqa: F401
     Batch,
     CPU_LOADED,
+    last_precision,
     matched_filter,
     matched_filter_device,
     test_matched_filter,

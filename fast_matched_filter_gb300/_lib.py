@@ -25,7 +25,10 @@ STATUS_NAMES = {0: "OK", 1: "BAD_ARG", 2: "OOM", 3: "SMEM", 4: "CUDA_ERR",
 PREC_FP32 = 0
 PREC_SPLIT_BF16 = 1
 PREC_BF16 = 2
-PRECISIONS = {"fp32": PREC_FP32, "split_bf16": PREC_SPLIT_BF16, "bf16": PREC_BF16}
+PREC_AUTO = 3  # split bf16 where its error model allows 1e-5, else fp32
+PRECISIONS = {"fp32": PREC_FP32, "split_bf16": PREC_SPLIT_BF16, "bf16": PREC_BF16,
+              "auto": PREC_AUTO}
+PRECISION_NAMES = {v: k for k, v in PRECISIONS.items()}
 
 FLAG_DEVICE_POINTERS = 1
 
@@ -55,12 +58,13 @@ ARGTYPES_EX = [ct.c_void_p] * 5 + [_sz] * 7 + [ct.c_void_p, ct.c_int, ct.c_int,
 # every symbol declared in include/fmf_gb300.h
 EXPORTS = ("fmf_matched_filter", "matched_filter", "fmf_matched_filter_ex",
            "fmf_last_error", "fmf_version", "fmf_last_launch_count",
-           "fmf_release_cache", "fmf_timing_begin", "fmf_timing_end",
+           "fmf_release_cache", "fmf_timing_begin", "fmf_timing_end", "fmf_timing_end_ex",
            "fmf_device_errors", "fmf_matched_filter_noalloc", "fmf_batch_create",
            "fmf_batch_add", "fmf_batch_set_tiles", "fmf_batch_run", "fmf_batch_launch_count",
            "fmf_batch_destroy", "fmf_selftest_wait_timeout", "fmf_matched_filter_variable",
            "fmf_matched_filter_variable_ex", "fmf_detect", "fmf_matched_filter_detect",
-           "fmf_template_energies", "fmf_matched_filter_check_zeros", "fmf_eval_atanh")
+           "fmf_template_energies", "fmf_matched_filter_check_zeros", "fmf_eval_atanh",
+           "fmf_last_precision")
 
 DETECT_CAPACITY = 16384  # FMF_DETECT_CAPACITY
 # detection arguments after the rows: n_mad, min_separation, max_detections, six outputs,
@@ -100,6 +104,7 @@ def load(path=None):
     lib.fmf_last_error.restype = ct.c_int
     lib.fmf_version.restype = ct.c_char_p
     lib.fmf_last_launch_count.restype = ct.c_int
+    lib.fmf_last_precision.restype = ct.c_int
     lib.fmf_release_cache.restype = ct.c_int
     lib.fmf_timing_begin.restype = ct.c_int
     lib.fmf_device_errors.restype = ct.c_int
@@ -123,6 +128,8 @@ def load(path=None):
     lib.fmf_timing_end.argtypes = [ct.POINTER(ct.c_double), ct.POINTER(ct.c_double),
                                    ct.POINTER(ct.c_int)]
     lib.fmf_timing_end.restype = ct.c_int
+    lib.fmf_timing_end_ex.argtypes = [ct.POINTER(ct.c_double), ct.c_int, ct.POINTER(ct.c_int)]
+    lib.fmf_timing_end_ex.restype = ct.c_int
     lib.fmf_detect.argtypes = ARGTYPES_DETECT
     lib.fmf_detect.restype = ct.c_int
     lib.fmf_matched_filter_detect.argtypes = ARGTYPES_SEARCH_DETECT

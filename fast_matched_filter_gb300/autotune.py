@@ -56,6 +56,8 @@ def flags_for(L, step, n_channels, normalize, precision):
     """fmf_matched_filter_ex flag bits of the cached shape (0: library default)."""
     if precision == "fp32":
         return 0
+    if precision == "auto":  # the tile shape of the tensor-core form it may choose
+        precision = "split_bf16"
     shape = lookup(L, step, n_channels, normalize, precision)
     if shape is None:
         return 0

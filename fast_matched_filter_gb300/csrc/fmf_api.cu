@@ -13,7 +13,16 @@
 #include <cstdlib>
 #include <climits>
 #include <mutex>
+#include <thread>
 #include <vector>
+
+#if defined(__linux__)
+#include <sys/mman.h>
+#include <unistd.h>
+#ifndef MADV_POPULATE_WRITE
+#define MADV_POPULATE_WRITE 23  /* Linux 5.14 */
+#endif
+#endif
 
 #include "fmf_common.cuh"
 
@@ -44,14 +53,25 @@ static int clear_error()
 }
 
 void count_launch(int n) { g_launches += n; }
+static thread_local int g_last_precision = -1;
+void set_last_precision(int precision) { g_last_precision = precision; }
 void reset_launch_count() { g_launches = 0; }
 
 // ---------------------------------------------------------------- event timing
 // Opt-in (fmf_timing_begin/end): every call records CUDA events on its stream
-// around the preprocessing kernels and around the correlation kernel.
+// around the preprocessing kernels and around the correlation kernel, and
+// host-pointer calls around their copies.
+enum SpanKind {
+    kSpanPrep = 0,     // preprocessing kernels
+    kSpanKernel = 1,   // correlation kernels (with their operand repacking)
+    kSpanInput = 2,    // host-to-device copies of the inputs
+    kSpanOutput = 3,   // device-to-host copies of the result, first to last
+    kSpanTail = 4,     // the part of those copies after the last correlation kernel
+    kSpanKinds = 5
+};
 struct TimedSpan {
     cudaEvent_t a, b;
-    int kind;  // 0 preprocessing, 1 correlation kernel
+    int kind;
 };
 static thread_local bool g_timing = false;
 static thread_local TimedSpan g_spans[4096];
@@ -80,6 +100,49 @@ static void span(cudaEvent_t a, cudaEvent_t b, int kind)
     }
 }
 
+// Maps the host pages of [p, p + bytes) for writing, on several threads, so
+// that the device-to-host copy of a result into them does not fault every page
+// in on its way: a fresh output array -- the reference's front-end allocates
+// one per call, fast_matched_filter.py:269-274 -- is untouched memory, and a
+// copy into it ran at 29 GB/s against 190 GB/s into mapped pages (8.6 GB for
+// the full-day search).  Mapped pages cost a page-table walk; where the
+// kernel refuses the advice (older kernels, page-locked mappings) nothing
+// is done.
+void populate_host(void *p, size_t bytes)
+{
+#if defined(__linux__)
+    const long page = sysconf(_SC_PAGESIZE);
+    if (!p || bytes == 0 || page <= 0)
+        return;
+    const uintptr_t a = (uintptr_t)p & ~(uintptr_t)(page - 1);
+    const uintptr_t b = ((uintptr_t)p + bytes + page - 1) & ~(uintptr_t)(page - 1);
+    const size_t pages = (b - a) / page;
+    const size_t min_part = ((size_t)32 << 20) / page;  // at least 32 MB per thread
+    unsigned nt = std::thread::hardware_concurrency();
+    nt = nt == 0 ? 1 : (nt > 16 ? 16 : nt);
+    if (pages / min_part < nt)
+        nt = (unsigned)(pages / min_part > 0 ? pages / min_part : 1);
+    auto part = [&](unsigned i) {
+        const size_t p0 = pages * i / nt, p1 = pages * (i + 1) / nt;
+        if (p1 > p0)
+            madvise((void *)(a + p0 * page), (p1 - p0) * page, MADV_POPULATE_WRITE);
+    };
+    if (nt == 1) {
+        part(0);
+        return;
+    }
+    std::vector<std::thread> pool;
+    for (unsigned i = 1; i < nt; i++)
+        pool.emplace_back(part, i);
+    part(0);
+    for (auto &t : pool)
+        t.join();
+#else
+    (void)p;
+    (void)bytes;
+#endif
+}
+
 int check_launch(const char *what)
 {
     cudaError_t e = cudaGetLastError();
@@ -101,9 +164,8 @@ static int cuda_status(cudaError_t e, const char *what)
 __global__ void template_range_kernel(const int *, int, int, int, int, int, int, int *, int *);
 __global__ void template_center_kernel(const float *, int, float *, float *);
 __global__ void template_energy_kernel(const float *, int, int, float *);
-__global__ void channel_mean_kernel(const float *, int, float *);
+__global__ void channel_centre_kernel(const float *, int, float *);
 __global__ void zero_count_kernel(const float *, long long, long long, long long, unsigned long long *);
-__global__ void window_stats_kernel(const float *, int, int, int, const float *, float *, float *);
 int launch_tc(const Problem &P, const float *data_for_tc, int precision, unsigned *err, Scratch &ws,
               cudaStream_t s, int forced_nb, int template_group);
 int launch_wait_selftest(unsigned *err, unsigned ms, cudaStream_t s);
@@ -186,7 +248,7 @@ int validate_args(const Args &a)
                          (a.N - a.L) / a.step + 1);
     if (a.normalize != 0 && a.normalize != 1)
         return set_error(FMF_ERR_ARG, "normalize must be 0 (short) or 1 (full), got %d", a.normalize);
-    if (a.precision < FMF_PREC_FP32 || a.precision > FMF_PREC_BF16)
+    if (a.precision < FMF_PREC_FP32 || a.precision > FMF_PREC_AUTO)
         return set_error(FMF_ERR_ARG, "unknown precision %d", a.precision);
     if (a.flags & FMF_FLAG_DEVICE_POINTERS) {  // the kernels load these in place: 4-byte elements
         const void *ptrs[6] = {a.tpl, a.sst, a.mo, a.data, a.w, a.out};
@@ -197,16 +259,13 @@ int validate_args(const Args &a)
     return FMF_OK;
 }
 
-constexpr int kStatBlock = 4096;
-
 // ---------------------------------------------------------------- core (device pointers)
 int prepare_problem(const Args &a, Scratch &ws, cudaStream_t s, Problem *Pout, const float **data_for_tc)
 {
     int rc;
     const int T = (int)a.T, SC = (int)(a.S * a.C), L = (int)a.L, N = (int)a.N;
     const bool full = a.normalize == 1;
-    size_t stat_smem = (size_t)(kStatBlock + L + 1) * sizeof(double) * (full ? 2 : 1);
-    if (stat_smem > 227 * 1024)
+    if (window_stats_smem(L, full) > 227 * 1024)
         return set_error(FMF_ERR_SMEM, "template length %d too long for the window-statistics kernel", L);
 
     int *k_lo, *k_hi;
@@ -217,7 +276,7 @@ int prepare_problem(const Args &a, Scratch &ws, cudaStream_t s, Problem *Pout, c
     if ((rc = ws.get(&stat_e, (size_t)SC * N * (full ? 2 : 1), "window statistics")))
         return rc;
     if (full) {
-        if ((rc = ws.get(&mu, (size_t)SC, "channel means")) ||
+        if ((rc = ws.get(&mu, (size_t)SC, "channel centres")) ||
             (rc = ws.get(&dcen, (size_t)SC * N, "centred data")) ||
             (rc = ws.get(&tcen, (size_t)T * SC * L, "centred templates")) ||
             (rc = ws.get(&tsum, (size_t)T * SC, "template sums")))
@@ -239,17 +298,11 @@ int prepare_problem(const Args &a, Scratch &ws, cudaStream_t s, Problem *Pout, c
     }
     if (full) {
         template_center_kernel<<<(unsigned)((size_t)T * SC), 128, 0, s>>>(a.tpl, L, tcen, tsum);
-        channel_mean_kernel<<<SC, 1024, 0, s>>>(a.data, N, mu);
+        channel_centre_kernel<<<SC, 1024, 0, s>>>(a.data, N, mu);
         count_launch(2);
     }
-    if ((rc = cuda_status(cudaFuncSetAttribute(window_stats_kernel,
-                                               cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                               (int)stat_smem),
-                          "window statistics shared memory")))
+    if ((rc = launch_window_stats(a.data, N, L, SC, mu, dcen, stat_e, s)))
         return rc;
-    dim3 sgrid((N + kStatBlock - 1) / kStatBlock, SC);
-    window_stats_kernel<<<sgrid, 256, stat_smem, s>>>(a.data, N, L, kStatBlock, mu, dcen, stat_e);
-    count_launch();
     if ((rc = check_launch("preprocessing kernels")))
         return rc;
 
@@ -273,7 +326,8 @@ int prepare_problem(const Args &a, Scratch &ws, cudaStream_t s, Problem *Pout, c
     P.normalize = a.normalize;
     P.network_sum = a.sum_mode != 0;
     P.ntap = nullptr;
-    P.pre2f = nullptr;
+    P.pre2q = nullptr;
+    P.unit2 = nullptr;
     P.pre1f = nullptr;
     P.zweight = nullptr;
     P.vp_norm = P.vp_bias = P.vp_scale = nullptr;
@@ -343,8 +397,12 @@ static int run_device_ws(const Args &a, cudaStream_t s, Scratch &ws, Problem *Po
     if ((rc = prepare_problem(a, ws, s, &P, &data_for_tc)))
         return rc;
     cudaEvent_t ev_prep1 = mark(s);
-    span(ev_prep0, ev_prep1, 0);
-    if (a.precision != FMF_PREC_FP32) {
+    span(ev_prep0, ev_prep1, kSpanPrep);
+    int precision = a.precision;
+    if (precision == FMF_PREC_AUTO && (rc = choose_auto_precision(P, ws, s, &precision)))
+        return rc;
+    set_last_precision(precision);
+    if (precision != FMF_PREC_FP32) {
         unsigned *err = nullptr;
         if ((rc = device_error_word(&err)))
             return rc;
@@ -356,13 +414,13 @@ static int run_device_ws(const Args &a, cudaStream_t s, Scratch &ws, Problem *Po
         if (forced != 0 && forced != 32 && forced != 64 && forced != 128)
             return set_error(FMF_ERR_ARG, "tensor-core tile of %d lag blocks (32, 64 or 128)", forced);
         cudaEvent_t ev0 = mark(s);
-        rc = launch_tc(P, data_for_tc, a.precision, err, ws, s, forced, group);
-        span(ev0, mark(s), 1);
+        rc = launch_tc(P, data_for_tc, precision, err, ws, s, forced, group);
+        span(ev0, mark(s), kSpanKernel);
         return rc;
     }
     cudaEvent_t ev_main0 = mark(s);
     rc = launch_plain_all(P, s);
-    span(ev_main0, mark(s), 1);
+    span(ev_main0, mark(s), kSpanKernel);
     return rc;
 }
 
@@ -407,8 +465,11 @@ static int run_streamed(const Args &d, float *host_out, cudaStream_t s)
     Scratch ws(s);
     Problem P;
     const float *data_for_tc = nullptr;
+    cudaEvent_t ev_prep0 = mark(s);
     if ((rc = prepare_problem(d, ws, s, &P, &data_for_tc)))
         return rc;
+    cudaEvent_t ev_kern0 = mark(s);
+    span(ev_prep0, ev_kern0, kSpanPrep);
     const size_t row = (size_t)P.n_corr * (P.network_sum ? 1 : P.SC);  // floats per template
     const size_t out_bytes = (size_t)P.T * row * sizeof(float);
     const int n_chunks = out_bytes < ((size_t)64 << 20) ? 1 : (P.T < 8 ? P.T : 8);
@@ -431,10 +492,14 @@ static int run_streamed(const Args &d, float *host_out, cudaStream_t s)
     unsigned *err = nullptr;
     std::vector<unsigned char> tcfull;
     int split = 0;
-    if (d.precision != FMF_PREC_FP32) {
+    int precision = d.precision;
+    if (precision == FMF_PREC_AUTO && (rc = choose_auto_precision(P, ws, s, &precision)))
+        return rc;
+    set_last_precision(precision);
+    if (precision != FMF_PREC_FP32) {
         if ((rc = device_error_word(&err)))
             return rc;
-        split = d.precision == FMF_PREC_SPLIT_BF16;
+        split = precision == FMF_PREC_SPLIT_BF16;
         const char *nb_env = getenv("FMF_TC_NB");
         int forced = nb_env ? atoi(nb_env) : 0;
         if (d.flags & 0xff00)
@@ -483,16 +548,29 @@ static int run_streamed(const Args &d, float *host_out, cudaStream_t s)
             if (!rc)
                 e = cudaEventRecord(ev[c], s);
         }
+        // end of the last correlation kernel (twice: each span owns its events)
+        cudaEvent_t ev_kern1 = mark(s), ev_kern1b = mark(s), ev_out0 = nullptr;
+        span(ev_kern0, ev_kern1, kSpanKernel);
         for (int c = 0; c < launched && rc == FMF_OK && e == cudaSuccess; c++) {
             const int t0 = bounds[c], nt = bounds[c + 1] - bounds[c];
             if (nt <= 0)
                 continue;
             const size_t off = (size_t)t0 * row, n = (size_t)nt * row * sizeof(float);
-            if ((e = cudaStreamWaitEvent(s2, ev[c], 0)) != cudaSuccess ||
-                (e = cudaMemcpyAsync(host_out + off, P.out + off, n, cudaMemcpyDeviceToHost, s2)) !=
-                    cudaSuccess)
+            if ((e = cudaStreamWaitEvent(s2, ev[c], 0)) != cudaSuccess)
+                break;
+            if (!ev_out0)
+                ev_out0 = mark(s2);
+            populate_host(host_out + off, n);  // while the kernels run
+            if ((e = cudaMemcpyAsync(host_out + off, P.out + off, n, cudaMemcpyDeviceToHost, s2)) !=
+                cudaSuccess)
                 break;
         }
+        // the copy-out window, and its part after the last correlation kernel
+        cudaEvent_t ev_out1 = ev_out0 ? mark(s2) : nullptr, ev_out1b = ev_out0 ? mark(s2) : nullptr;
+        span(ev_out0, ev_out1, kSpanOutput);
+        span(ev_kern1b, ev_out1b, kSpanTail);
+        if (!ev_out1b && ev_kern1b)
+            cudaEventDestroy(ev_kern1b);
         if (e == cudaSuccess && rc == FMF_OK && zc)
             e = cudaMemcpyAsync(d.zero_counts, zc, (size_t)P.T * sizeof(unsigned long long),
                                 cudaMemcpyDeviceToHost, s);
@@ -550,15 +628,17 @@ static int run_host(const Args &a, cudaStream_t s)
         Scratch io(s);  // device copies of the arguments, freed in stream order
         Args d;
         float *out;
+        cudaEvent_t ev_in0 = mark(s);
         if ((rc = copy_inputs(a, io, s, &d)) || (rc = io.get(&out, out_n, "output copy")))
             return rc;
+        span(ev_in0, mark(s), kSpanInput);
         d.out = out;
         if ((rc = run_streamed(d, a.out, s)))
             return rc;
     }
     if ((rc = cuda_status(cudaStreamSynchronize(s), "matched filter")))
         return rc;
-    return a.precision != FMF_PREC_FP32 ? collect_device_errors() : FMF_OK;
+    return g_last_precision != FMF_PREC_FP32 ? collect_device_errors() : FMF_OK;
 }
 
 static int entry(const Args &a, void *stream)
@@ -744,7 +824,7 @@ static int search_detect_entry(const Args &a0, const DetectOut &o, cudaStream_t 
         return FMF_OK;
     if ((rc = detect_copy_back(o, a.T, dd, s)))
         return rc;
-    return a.precision != FMF_PREC_FP32 ? collect_device_errors() : FMF_OK;
+    return g_last_precision != FMF_PREC_FP32 ? collect_device_errors() : FMF_OK;
 }
 
 }  // namespace fmf
@@ -997,34 +1077,45 @@ int fmf_timing_begin(void)
     return FMF_OK;
 }
 
-int fmf_timing_end(double *prep_ms, double *kernel_ms, int *n_calls)
+int fmf_timing_end_ex(double *ms, int n_kinds, int *n_calls)
 {
-    double acc[2] = {0.0, 0.0};
+    double acc[fmf::kSpanKinds] = {};
     int calls = 0, rc = FMF_OK;
     for (int i = 0; i < fmf::g_nspans; i++) {
         fmf::TimedSpan &sp = fmf::g_spans[i];
-        float ms = 0.0f;
+        float t = 0.0f;
         cudaError_t e = cudaEventSynchronize(sp.b);
         if (e == cudaSuccess)
-            e = cudaEventElapsedTime(&ms, sp.a, sp.b);
+            e = cudaEventElapsedTime(&t, sp.a, sp.b);
         if (e != cudaSuccess)
             rc = fmf::cuda_status(e, "fmf_timing_end");
-        acc[sp.kind] += ms;
-        calls += sp.kind == 1;
+        acc[sp.kind] += t;
+        calls += sp.kind == fmf::kSpanKernel;
         cudaEventDestroy(sp.a);
         if (i + 1 >= fmf::g_nspans || fmf::g_spans[i + 1].a != sp.b)
             cudaEventDestroy(sp.b);
     }
     fmf::g_nspans = 0;
     fmf::g_timing = false;
-    if (prep_ms)
-        *prep_ms = acc[0];
-    if (kernel_ms)
-        *kernel_ms = acc[1];
+    for (int k = 0; ms && k < n_kinds; k++)
+        ms[k] = k < fmf::kSpanKinds ? acc[k] : 0.0;
     if (n_calls)
         *n_calls = calls;
     return rc;
 }
+
+int fmf_timing_end(double *prep_ms, double *kernel_ms, int *n_calls)
+{
+    double ms[2];
+    const int rc = fmf_timing_end_ex(ms, 2, n_calls);
+    if (prep_ms)
+        *prep_ms = ms[0];
+    if (kernel_ms)
+        *kernel_ms = ms[1];
+    return rc;
+}
+
+int fmf_last_precision(void) { return fmf::g_last_precision; }
 
 int fmf_release_cache(void)
 {

@@ -40,8 +40,10 @@ struct Problem {
     int network_sum;      // 1 weighted sum over channels, 0 per channel
     // Per-channel template lengths (Fisher-z network sum), else null:
     const int *ntap;      // (T, SC) taps of each channel (templates zero-padded to L)
-    const float2 *pre2f;  // (SC, N+1) prefix sums of d^2 (centred d for full) as hi + lo floats
-    const float2 *pre1f;  // (SC, N+1) prefix sums of centred d as hi + lo floats (full), else null
+    const long long *pre2q; // (SC, N+1) running sums of d^2 (centred d for full), exact, in units
+                            // unit2[ch] (64-bit fixed point)
+    const float *unit2;     // (SC) the fixed-point unit of each channel's running sums, a power of two
+    const float2 *pre1f;    // (SC, N+1) running sums of centred d as hi + lo floats (full), else null
     const float *zweight; // (T, SC) Fisher-z weight of each channel
     // (T) each, or null: when set, the tensor-core kernel writes
     // (tanh(x / vp_norm[t]) + vp_bias[t]) * vp_scale[t] for every output x
@@ -49,9 +51,9 @@ struct Problem {
 };
 
 #ifdef __CUDACC__
-// Window sums of a per-channel length n from prefix sums stored as float
-// pairs P = hi + lo (hi = fl(P), lo = fl(P - hi), ~48 significant bits), in
-// FP32 arithmetic only.
+// Window sums of a per-channel length n from running sums: of d^2 as exact
+// 64-bit fixed point (the difference of two is exact), of d as float pairs
+// P = hi + lo (hi = fl(P), lo = fl(P - hi), ~48 significant bits).
 
 // a - b = s + e exactly (Knuth's TwoSum on a and -b).
 __device__ __forceinline__ float two_diff(float a, float b, float &e)
@@ -77,24 +79,20 @@ __device__ __forceinline__ float2 pair_normalise(float h, float l)
     return make_float2(hi, l - (hi - h));
 }
 
-// 'short': sum of d^2 over the window [a, b) = (hi_b - hi_a) + (lo_b - lo_a).
-__device__ __forceinline__ float window_energy(float2 pa, float2 pb)
+// 'short': sum of d^2 over the window [a, b) from the fixed-point running sums.
+__device__ __forceinline__ float window_energy(long long pa, long long pb, float unit)
 {
-    return (pb.x - pa.x) + (pb.y - pa.y);
+    return __ll2float_rn(pb - pa) * unit;
 }
 
-// 'full': centred energy v = S2 - S1^2 / n and mean S1 / n of the window,
-// with S2, S1 and S1^2 / n carried as unevaluated float pairs (TwoSum, and
-// FMA for the exact square and division residuals), so that v keeps float
-// accuracy even when the window mean dominates (S2 / v large).
-__device__ __forceinline__ void window_centred(float2 a2, float2 b2, float2 a1, float2 b1, float nf,
-                                               float inv_n, float &v, float &mean)
+// 'full': centred energy v = S2 - S1^2 / n and mean S1 / n of a window whose
+// sums are the float pairs S2 = s2h + s2l (of d^2) and S1 = s1h + s1l (of d),
+// with S1^2 / n carried as an unevaluated float pair too (TwoSum, and FMA for
+// the exact square and division residuals), so that v keeps float accuracy
+// even when the window mean dominates (S2 / v large).
+__device__ __forceinline__ void window_centred_sums(float s2h, float s2l, float s1h, float s1l,
+                                                    float nf, float inv_n, float &v, float &mean)
 {
-    float e2, e1;
-    const float s2h = two_diff(b2.x, a2.x, e2);
-    const float s2l = e2 + (b2.y - a2.y);
-    const float s1h = two_diff(b1.x, a1.x, e1);
-    const float s1l = e1 + (b1.y - a1.y);
     const float h = s1h + s1l, l = s1l - (h - s1h);  // S1 = h + l, |l| <= ulp(h) / 2
     mean = h * inv_n;
     const float p = h * h;
@@ -105,6 +103,20 @@ __device__ __forceinline__ void window_centred(float2 a2, float2 b2, float2 a1, 
     const float vh = two_diff(s2h, qh, ev);
     const float r = vh + ((ev + s2l) - ql);
     v = r > 0.0f ? r : 0.0f;
+}
+
+// The same from running sums: of d^2 in fixed point (a2, b2; the exact
+// difference taken as a float pair), of d as float pairs (a1, b1).
+__device__ __forceinline__ void window_centred(long long a2, long long b2, float unit, float2 a1,
+                                               float2 b1, float nf, float inv_n, float &v, float &mean)
+{
+    const long long d2 = b2 - a2;
+    const float dh = __ll2float_rn(d2);  // an integer value: d2 - dh is exact
+    const float s2h = dh * unit, s2l = __ll2float_rn(d2 - __float2ll_rz(dh)) * unit;
+    float e1;
+    const float s1h = two_diff(b1.x, a1.x, e1);
+    const float s1l = e1 + (b1.y - a1.y);
+    window_centred_sums(s2h, s2l, s1h, s1l, nf, inv_n, v, mean);
 }
 #endif
 
@@ -118,6 +130,9 @@ void count_launch(int n = 1);
 void reset_launch_count();  // at the start of every entry point (fmf_last_launch_count)
 void keep_pool_cached();    // at the start of every entry point that allocates scratch
 int check_launch(const char *what);
+// Maps the host pages of a result buffer for writing before a copy into it
+// (parallel; a no-op where the kernel refuses).
+void populate_host(void *p, size_t bytes);
 
 // Stream-ordered scratch allocations (cudaMallocAsync from the device's
 // default pool).  The pool keeps freed blocks for reuse by later calls;
@@ -167,6 +182,12 @@ struct Args {
     long long zero_stop = 0;
 };
 int validate_args(const Args &a);
+// Window statistics of every channel (fmf_prep.cu): blocks of kStatWindows
+// windows; the shared memory a launch needs, and the launch itself.
+constexpr int kStatWindows = 4096;
+size_t window_stats_smem(int L, bool full);
+int launch_window_stats(const float *data, int N, int L, int SC, const float *mu, float *dcen,
+                        float *stat_e, cudaStream_t s);
 int prepare_problem(const Args &a, Scratch &ws, cudaStream_t s, Problem *P, const float **data_for_tc);
 
 // Tensor-core form (fmf_tc.cu).
@@ -181,6 +202,9 @@ size_t tc_prob_size();
 void tc_subset(const TcProb *full, int t0, int nt, TcProb *out);
 int launch_plain(const Problem &P, cudaStream_t stream);
 int launch_plain_all(const Problem &P, cudaStream_t stream);
+// FMF_PREC_AUTO: the precision a prepared search runs in (fmf_auto.cu); waits on s.
+int choose_auto_precision(const Problem &P, Scratch &ws, cudaStream_t s, int *precision);
+void set_last_precision(int precision);
 int device_error_word(unsigned **out);
 
 // Detection on network-summed rows (fmf_detect.cu).

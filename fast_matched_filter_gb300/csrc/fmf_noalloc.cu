@@ -40,8 +40,7 @@ namespace fmf {
 __global__ void template_range_kernel(const int *, int, int, int, int, int, int, int *, int *);
 __global__ void template_energy_kernel(const float *, int, int, float *);
 __global__ void template_center_kernel(const float *, int, float *, float *);
-__global__ void channel_mean_kernel(const float *, int, float *);
-__global__ void window_stats_kernel(const float *, int, int, int, const float *, float *, float *);
+__global__ void channel_centre_kernel(const float *, int, float *);
 
 // The only working memory of fmf_matched_filter_noalloc.  In host code this
 // name is a host-side stand-in, not a device address: host code uses the
@@ -51,7 +50,6 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[FMF_NOALLOC_SCR
 namespace {
 
 constexpr int kNoallocDevices = 64;
-constexpr int kNoallocStatBlock = 4096;  // windows per block of the statistics kernel
 unsigned char *g_scratch_base[kNoallocDevices];
 std::mutex g_scratch_mutex;
 
@@ -93,7 +91,7 @@ struct Carve {
 // Bytes of the carve of fmf_matched_filter_noalloc, or SIZE_MAX when the
 // search cannot fit (so that no product below can wrap): lag ranges, window
 // statistics ('full': (energy, mean) pairs), the template energies when the
-// caller passes none, then for 'full' the centred data, channel means,
+// caller passes none, then for 'full' the centred data, channel centres,
 // centred templates and their sums.
 size_t scratch_bytes(size_t T, size_t SC, size_t L, size_t N, bool full, bool energies)
 {
@@ -164,8 +162,7 @@ extern "C" int fmf_matched_filter_noalloc(const float *templates, const float *s
     }
     const int T = (int)n_templates, SC = (int)SCz, L = (int)n_samples_template,
               N = (int)n_samples_data;
-    const size_t stat_smem = (size_t)(kNoallocStatBlock + L + 1) * sizeof(double) * (full ? 2 : 1);
-    if (stat_smem > 227 * 1024)
+    if (window_stats_smem(L, full) > 227 * 1024)
         return set_error(FMF_ERR_SMEM, "noalloc: template length %d too long", L);
 
     unsigned char *base = nullptr;
@@ -196,16 +193,12 @@ extern "C" int fmf_matched_filter_noalloc(const float *templates, const float *s
     }
     if (full) {
         template_center_kernel<<<(unsigned)((size_t)T * SC), 128, 0, s>>>(templates, L, tcen, tsum);
-        channel_mean_kernel<<<SC, 1024, 0, s>>>(data, N, mu);
+        channel_centre_kernel<<<SC, 1024, 0, s>>>(data, N, mu);
         count_launch(2);
     }
-    cudaError_t e = cudaFuncSetAttribute(window_stats_kernel,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)stat_smem);
-    if (e != cudaSuccess)
-        return set_error(FMF_ERR_CUDA, "noalloc: statistics shared memory: %s", cudaGetErrorString(e));
-    dim3 sgrid((N + kNoallocStatBlock - 1) / kNoallocStatBlock, SC);
-    window_stats_kernel<<<sgrid, 256, stat_smem, s>>>(data, N, L, kNoallocStatBlock, mu, dcen, stat_e);
-    count_launch();
+    if ((rc = launch_window_stats(data, N, L, SC, mu, dcen, stat_e, s)))
+        return rc;
+    cudaError_t e;
     if ((e = cudaGetLastError()) != cudaSuccess)
         return set_error(FMF_ERR_CUDA, "noalloc: preprocessing launch: %s", cudaGetErrorString(e));
     if (!sum_cc_mode) {
@@ -234,7 +227,8 @@ extern "C" int fmf_matched_filter_noalloc(const float *templates, const float *s
     P.normalize = normalize;
     P.network_sum = sum_cc_mode != 0;
     P.ntap = nullptr;
-    P.pre2f = nullptr;
+    P.pre2q = nullptr;
+    P.unit2 = nullptr;
     P.pre1f = nullptr;
     P.zweight = nullptr;
     P.vp_norm = P.vp_bias = P.vp_scale = nullptr;

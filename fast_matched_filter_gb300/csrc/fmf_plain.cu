@@ -211,7 +211,7 @@ plain_kernel(const Problem P, const PlainGeom g)
             compute_phase(smem + b * g.stage_floats, g, taps, acc);
             if (VAR && phi == P.step - 1) {
                 // per-channel template length: window sums of that length from the
-                // float-pair prefix sums,
+                // running sums (d^2 in exact fixed point, d as float pairs),
                 // the 'precise' threshold (on the square root, matched_filter.c:650-652)
                 // and a Fisher-z network sum (matched_filter.c:596-601)
                 const size_t row = (size_t)t * P.SC + ch;
@@ -219,7 +219,8 @@ plain_kernel(const Problem P, const PlainGeom g)
                 const float ts = FULL ? P.tsum[row] : 0.0f;
                 const int n = P.ntap[row];
                 const float nf = (float)n, inv_n = 1.0f / nf;
-                const float2 *p2 = P.pre2f + (size_t)ch * (P.N + 1);
+                const long long *p2 = P.pre2q + (size_t)ch * (P.N + 1);
+                const float unit = P.unit2[ch];
                 const float2 *p1 = FULL ? P.pre1f + (size_t)ch * (P.N + 1) : nullptr;
 #pragma unroll
                 for (int r = 0; r < PL_R; r++) {
@@ -229,10 +230,11 @@ plain_kernel(const Problem P, const PlainGeom g)
                         float num = acc[r], ssd;
                         if (FULL) {
                             float mean;
-                            window_centred(p2[u], p2[u + n], p1[u], p1[u + n], nf, inv_n, ssd, mean);
+                            window_centred(p2[u], p2[u + n], unit, p1[u], p1[u + n], nf, inv_n, ssd,
+                                           mean);
                             num = fmaf(-mean, ts, num);
                         } else {
-                            ssd = window_energy(p2[u], p2[u + n]);
+                            ssd = window_energy(p2[u], p2[u + n], unit);
                         }
                         const float den = sqrtf(sst * ssd);
                         const float cc = den > kThreshold ? num / den : 0.0f;

@@ -7,8 +7,8 @@
 //    the FP64 sum of the centred values.  sum(t*(d-m)) equals
 //    sum((t-tbar)*(d-m)) exactly, so centring changes no result; it removes
 //    the template's DC term from the products the numerator sums.
-//  * channel_mean_kernel   : "full" only -- mean of each data channel (double-float sum),
-//    rounded to float; d - mu is exact in FP32 wherever mu/2 <= d <= 2 mu.
+//  * channel_centre_kernel : "full" only -- the constant subtracted from each
+//    data channel, the median of evenly spaced samples (robust to transients).
 //  * template_energy_kernel: the template energies sum(t^2) when the caller
 //    passes none, computed as the reference wrapper computes them for
 //    float32 templates (numpy.sum(templates**2, axis=-1),
@@ -18,13 +18,12 @@
 //    windows of L samples starting at each sample index:
 //      short: E = sum d^2                      (matched_filter.c:622)
 //      full : m = sum d'/L, V = sum d'^2 - (sum d')^2/L   (d' = d - mu)
-//    computed from a prefix sum local to each block of windows (so the
-//    differenced values are of the size of the block's energy, not of the
-//    whole trace's) held as double-float pairs in FP32 arithmetic: squares
-//    split exactly by FMA, TwoSum additions with the rounding errors carried
-//    in the low word, window differences by TwoSum; about 44 significant bits,
-//    the accuracy of an FP64 scan at FP32 speed (FP64 runs at ~2 operations
-//    per clock per SM on this part, which made this kernel FP64-bound).
+//    each window's sums composed from parts inside the window (the end of
+//    its first 32-sample chunk, whole chunks, the start of its last chunk) in
+//    double-float FP32 arithmetic, so that no window sum is the difference of
+//    running sums and a large transient before a quiet window costs it no
+//    digits (the reference's FP64 running sums lose 2^-53 of everything summed
+//    before the window, matched_filter.c:29-31, 660-705).
 #include "fmf_common.cuh"
 
 namespace fmf {
@@ -202,151 +201,258 @@ __global__ void template_center_kernel(const float *__restrict__ tpl, int L,
         tsum[row] = (float)tot;
 }
 
-// grid = SC blocks of 1024 threads: the mean of each data channel, rounded
-// to float, from double-float sums (FP32 arithmetic, fixed order); each
-// thread keeps four 16-byte loads in flight.
-__global__ void channel_mean_kernel(const float *__restrict__ data, int N,
-                                    float *__restrict__ mu)
+// grid = SC blocks of 1024 threads: the centre c[ch] that 'full' subtracts
+// from each data channel.  Any constant gives the same coefficients (the
+// centred templates sum to zero, so sum t'(d - m) = sum t'(d - c - (m - c))),
+// but the size of d - c sets the rounding of the numerator's products, of the
+// tensor-core split most of all (2^-16 of each operand).  The channel mean
+// moves with a large transient (a 1,000-sample burst at 1e3 shifts a 40,000-
+// sample channel's mean by ~80 times a 1e-2 noise); the median of 8192
+// evenly spaced samples stays at the level of the quiet data.  It is one of
+// the samples, so d - c is exact in FP32 wherever c/2 <= d <= 2c.
+constexpr int kCentreSample = 8192;
+__global__ void __launch_bounds__(1024) channel_centre_kernel(const float *__restrict__ data, int N,
+                                                              float *__restrict__ centre)
 {
-    __shared__ float2 red[32];
+    __shared__ float v[kCentreSample];
     const float *src = data + (size_t)blockIdx.x * N;
-    float h = 0.0f, l = 0.0f;
-    // the floats before the first 16-byte boundary of the row (any caller pointer), then
-    // float4 groups
-    const int head = (int)min((long long)N, (long long)(((16 - ((uintptr_t)src & 15)) & 15) >> 2));
-    for (int i = threadIdx.x; i < head; i += blockDim.x)
-        pair_add(h, l, src[i], 0.0f);
-    const float4 *v4 = reinterpret_cast<const float4 *>(src + head);
-    const int n4 = (N - head) >> 2;
-    constexpr int U = 4;
-    for (int i0 = threadIdx.x; i0 < n4; i0 += U * blockDim.x) {
-        float4 x[U];
-#pragma unroll
-        for (int u = 0; u < U; u++)
-            x[u] = i0 + u * (int)blockDim.x < n4 ? v4[i0 + u * blockDim.x] : make_float4(0.f, 0.f, 0.f, 0.f);
-#pragma unroll
-        for (int u = 0; u < U; u++) {
-            pair_add(h, l, x[u].x, 0.0f);
-            pair_add(h, l, x[u].y, 0.0f);
-            pair_add(h, l, x[u].z, 0.0f);
-            pair_add(h, l, x[u].w, 0.0f);
+    const int S = min(N, kCentreSample);
+    for (int k = threadIdx.x; k < kCentreSample; k += blockDim.x)
+        v[k] = k < S ? src[(long long)k * N / S] : INFINITY;
+    __syncthreads();
+    for (int k = 2; k <= kCentreSample; k <<= 1) {  // bitonic sort, ascending
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            for (int i = threadIdx.x; i < kCentreSample; i += blockDim.x) {
+                const int p = i ^ j;
+                if (p > i) {
+                    const float a = v[i], b = v[p];
+                    if (((i & k) == 0) == (a > b)) {
+                        v[i] = b;
+                        v[p] = a;
+                    }
+                }
+            }
+            __syncthreads();
         }
     }
-    for (int i = head + 4 * n4 + threadIdx.x; i < N; i += blockDim.x)
-        pair_add(h, l, src[i], 0.0f);
-    for (int o = 16; o > 0; o >>= 1) {
-        const float yh = __shfl_down_sync(0xffffffffu, h, o), yl = __shfl_down_sync(0xffffffffu, l, o);
-        pair_add(h, l, yh, yl);
-    }
-    if ((threadIdx.x & 31) == 0)
-        red[threadIdx.x >> 5] = make_float2(h, l);
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        float th = 0.0f, tl = 0.0f;
-        for (int i = 0; i < (int)(blockDim.x >> 5); i++)
-            pair_add(th, tl, red[i].x, red[i].y);
-        mu[blockIdx.x] = (float)(((double)th + (double)tl) / (double)N);
-    }
+    if (threadIdx.x == 0)
+        centre[blockIdx.x] = v[(S - 1) / 2];
 }
 
-// In-place inclusive scan of a[1..len] (a[0] = 0) as double-float pairs, by the
-// block: a contiguous segment per thread, then the segment totals by warp
-// shuffles and one thread over the warps.
-__device__ void block_scan_pair(float2 *a, int len, float2 *part)
-{
-    const int nt = blockDim.x;
-    const int seg = (len + nt - 1) / nt;
-    const int b = 1 + threadIdx.x * seg;
-    const int e = min(len + 1, b + seg);
-    float h = 0.0f, l = 0.0f;
-    for (int i = b; i < e; i++) {
-        const float2 x = a[i];
-        pair_add(h, l, x.x, x.y);
-        a[i] = make_float2(h, l);
-    }
-    // inclusive warp scan of the segment totals
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    float xh = h, xl = l;
-    for (int o = 1; o < 32; o <<= 1) {
-        const float yh = __shfl_up_sync(0xffffffffu, xh, o), yl = __shfl_up_sync(0xffffffffu, xl, o);
-        if (lane >= o)
-            pair_add(xh, xl, yh, yl);
-    }
-    if (lane == 31)
-        part[wid] = make_float2(xh, xl);
-    // exclusive value of this thread within its warp
-    float eh = __shfl_up_sync(0xffffffffu, xh, 1), el = __shfl_up_sync(0xffffffffu, xl, 1);
-    if (lane == 0)
-        eh = el = 0.0f;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        float rh = 0.0f, rl = 0.0f;
-        for (int i = 0; i < (nt >> 5); i++) {
-            const float2 v = part[i];
-            part[i] = make_float2(rh, rl);
-            pair_add(rh, rl, v.x, v.y);
-        }
-    }
-    __syncthreads();
-    float oh = part[wid].x, ol = part[wid].y;
-    pair_add(oh, ol, eh, el);
-    for (int i = b; i < e; i++) {
-        float2 x = a[i];
-        pair_add(x.x, x.y, oh, ol);
-        a[i] = x;
-    }
-    __syncthreads();
-}
+// ---------------------------------------------------------------- window statistics
+// Each window's sums are composed from parts that all lie inside the window,
+// never taken as the difference of running sums: with samples in 32-sample
+// chunks, the window [u, u + L) is
+//     (u to the end of u's chunk) + (whole chunks) + (start of the last chunk to u + L),
+// each part summed in double-float FP32 arithmetic (squares split exactly by
+// FMA, TwoSum additions with the rounding errors carried in the low word).
+// A difference of running sums loses the digits of everything summed before
+// the window -- after a large transient, a quiet window holds 1e-10 of the
+// running energy -- whereas here the sums of d^2 have only non-negative parts
+// (about 44 significant bits whatever came before) and the sums of d' are
+// accurate to 2^-44 of the window's own sum of |d'|.
 
-// grid = (ceil(N / B), SC), block 256, dynamic smem = (B + L + 1) * 8 * (full ? 2 : 1)
-__global__ void window_stats_kernel(const float *__restrict__ data, int N, int L,
-                                    int B, const float *__restrict__ mu,
-                                    float *__restrict__ dcen,
-                                    float *__restrict__ stat_e)
+constexpr int kStatThreads = 256;
+constexpr int kStatGroup = 16;  // consecutive windows per thread
+static_assert(kStatWindows == kStatThreads * kStatGroup, "one group of windows per thread");
+
+// padded shared-memory index: one spare slot per 32, so that threads 16 or 32
+// samples apart hit different banks
+__device__ __forceinline__ int stat_pad(int i) { return i + (i >> 5); }
+
+// Staged samples per block: the windows' span plus a zero tail read by the last
+// group's loops, a multiple of the 32-sample chunk.
+__host__ __device__ __forceinline__ int stat_span(int L) { return (kStatWindows + L + 63) & ~31; }
+
+// Shared-memory carve (in floats, each part 16-byte aligned): squares, values
+// ('full'), chunk sums of both, staged outputs.
+struct StatLayout {
+    int s2, s1, q2, q1, out, total;
+    __host__ __device__ StatLayout(int L, bool full)
+    {
+        const int span = stat_span(L), padded = span + (span >> 5);
+        const int nq = span >> 5, pw = kStatWindows + (kStatWindows >> 5);
+        auto al = [](int x) { return (x + 3) & ~3; };
+        s2 = 0;
+        s1 = al(s2 + 2 * padded);
+        q2 = al(s1 + (full ? padded : 0));
+        q1 = al(q2 + 2 * nq);
+        out = al(q1 + (full ? 2 * nq : 0));
+        total = al(out + (full ? 2 : 1) * pw);
+    }
+};
+
+size_t window_stats_smem(int L, bool full) { return (size_t)StatLayout(L, full).total * sizeof(float); }
+
+// grid = (ceil(N / kStatWindows), SC), kStatThreads threads, dynamic smem =
+// window_stats_smem(L, full).  short: stat_e[ch][u] = sum of d^2 over
+// [u, u + L); full: (centred energy, mean) of d' = d - mu[ch] as float pairs,
+// and the centred data into dcen.  Windows past N - L are not written.
+__global__ void __launch_bounds__(kStatThreads)
+window_stats_kernel(const float *__restrict__ data, int N, int L, const float *__restrict__ mu,
+                    float *__restrict__ dcen, float *__restrict__ stat_e)
 {
-    extern __shared__ float2 shp[];
-    __shared__ float2 part[33];
-    const int ch = blockIdx.y;
-    const long long c0 = (long long)blockIdx.x * B;
-    const int len = (int)min((long long)B + L, (long long)N - c0);
+    extern __shared__ float4 stat_smem[];
     const bool full = mu != nullptr;
-    float2 *P2 = shp;
-    float2 *P1 = shp + (B + L + 1);
-    const float *src = data + (size_t)ch * N + c0;
+    const StatLayout lay(L, full);
+    float *base = reinterpret_cast<float *>(stat_smem);
+    float2 *s2 = reinterpret_cast<float2 *>(base + lay.s2);
+    float *s1 = base + lay.s1;
+    float2 *q2 = reinterpret_cast<float2 *>(base + lay.q2);
+    float2 *q1 = reinterpret_cast<float2 *>(base + lay.q1);
+    float *out1 = base + lay.out;
+    float2 *out2 = reinterpret_cast<float2 *>(base + lay.out);
+
+    const int ch = blockIdx.y;
+    const long long c0 = (long long)blockIdx.x * kStatWindows;
+    const int len = (int)min((long long)kStatWindows + L - 1, (long long)N - c0);
+    const int nwin = min(kStatWindows, len - L + 1);
+    const int span = stat_span(L), nq = span >> 5;
     const float m = full ? mu[ch] : 0.0f;
-    for (int i = threadIdx.x; i < len; i += blockDim.x) {
-        const float v = src[i] - m;
-        if (full && i < B)
-            dcen[(size_t)ch * N + c0 + i] = v;
+    const float *src = data + (size_t)ch * N + c0;
+    for (int i = threadIdx.x; i < span; i += kStatThreads) {
+        float v = 0.0f;
+        if (i < len) {
+            v = src[i] - m;
+            if (full && i < kStatWindows)
+                dcen[(size_t)ch * N + c0 + i] = v;
+        }
         const float sq = v * v;
-        P2[i + 1] = make_float2(sq, fmaf(v, v, -sq));  // v^2 exactly
+        s2[stat_pad(i)] = make_float2(sq, fmaf(v, v, -sq));  // v^2 exactly
         if (full)
-            P1[i + 1] = make_float2(v, 0.0f);
-    }
-    if (threadIdx.x == 0) {
-        P2[0] = make_float2(0.0f, 0.0f);
-        if (full)
-            P1[0] = make_float2(0.0f, 0.0f);
+            s1[stat_pad(i)] = v;
     }
     __syncthreads();
-    block_scan_pair(P2, len, part);
-    if (full)
-        block_scan_pair(P1, len, part);
-    const int nwin = min(B, len - L + 1);
+    for (int k = threadIdx.x; k < nq; k += kStatThreads) {  // chunk sums
+        float h2 = 0.0f, l2 = 0.0f, h1 = 0.0f, l1 = 0.0f;
+#pragma unroll 8
+        for (int j = 0; j < 32; j++) {
+            const float2 x = s2[stat_pad(32 * k + j)];
+            pair_add(h2, l2, x.x, x.y);
+            if (full)
+                pair_add(h1, l1, s1[stat_pad(32 * k + j)], 0.0f);
+        }
+        q2[k] = make_float2(h2, l2);
+        if (full)
+            q1[k] = make_float2(h1, l1);
+    }
+    __syncthreads();
+
     const float Lf = (float)L, invL = 1.0f / Lf;
-    for (int u = threadIdx.x; u < nwin; u += blockDim.x) {
-        const size_t o = (size_t)ch * N + c0 + u;
+    auto emit = [&](int u, float h2, float l2, float h1, float l1) {
         if (full) {
             float v, mean;
-            window_centred(P2[u], P2[u + L], P1[u], P1[u + L], Lf, invL, v, mean);
-            reinterpret_cast<float2 *>(stat_e)[o] = make_float2(v, mean);
+            window_centred_sums(h2, l2, h1, l1, Lf, invL, v, mean);
+            out2[stat_pad(u)] = make_float2(v, mean);
         } else {
-            float e;
-            const float2 a2 = P2[u], b2 = P2[u + L];
-            const float h = two_diff(b2.x, a2.x, e);
-            stat_e[o] = h + (e + (b2.y - a2.y));
+            out1[stat_pad(u)] = h2 + l2;
+        }
+    };
+    if (L >= 32) {
+        // windows u0 .. u0 + 15 of this thread: all start in chunk a and end
+        // past it, so suffix (in chunk a) + whole chunks + tail never overlap
+        const int u0 = threadIdx.x * kStatGroup;
+        if (u0 < nwin) {
+            const int a = u0 >> 5;
+            float sh2[kStatGroup], sl2[kStatGroup], sh1[kStatGroup], sl1[kStatGroup];
+            float h2 = 0.0f, l2 = 0.0f, h1 = 0.0f, l1 = 0.0f;
+            for (int j = u0 + kStatGroup; j < 32 * a + 32; j++) {
+                const float2 x = s2[stat_pad(j)];
+                pair_add(h2, l2, x.x, x.y);
+                if (full)
+                    pair_add(h1, l1, s1[stat_pad(j)], 0.0f);
+            }
+#pragma unroll
+            for (int r = kStatGroup - 1; r >= 0; r--) {  // suffix sums, last start first
+                const float2 x = s2[stat_pad(u0 + r)];
+                pair_add(h2, l2, x.x, x.y);
+                sh2[r] = h2;
+                sl2[r] = l2;
+                if (full) {
+                    pair_add(h1, l1, s1[stat_pad(u0 + r)], 0.0f);
+                    sh1[r] = h1;
+                    sl1[r] = l1;
+                }
+            }
+            const int e0 = u0 + L;  // end (exclusive) of window u0
+            float mh2 = 0.0f, ml2 = 0.0f, mh1 = 0.0f, ml1 = 0.0f;  // whole chunks
+            for (int k = a + 1; k < (e0 >> 5); k++) {
+                pair_add(mh2, ml2, q2[k].x, q2[k].y);
+                if (full)
+                    pair_add(mh1, ml1, q1[k].x, q1[k].y);
+            }
+            float rh2 = 0.0f, rl2 = 0.0f, rh1 = 0.0f, rl1 = 0.0f;  // tail in the last chunk
+            for (int j = e0 & ~31; j < e0; j++) {
+                const float2 x = s2[stat_pad(j)];
+                pair_add(rh2, rl2, x.x, x.y);
+                if (full)
+                    pair_add(rh1, rl1, s1[stat_pad(j)], 0.0f);
+            }
+#pragma unroll
+            for (int r = 0; r < kStatGroup; r++) {
+                const int e = e0 + r;
+                if (r > 0 && (e & 31) == 0) {  // the tail's chunk is whole: move it to the middle
+                    const int k = (e >> 5) - 1;
+                    pair_add(mh2, ml2, q2[k].x, q2[k].y);
+                    rh2 = rl2 = 0.0f;
+                    if (full) {
+                        pair_add(mh1, ml1, q1[k].x, q1[k].y);
+                        rh1 = rl1 = 0.0f;
+                    }
+                }
+                if (u0 + r < nwin) {
+                    float th2 = sh2[r], tl2 = sl2[r], th1 = 0.0f, tl1 = 0.0f;
+                    pair_add(th2, tl2, mh2, ml2);
+                    pair_add(th2, tl2, rh2, rl2);
+                    if (full) {
+                        th1 = sh1[r];
+                        tl1 = sl1[r];
+                        pair_add(th1, tl1, mh1, ml1);
+                        pair_add(th1, tl1, rh1, rl1);
+                    }
+                    emit(u0 + r, th2, tl2, th1, tl1);
+                }
+                const float2 x = s2[stat_pad(e)];
+                pair_add(rh2, rl2, x.x, x.y);
+                if (full)
+                    pair_add(rh1, rl1, s1[stat_pad(e)], 0.0f);
+            }
+        }
+    } else {  // windows shorter than a chunk: direct sums
+        for (int u = threadIdx.x; u < nwin; u += kStatThreads) {
+            float h2 = 0.0f, l2 = 0.0f, h1 = 0.0f, l1 = 0.0f;
+            for (int j = u; j < u + L; j++) {
+                const float2 x = s2[stat_pad(j)];
+                pair_add(h2, l2, x.x, x.y);
+                if (full)
+                    pair_add(h1, l1, s1[stat_pad(j)], 0.0f);
+            }
+            emit(u, h2, l2, h1, l1);
         }
     }
+    __syncthreads();
+    for (int u = threadIdx.x; u < nwin; u += kStatThreads) {  // coalesced stores
+        const size_t o = (size_t)ch * N + c0 + u;
+        if (full)
+            reinterpret_cast<float2 *>(stat_e)[o] = out2[stat_pad(u)];
+        else
+            stat_e[o] = out1[stat_pad(u)];
+    }
+}
+
+int launch_window_stats(const float *data, int N, int L, int SC, const float *mu, float *dcen,
+                        float *stat_e, cudaStream_t s)
+{
+    const size_t smem = window_stats_smem(L, mu != nullptr);
+    cudaError_t e = cudaFuncSetAttribute(window_stats_kernel,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess)
+        return set_error(FMF_ERR_CUDA, "window statistics shared memory (%zu bytes): %s", smem,
+                         cudaGetErrorString(e));
+    dim3 grid((N + kStatWindows - 1) / kStatWindows, SC);
+    window_stats_kernel<<<grid, kStatThreads, smem, s>>>(data, N, L, mu, dcen, stat_e);
+    count_launch();
+    return FMF_OK;
 }
 
 }  // namespace fmf

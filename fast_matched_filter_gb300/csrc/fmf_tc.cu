@@ -47,7 +47,7 @@
 //               (channel order, fused multiply-add), outputs.
 // Instantiations: tc_persistent<VAR, PARTS>.  VAR: per-channel template
 // lengths (the issuers cut each channel's K range at its own taps; 16 epilogue
-// warps, warps 4-19, form window sums from float-pair prefix sums and add
+// warps, warps 4-19, form window sums from per-channel running sums and add
 // atanh(cc) * z).  PARTS: the items of a small search are split into channel
 // parts whose partial sums a second kernel adds in order.
 // Every wait is bounded (globaltimer); on timeout the CTA raises an error
@@ -837,14 +837,17 @@ __global__ void __launch_bounds__(tc_threads(VAR), 1) tc_persistent(const __grid
                 if constexpr (!VAR)
                     load_chunk(0);
                 // per-channel lengths: the channel's own length and Fisher-z weight, its
-                // prefix-sum pairs (d^2, and d for full) at the first window of the thread
+                // running sums (d^2 in fixed point, and d for full) at the first window of
+                // the thread
                 [[maybe_unused]] int ntap = 0;
-                [[maybe_unused]] float zw = 0.0f, nf = 0.0f, inv_n = 0.0f;
-                [[maybe_unused]] const float2 *pf = nullptr, *pg = nullptr;
+                [[maybe_unused]] float zw = 0.0f, nf = 0.0f, inv_n = 0.0f, unit = 0.0f;
+                [[maybe_unused]] const long long *pf = nullptr;
+                [[maybe_unused]] const float2 *pg = nullptr;
                 if constexpr (VAR) {
                     ntap = pr.P.ntap[row];
                     zw = pr.P.zweight[row];
-                    pf = pr.P.pre2f + (size_t)ch * (N + 1) + u0;
+                    unit = pr.P.unit2[ch];
+                    pf = pr.P.pre2q + (size_t)ch * (N + 1) + u0;
                     pg = full ? pr.P.pre1f + (size_t)ch * (N + 1) + u0 : nullptr;
                     nf = (float)ntap;
                     inv_n = 1.0f / nf;
@@ -871,7 +874,7 @@ __global__ void __launch_bounds__(tc_threads(VAR), 1) tc_persistent(const __grid
                             mbar_arrive(dempty0 + 8 * d);
                     }
                     if constexpr (VAR) {
-                        // window sums of the channel's own length from the float-pair prefix sums,
+                        // window sums of the channel's own length from the running sums,
                         // the 'precise' threshold on the square root, and
                         // atanh(cc - 10 eps) * z into the network sum
                         // CHECK: some output of the warp lies outside the valid lags (clamped
@@ -894,37 +897,39 @@ __global__ void __launch_bounds__(tc_threads(VAR), 1) tc_persistent(const __grid
                             };
                             const bool ld = !CHECK || any;
                             const float2 z2 = make_float2(0.0f, 0.0f);
-                            if (!full) {  // hi + lo float prefix pairs: FP32 only
-                                const float2 *__restrict__ pf_hi = pf + ntap;
+                            if (!full) {  // fixed-point running sums: an exact difference
+                                const long long *__restrict__ pf_hi = pf + ntap;
 #pragma unroll
                                 for (int h = 0; h < CH; h += 4) {  // loads of 4 values, then their use
-                                    float2 lo[4], hi[4];
+                                    long long lo[4], hi[4];
 #pragma unroll
                                     for (int j = 0; j < 4; j++) {
                                         const int o = off(h + j);
-                                        lo[j] = ld ? pf[o] : z2;
-                                        hi[j] = ld ? pf_hi[o] : z2;
+                                        lo[j] = ld ? pf[o] : 0;
+                                        hi[j] = ld ? pf_hi[o] : 0;
                                     }
 #pragma unroll
                                     for (int j = 0; j < 4; j++)
-                                        var_value(h + j, x[h + j], window_energy(lo[j], hi[j]));
+                                        var_value(h + j, x[h + j], window_energy(lo[j], hi[j], unit));
                                 }
                             } else {  // centred windows: double-float FP32 arithmetic
 #pragma unroll
                                 for (int h = 0; h < CH; h += 2) {
-                                    float2 lo2[2], hi2[2], lo1[2], hi1[2];
+                                    long long lo2[2], hi2[2];
+                                    float2 lo1[2], hi1[2];
 #pragma unroll
                                     for (int j = 0; j < 2; j++) {
                                         const int o = off(h + j);
-                                        lo2[j] = ld ? pf[o] : z2;
-                                        hi2[j] = ld ? pf[o + ntap] : z2;
+                                        lo2[j] = ld ? pf[o] : 0;
+                                        hi2[j] = ld ? pf[o + ntap] : 0;
                                         lo1[j] = ld ? pg[o] : z2;
                                         hi1[j] = ld ? pg[o + ntap] : z2;
                                     }
 #pragma unroll
                                     for (int j = 0; j < 2; j++) {
                                         float v, mean;
-                                        window_centred(lo2[j], hi2[j], lo1[j], hi1[j], nf, inv_n, v, mean);
+                                        window_centred(lo2[j], hi2[j], unit, lo1[j], hi1[j], nf, inv_n, v,
+                                                       mean);
                                         var_value(h + j, fmaf(-mean, ts, x[h + j]), v);
                                     }
                                 }

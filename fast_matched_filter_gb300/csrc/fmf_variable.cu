@@ -18,8 +18,9 @@
 // Kernels: metadata (Fisher-z weights per (t, ch), lag ranges and weight sums
 // per template, the cumulative scale in one thread, each in the reference's
 // float operation order),
-// masked/centred templates, double-float prefix sums of d^2 and d stored as float
-// pairs (global, so that any window length is a few FP32 operations), the
+// masked/centred templates, running sums over the whole trace of d^2 (exact
+// 64-bit fixed point) and of d (float pairs), so that any window length is a
+// few operations, the
 // numerator kernel with its
 // variable-length epilogue -- the plain FP32 kernel (fmf_plain.cu) or the
 // tensor-core kernel (fmf_tc.cu), whose issuers stop each channel's K range
@@ -34,7 +35,7 @@
 
 namespace fmf {
 
-__global__ void channel_mean_kernel(const float *, int, float *);
+__global__ void channel_centre_kernel(const float *, int, float *);
 int collect_device_errors();
 
 // Fisher-z weight of every (t, ch), one thread each, in the reference's mix
@@ -177,66 +178,118 @@ __global__ void vp_template_kernel(const float *__restrict__ tpl, const int *__r
 
 constexpr int kPrefixBlock = 2048;
 
-// Prefix sums of d'^2 and d' (d' = d - mu) per channel in three phases, all in
-// double-float FP32 arithmetic (squares split exactly by FMA, TwoSum
-// additions; FP64 runs at ~2 operations per clock per SM on this part):
-// block sums, their exclusive scan per channel, then the scan inside each
-// block plus its offset.  Stored as normalised float pairs hi = fl(P),
-// lo = P - hi (~44-48 significant bits), so that the correlation epilogues
-// form window sums in FP32 arithmetic, exact to float rounding while the
-// window holds more than ~2^-24 of the channel's energy up to that point.
+// Running sums per channel for windows of any length, in three phases (block
+// sums, their exclusive scan per channel, the scan inside each block plus its
+// offset):
+//  * of d'^2 (d' = d - mu; d for 'short') as 64-bit integers in a unit q of
+//    the channel (a power of two, its energy times 2^-60): each square, split
+//    exactly by FMA into two floats, is rounded to the unit, and the integer
+//    sums are exact, so a window's energy is an exact difference -- only the
+//    rounding of its own n squares remains, at most n q, whatever was summed
+//    before it.  (A floating-point running sum loses the digits of everything
+//    summed before the window: after a large transient a quiet window holds
+//    1e-10 of the channel's running energy.)
+//  * of d' ('full') as normalised float pairs hi = fl(P), lo = P - hi summed in
+//    double-float FP32 arithmetic: the window sum of d' enters the centred
+//    energy multiplied by the window mean, so its cancellation error stays far
+//    below float rounding of the energy.
+
+// grid = SC blocks of 1024 threads: the fixed-point unit q[ch] of the running
+// sums of d'^2: 2^(e - 60) with the channel energy below 2^e, so that no
+// running sum exceeds 2^61 units (clamped to the normal float range).
+__global__ void channel_unit_kernel(const float *__restrict__ data, int N, const float *__restrict__ mu,
+                                    float *__restrict__ unit)
+{
+    __shared__ float2 red[32];
+    const float m = mu ? mu[blockIdx.x] : 0.0f;
+    const float *src = data + (size_t)blockIdx.x * N;
+    float h = 0.0f, l = 0.0f;
+    for (int i = threadIdx.x; i < N; i += blockDim.x) {
+        const float v = src[i] - m, sq = v * v;
+        pair_add(h, l, sq, fmaf(v, v, -sq));
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        const float yh = __shfl_down_sync(0xffffffffu, h, o), yl = __shfl_down_sync(0xffffffffu, l, o);
+        pair_add(h, l, yh, yl);
+    }
+    if ((threadIdx.x & 31) == 0)
+        red[threadIdx.x >> 5] = make_float2(h, l);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float th = 0.0f, tl = 0.0f;
+        for (int i = 0; i < (int)(blockDim.x >> 5); i++)
+            pair_add(th, tl, red[i].x, red[i].y);
+        int e = 0;
+        // the sum rounded up by a margin, so that the float total cannot undershoot it
+        frexpf((th + tl) * 1.0001f, &e);
+        unit[blockIdx.x] = th + tl > 0.0f ? ldexpf(1.0f, max(e - 60, -126)) : 1.0f;
+    }
+}
+
+// d'^2 in units of 1 / inv_unit, as the two roundings of its exact float split
+__device__ __forceinline__ long long fixed_square(float v, float inv_unit)
+{
+    const float sq = v * v;
+    return __float2ll_rn(sq * inv_unit) + __float2ll_rn(fmaf(v, v, -sq) * inv_unit);
+}
 
 // Phase 1, grid (blocks, SC), 256 threads: block sums.
 __global__ void prefix_block_kernel(const float *__restrict__ data, int N, const float *__restrict__ mu,
-                                    float2 *__restrict__ bs2, float2 *__restrict__ bs1, int nblk)
+                                    const float *__restrict__ unit, long long *__restrict__ bs2,
+                                    float2 *__restrict__ bs1, int nblk)
 {
-    __shared__ float2 r2[32], r1[32];
+    __shared__ long long r2[32];
+    __shared__ float2 r1[32];
     const int ch = blockIdx.y, blk = blockIdx.x;
-    const float m = mu ? mu[ch] : 0.0f;
+    const float m = mu ? mu[ch] : 0.0f, inv_unit = 1.0f / unit[ch];
     const float *src = data + (size_t)ch * N;
-    float h2 = 0.0f, l2 = 0.0f, h1 = 0.0f, l1 = 0.0f;
+    long long s2 = 0;
+    float h1 = 0.0f, l1 = 0.0f;
     for (int i = blk * kPrefixBlock + threadIdx.x; i < min(N, (blk + 1) * kPrefixBlock); i += blockDim.x) {
-        const float v = src[i] - m, sq = v * v;
-        pair_add(h2, l2, sq, fmaf(v, v, -sq));
+        const float v = src[i] - m;
+        s2 += fixed_square(v, inv_unit);
         pair_add(h1, l1, v, 0.0f);
     }
     for (int o = 16; o > 0; o >>= 1) {
-        const float a = __shfl_down_sync(0xffffffffu, h2, o), b = __shfl_down_sync(0xffffffffu, l2, o);
+        s2 += __shfl_down_sync(0xffffffffu, s2, o);
         const float c = __shfl_down_sync(0xffffffffu, h1, o), d = __shfl_down_sync(0xffffffffu, l1, o);
-        pair_add(h2, l2, a, b);
         pair_add(h1, l1, c, d);
     }
     if ((threadIdx.x & 31) == 0) {
-        r2[threadIdx.x >> 5] = make_float2(h2, l2);
+        r2[threadIdx.x >> 5] = s2;
         r1[threadIdx.x >> 5] = make_float2(h1, l1);
     }
     __syncthreads();
     if (threadIdx.x == 0) {
-        float a = 0.0f, b = 0.0f, c = 0.0f, d = 0.0f;
+        long long a = 0;
+        float c = 0.0f, d = 0.0f;
         for (int i = 0; i < (int)(blockDim.x >> 5); i++) {
-            pair_add(a, b, r2[i].x, r2[i].y);
+            a += r2[i];
             pair_add(c, d, r1[i].x, r1[i].y);
         }
-        bs2[(size_t)ch * nblk + blk] = pair_normalise(a, b);
+        bs2[(size_t)ch * nblk + blk] = a;
         bs1[(size_t)ch * nblk + blk] = pair_normalise(c, d);
     }
 }
 
-// Phase 2, one thread per channel: exclusive scan of the block sums
-// (renormalised at every step).
-__global__ void prefix_offsets_kernel(float2 *bs2, float2 *bs1, int nblk, int SC)
+// Phase 2, one thread per channel: exclusive scan of the block sums (the
+// float pairs renormalised at every step).
+__global__ void prefix_offsets_kernel(long long *bs2, float2 *bs1, int nblk, int SC)
 {
     const int ch = blockIdx.x * blockDim.x + threadIdx.x;
     if (ch >= SC)
         return;
-    float2 a = make_float2(0.0f, 0.0f), b = make_float2(0.0f, 0.0f);
-    float2 *p2 = bs2 + (size_t)ch * nblk, *p1 = bs1 + (size_t)ch * nblk;
+    long long a = 0;
+    float2 b = make_float2(0.0f, 0.0f);
+    long long *p2 = bs2 + (size_t)ch * nblk;
+    float2 *p1 = bs1 + (size_t)ch * nblk;
     constexpr int G = 8;  // loads of a group issued before the dependent additions
     for (int i0 = 0; i0 < nblk; i0 += G) {
-        float2 x[G], y[G];
+        long long x[G];
+        float2 y[G];
 #pragma unroll
         for (int j = 0; j < G; j++) {
-            x[j] = i0 + j < nblk ? p2[i0 + j] : make_float2(0.0f, 0.0f);
+            x[j] = i0 + j < nblk ? p2[i0 + j] : 0;
             y[j] = i0 + j < nblk ? p1[i0 + j] : make_float2(0.0f, 0.0f);
         }
 #pragma unroll
@@ -245,8 +298,7 @@ __global__ void prefix_offsets_kernel(float2 *bs2, float2 *bs1, int nblk, int SC
                 p2[i0 + j] = a;
                 p1[i0 + j] = b;
             }
-            pair_add(a.x, a.y, x[j].x, x[j].y);
-            a = pair_normalise(a.x, a.y);
+            a += x[j];
             pair_add(b.x, b.y, y[j].x, y[j].y);
             b = pair_normalise(b.x, b.y);
         }
@@ -254,21 +306,25 @@ __global__ void prefix_offsets_kernel(float2 *bs2, float2 *bs1, int nblk, int SC
 }
 
 // Phase 3, grid (blocks, SC), 256 threads: inclusive scan of the block plus
-// its offset -> P2[ch][i + 1] = sum_{x <= i} d'^2 (P2[ch][0] = 0) and, for
-// 'full', P1 of d' and the centred data.
+// its offset -> P2[ch][i + 1] = sum_{x <= i} d'^2 in units (P2[ch][0] = 0)
+// and, for 'full', P1 of d' and the centred data.
 __global__ void prefix_write_kernel(const float *__restrict__ data, int N, const float *__restrict__ mu,
-                                    const float2 *__restrict__ bs2, const float2 *__restrict__ bs1,
-                                    int nblk, float2 *__restrict__ pre2f, float2 *__restrict__ pre1f,
+                                    const float *__restrict__ unit, const long long *__restrict__ bs2,
+                                    const float2 *__restrict__ bs1, int nblk,
+                                    long long *__restrict__ pre2q, float2 *__restrict__ pre1f,
                                     float *__restrict__ dcen)
 {
-    __shared__ float2 part2[32], part1[32];
+    __shared__ long long part2[32];
+    __shared__ float2 part1[32];
     const int ch = blockIdx.y, blk = blockIdx.x;
-    const float m = mu ? mu[ch] : 0.0f;
+    const float m = mu ? mu[ch] : 0.0f, inv_unit = 1.0f / unit[ch];
     const float *src = data + (size_t)ch * N;
     const int i0 = blk * kPrefixBlock;
     constexpr int per = kPrefixBlock / 256;  // 8 consecutive samples per thread
-    float2 v2[per], v1[per];                 // running pairs of this thread
-    float h2 = 0.0f, l2 = 0.0f, h1 = 0.0f, l1 = 0.0f;
+    long long v2[per];                       // running sums of this thread
+    float2 v1[per];
+    long long s2 = 0;
+    float h1 = 0.0f, l1 = 0.0f;
 #pragma unroll
     for (int e = 0; e < per; e++) {
         const int i = i0 + threadIdx.x * per + e;
@@ -278,51 +334,55 @@ __global__ void prefix_write_kernel(const float *__restrict__ data, int N, const
             if (dcen)
                 dcen[(size_t)ch * N + i] = v;
         }
-        const float sq = v * v;
-        pair_add(h2, l2, sq, fmaf(v, v, -sq));
+        s2 += fixed_square(v, inv_unit);
         pair_add(h1, l1, v, 0.0f);
-        v2[e] = make_float2(h2, l2);
+        v2[e] = s2;
         v1[e] = make_float2(h1, l1);
     }
     // inclusive warp scan of the thread totals, then the exclusive value of this thread
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    float x2 = h2, y2 = l2, x1 = h1, y1 = l1;
+    long long x2 = s2;
+    float x1 = h1, y1 = l1;
     for (int o = 1; o < 32; o <<= 1) {
-        const float a = __shfl_up_sync(0xffffffffu, x2, o), b = __shfl_up_sync(0xffffffffu, y2, o);
+        const long long a = __shfl_up_sync(0xffffffffu, x2, o);
         const float c = __shfl_up_sync(0xffffffffu, x1, o), d = __shfl_up_sync(0xffffffffu, y1, o);
         if (lane >= o) {
-            pair_add(x2, y2, a, b);
+            x2 += a;
             pair_add(x1, y1, c, d);
         }
     }
     if (lane == 31) {
-        part2[wid] = make_float2(x2, y2);
+        part2[wid] = x2;
         part1[wid] = make_float2(x1, y1);
     }
-    float e2h = __shfl_up_sync(0xffffffffu, x2, 1), e2l = __shfl_up_sync(0xffffffffu, y2, 1);
+    long long e2 = __shfl_up_sync(0xffffffffu, x2, 1);
     float e1h = __shfl_up_sync(0xffffffffu, x1, 1), e1l = __shfl_up_sync(0xffffffffu, y1, 1);
-    if (lane == 0)
-        e2h = e2l = e1h = e1l = 0.0f;
+    if (lane == 0) {
+        e2 = 0;
+        e1h = e1l = 0.0f;
+    }
     __syncthreads();
     if (threadIdx.x == 0) {  // warp offsets, starting from the block's offset
-        const float2 o2 = bs2[(size_t)ch * nblk + blk], o1 = bs1[(size_t)ch * nblk + blk];
-        float a = o2.x, b = o2.y, c = o1.x, d = o1.y;
+        long long a = bs2[(size_t)ch * nblk + blk];
+        const float2 o1 = bs1[(size_t)ch * nblk + blk];
+        float c = o1.x, d = o1.y;
         for (int k = 0; k < (int)(blockDim.x >> 5); k++) {
-            const float2 p = part2[k], q = part1[k];
-            part2[k] = make_float2(a, b);
+            const long long p = part2[k];
+            const float2 q = part1[k];
+            part2[k] = a;
             part1[k] = make_float2(c, d);
-            pair_add(a, b, p.x, p.y);
+            a += p;
             pair_add(c, d, q.x, q.y);
         }
     }
     __syncthreads();
-    float oh2 = part2[wid].x, ol2 = part2[wid].y, oh1 = part1[wid].x, ol1 = part1[wid].y;
-    pair_add(oh2, ol2, e2h, e2l);
+    const long long o2 = part2[wid] + e2;
+    float oh1 = part1[wid].x, ol1 = part1[wid].y;
     pair_add(oh1, ol1, e1h, e1l);
-    float2 *p2 = pre2f + (size_t)ch * (N + 1);
+    long long *p2 = pre2q + (size_t)ch * (N + 1);
     float2 *p1 = pre1f ? pre1f + (size_t)ch * (N + 1) : nullptr;
     if (blk == 0 && threadIdx.x == 0) {
-        p2[0] = make_float2(0.0f, 0.0f);
+        p2[0] = 0;
         if (p1)
             p1[0] = make_float2(0.0f, 0.0f);
     }
@@ -330,9 +390,7 @@ __global__ void prefix_write_kernel(const float *__restrict__ data, int N, const
     for (int e = 0; e < per; e++) {
         const int i = i0 + threadIdx.x * per + e;
         if (i < N) {
-            float a = oh2, b = ol2;
-            pair_add(a, b, v2[e].x, v2[e].y);
-            p2[i + 1] = pair_normalise(a, b);
+            p2[i + 1] = o2 + v2[e];
             if (p1) {
                 float c = oh1, d = ol1;
                 pair_add(c, d, v1[e].x, v1[e].y);
@@ -418,19 +476,21 @@ static int variable_device(const VArgs &a, int L, cudaStream_t s, float *host_ou
     Scratch ws(s);
     int *k_lo;
     float *zweight, *consts, *tmask, *tsum = nullptr, *mu = nullptr, *dcen = nullptr;
-    float2 *bs2, *bs1;
-    float2 *pre2f, *pre1f = nullptr;
+    long long *bs2, *pre2q;
+    float2 *bs1, *pre1f = nullptr;
+    float *unit;
     const int nblk = (N + kPrefixBlock - 1) / kPrefixBlock;
     if ((rc = ws.get(&k_lo, 2 * (size_t)T, "template ranges")) ||
         (rc = ws.get(&zweight, (size_t)T * SC, "Fisher-z weights")) ||
         (rc = ws.get(&consts, 3 * (size_t)T, "transform constants")) ||
         (rc = ws.get(&tmask, (size_t)T * SC * L, "masked templates")) ||
-        (rc = ws.get(&pre2f, (size_t)SC * (N + 1), "prefix sums")) ||
-        (rc = ws.get(&bs2, 2 * (size_t)SC * nblk, "block sums")))
+        (rc = ws.get(&pre2q, (size_t)SC * (N + 1), "running sums of d^2")) ||
+        (rc = ws.get(&unit, (size_t)SC, "fixed-point units")) ||
+        (rc = ws.get(&bs2, (size_t)SC * nblk, "block sums")) ||
+        (rc = ws.get(&bs1, (size_t)SC * nblk, "block sums")))
         return rc;
-    bs1 = bs2 + (size_t)SC * nblk;
     if (full && ((rc = ws.get(&tsum, (size_t)T * SC, "template sums")) ||
-                 (rc = ws.get(&mu, (size_t)SC, "channel means")) ||
+                 (rc = ws.get(&mu, (size_t)SC, "channel centres")) ||
                  (rc = ws.get(&dcen, (size_t)SC * N, "centred data")) ||
                  (rc = ws.get(&pre1f, (size_t)SC * (N + 1), "prefix sums of d"))))
         return rc;
@@ -444,11 +504,13 @@ static int variable_device(const VArgs &a, int L, cudaStream_t s, float *host_ou
     vp_scale_kernel<<<1, 256, 0, s>>>(a.w, T, SC, scale);
     vp_template_kernel<<<(unsigned)((size_t)T * SC), 128, 0, s>>>(a.tpl, a.ntap, L, full ? 1 : 0, tmask, tsum);
     if (full)
-        channel_mean_kernel<<<SC, 1024, 0, s>>>(a.data, N, mu);
-    prefix_block_kernel<<<dim3(nblk, SC), 256, 0, s>>>(a.data, N, mu, bs2, bs1, nblk);
+        channel_centre_kernel<<<SC, 1024, 0, s>>>(a.data, N, mu);
+    channel_unit_kernel<<<SC, 1024, 0, s>>>(a.data, N, mu, unit);
+    prefix_block_kernel<<<dim3(nblk, SC), 256, 0, s>>>(a.data, N, mu, unit, bs2, bs1, nblk);
     prefix_offsets_kernel<<<(SC + 127) / 128, 128, 0, s>>>(bs2, bs1, nblk, SC);
-    prefix_write_kernel<<<dim3(nblk, SC), 256, 0, s>>>(a.data, N, mu, bs2, bs1, nblk, pre2f, pre1f, dcen);
-    count_launch(full ? 8 : 7);
+    prefix_write_kernel<<<dim3(nblk, SC), 256, 0, s>>>(a.data, N, mu, unit, bs2, bs1, nblk, pre2q,
+                                                        pre1f, dcen);
+    count_launch(full ? 9 : 8);
     if ((rc = check_launch("variable-length preprocessing")))
         return rc;
 
@@ -472,11 +534,15 @@ static int variable_device(const VArgs &a, int L, cudaStream_t s, float *host_ou
     P.normalize = a.normalize;
     P.network_sum = 1;
     P.ntap = a.ntap;
-    P.pre2f = pre2f;
+    P.pre2q = pre2q;
+    P.unit2 = unit;
     P.pre1f = pre1f;
     P.zweight = zweight;
     P.vp_norm = P.vp_bias = P.vp_scale = nullptr;
-    const int precision = FMF_FLAG_PRECISION_OF(a.flags);
+    int precision = FMF_FLAG_PRECISION_OF(a.flags);
+    if (precision == FMF_PREC_AUTO && (rc = choose_auto_precision(P, ws, s, &precision)))
+        return rc;
+    set_last_precision(precision);
     const size_t row_bytes = a.n_corr * sizeof(float);
     const int n_chunks = (!host_out || (size_t)T * row_bytes < ((size_t)64 << 20)) ? 1 : (T < 8 ? T : 8);
     int bounds[9];
@@ -547,6 +613,7 @@ static int variable_device(const VArgs &a, int L, cudaStream_t s, float *host_ou
         const int t0 = bounds[c], nt = bounds[c + 1] - bounds[c];
         if (nt <= 0)
             continue;
+        populate_host(host_out + (size_t)t0 * a.n_corr, (size_t)nt * row_bytes);  // while kernels run
         if ((e = cudaStreamWaitEvent(cs.s2, cs.ev[c], 0)) != cudaSuccess ||
             (e = cudaMemcpyAsync(host_out + (size_t)t0 * a.n_corr, a.out + (size_t)t0 * a.n_corr,
                                  (size_t)nt * row_bytes, cudaMemcpyDeviceToHost, cs.s2)) != cudaSuccess)
@@ -572,9 +639,7 @@ static int variable_entry(const VArgs &a, void *stream)
         return set_error(FMF_ERR_ARG, "sizes exceed the 32-bit index range of this build");
     if (a.normalize != 0 && a.normalize != 1)
         return set_error(FMF_ERR_ARG, "normalize must be 0 or 1");
-    const int precision = FMF_FLAG_PRECISION_OF(a.flags);
-    if (precision != FMF_PREC_FP32 && precision != FMF_PREC_SPLIT_BF16 && precision != FMF_PREC_BF16)
-        return set_error(FMF_ERR_ARG, "unknown precision %d", precision);
+    // FMF_FLAG_PRECISION is two bits: every value is a precision (FMF_PREC_AUTO included)
     if (a.flags & FMF_FLAG_DEVICE_POINTERS) {  // read in place: 4-byte elements
         const void *ptrs[7] = {a.tpl, a.sst, a.mo, a.data, a.w, a.ntap, a.out};
         for (const void *p : ptrs)
@@ -642,7 +707,7 @@ static int variable_entry(const VArgs &a, void *stream)
     cudaError_t e = cudaStreamSynchronize(s);
     if (e != cudaSuccess)
         return set_error(FMF_ERR_CUDA, "variable-length search: %s", cudaGetErrorString(e));
-    return precision != FMF_PREC_FP32 ? collect_device_errors() : FMF_OK;
+    return fmf_last_precision() != FMF_PREC_FP32 ? collect_device_errors() : FMF_OK;  // the form that ran
 }
 
 }  // namespace fmf

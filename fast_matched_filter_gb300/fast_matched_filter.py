@@ -11,7 +11,9 @@ library is missing (fast_matched_filter.py:164-177).
 
 One keyword is added: ``precision`` -- 'fp32' (plain FP32 CUDA-core form,
 the default and the drop-in), 'split_bf16' (tensor cores, bf16 hi+lo with
-three products) or 'bf16' (single bf16 product).
+three products), 'auto' (split_bf16 where its error model puts the search's
+largest error at or below 1e-5, else fp32; ``last_precision()`` tells which)
+or 'bf16' (single bf16 product).
 
 ``matched_filter_device`` runs the same computation on arrays already
 resident on the GPU (torch CUDA tensors), asynchronously on a stream.
@@ -170,12 +172,14 @@ def prepare(templates, moveouts, weights, data, step, normalize="short", energie
         sst = None
     else:
         sst = np.ascontiguousarray(np.sum(templates ** 2, axis=-1).flatten(), dtype=np.float32)
+    # flat C-order buffers, as the reference's .flatten() makes them, but views
+    # (no copy) of inputs that are already C-contiguous in the right dtype
     return dict(
-        templates=np.ascontiguousarray(templates.flatten(), dtype=np.float32),
+        templates=np.ascontiguousarray(templates, dtype=np.float32).reshape(-1),
         sst=sst,
-        moveouts=np.ascontiguousarray(moveouts.flatten(), dtype=np.int32),
-        weights=np.ascontiguousarray(weights.flatten(), dtype=np.float32),
-        data=np.ascontiguousarray(data.flatten(), dtype=np.float32),
+        moveouts=np.ascontiguousarray(moveouts, dtype=np.int32).reshape(-1),
+        weights=np.ascontiguousarray(weights, dtype=np.float32).reshape(-1),
+        data=np.ascontiguousarray(data, dtype=np.float32).reshape(-1),
         T=T, S=S, C=C, L=int(L), N=int(N), step=step, n_corr=n_corr,
         normalize=1 if normalize == "full" else 0)
 
@@ -203,7 +207,8 @@ def matched_filter(templates, moveouts, weights, data, step,
         the reference's CPU libraries and are reported as not loaded.
     normalize : 'short' or 'full' (window mean removed).
     network_sum : True -> (T, n_corr) weighted sums; False -> (T, n_corr, S, C).
-    precision : 'fp32' | 'split_bf16' | 'bf16' (numerator arithmetic).
+    precision : 'fp32' | 'split_bf16' | 'auto' | 'bf16' (numerator arithmetic;
+        'auto' picks split_bf16 or fp32 per call, see ``last_precision``).
     out : optional writable, C-contiguous float32 array of the output's shape;
         every element is written and ``out`` is returned.  Reusing one array
         (or a page-locked one) across calls saves allocating and faulting in
@@ -258,11 +263,19 @@ def matched_filter(templates, moveouts, weights, data, step,
     return cc if out is None else out
 
 
+def last_precision():
+    """The numerator precision ('fp32', 'split_bf16' or 'bf16') of the last
+    search this thread ran; with precision='auto', the one chosen."""
+    return _lib.PRECISION_NAMES.get(_require_lib().fmf_last_precision())
+
+
 def _output_array(out, shape):
-    """The flat float32 output: a new zeroed array, or a view of ``out``
-    after checking that the library may write it in place."""
+    """The flat float32 output: a new array (the library writes every element,
+    so it is not zeroed first, and maps its pages on several threads while the
+    GPU computes), or a view of ``out`` after checking that the library may
+    write it in place."""
     if out is None:
-        return np.zeros(int(np.prod(shape)), dtype=np.float32)
+        return np.empty(int(np.prod(shape)), dtype=np.float32)
     if not (isinstance(out, np.ndarray) and out.dtype == np.float32 and out.flags.c_contiguous
             and out.flags.writeable and out.shape == tuple(shape)):
         raise ValueError("out must be a writable C-contiguous float32 array of shape %s"

@@ -54,6 +54,16 @@ extern "C" {
 #define FMF_PREC_FP32 0       /* plain FP32 CUDA-core form */
 #define FMF_PREC_SPLIT_BF16 1 /* tensor cores, bf16 hi+lo, 3 products, FP32 accumulate */
 #define FMF_PREC_BF16 2       /* tensor cores, single bf16 product (loss demonstration) */
+/* FMF_PREC_SPLIT_BF16 where an error model of that form puts the search's
+ * largest error at or below 1e-5 (of max(1, sum |w|) for network sums), else
+ * FMF_PREC_FP32: the model is 4.4e-6 / sqrt(effective taps) per coefficient
+ * (x sqrt(1 + L m^2 / V) for 'full', m and V the window mean and centred
+ * energy), a 2.8e-6 bias, and the Gaussian maximum over the outputs plus a
+ * margin.  The estimate reads the templates, weights and window statistics
+ * on the device and waits for its one-word result (the call synchronizes
+ * `stream` once).  fmf_last_precision() reports the choice.  Not for
+ * batches. */
+#define FMF_PREC_AUTO 3
 
 /* flags of fmf_matched_filter_ex */
 #define FMF_FLAG_DEVICE_POINTERS 1 /* all array arguments are device pointers */
@@ -313,6 +323,17 @@ FMF_API int fmf_eval_atanh(const float *y, float *out, size_t n, void *stream);
  * recording. */
 FMF_API int fmf_timing_begin(void);
 FMF_API int fmf_timing_end(double *prep_ms, double *kernel_ms, int *n_calls);
+/* The same with every class: ms[0] preprocessing, ms[1] correlation kernels,
+ * and for host-pointer calls ms[2] the input copies, ms[3] the result's
+ * copies from the first start to the last end (they overlap later kernels),
+ * ms[4] the part of those copies after the last correlation kernel; the
+ * first n_kinds (at most 5) are written. */
+FMF_API int fmf_timing_end_ex(double *ms, int n_kinds, int *n_calls);
+
+/* The numerator precision (FMF_PREC_FP32, _SPLIT_BF16 or _BF16) the last
+ * search entry point called on this thread used; with FMF_PREC_AUTO, the one
+ * it chose.  -1 before the first search. */
+FMF_API int fmf_last_precision(void);
 
 /* Releases device memory cached by the library on the current device. */
 FMF_API int fmf_release_cache(void);

@@ -104,16 +104,21 @@ def test_precision_flag_matches_header():
         assert _lib.flag_precision(name) == (code & mask) << shift
 
 
-def test_variable_unknown_precision_rejected(lib):
+def test_variable_precision_field_takes_auto(lib):
+    """FMF_FLAG_PRECISION is two bits and each value is a precision; AUTO (3)
+    passes the argument checks (here, without a GPU, the call then fails at
+    its first CUDA call, never on the precision)."""
     args, keep = _args()
     ex = [a if not hasattr(a, "contents") else ct.cast(a, ct.c_void_p).value for a in args]
     nt = np.full((2, 2, 3), 16, np.int32)
     # (templates, sst, moveouts, data, weights, step, n_samples_template, N, T, S, C, n_corr, cc,
     #  normalize, flags, stream)
     st = lib.fmf_matched_filter_variable_ex(ex[0], ex[1], ex[2], ex[3], ex[4], 1, nt.ctypes.data,
-                                            200, 2, 2, 3, 185, ex[12], 0, 3 << 24, None)
-    assert st == _lib.FMF_ERR_ARG
-    assert "precision" in _lib.last_error(lib)[1]
+                                            200, 2, 2, 3, 185, ex[12], 0,
+                                            _lib.flag_precision("auto"), None)
+    assert st != _lib.FMF_ERR_ARG
+    assert "precision" not in _lib.last_error(lib)[1]
+    assert _lib.PRECISIONS["auto"] == 3 and _lib.flag_precision("auto") == 3 << 24
 
 
 def test_python_layer_raises_on_status(lib):
