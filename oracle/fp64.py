@@ -92,3 +92,62 @@ def fp64_matched_filter(templates, moveouts, weights, data, step,
     if not network_sum:
         out = out.reshape(len(tix), K, S, C)
     return out
+
+
+def fp64_matched_filter_variable(templates, n_samples_template, moveouts, weights, data, step,
+                                 normalize="short", k_range=None, chunk=16384):
+    """FP64 evaluation of the per-channel-length search (the reference's
+    arch='variable_precise', matched_filter.c:321-412, 569-606): channel ch of
+    template t uses its first n[t, ch] taps; per output the Fisher-z network
+    sum sum_ch atanh(cc_ch - 10 eps) * z_ch with z_ch = sqrt(n - 3) * w_ch,
+    then (tanh(sum / sum_ch z_ch) + n_used * 10 eps) * scale[t], where scale[t]
+    is the running sum of the weights of templates 0..t (never reset in the
+    reference, matched_filter.c:329,365).  Valid outputs: start <= k*step <
+    N - L - max_mo - step (matched_filter.c:381-382), L the longest channel;
+    the transform also maps the zeros outside that range.  cc uses the
+    'precise' threshold sqrt(sst * ssd) > 1e-6 (matched_filter.c:650-652);
+    sst is the raw sum of the channel's own taps squared.  Returns float64
+    (T, K) for the outputs of k_range (default all n_corr)."""
+    eps = float(np.finfo(np.float32).eps)
+    templates = np.asarray(templates, dtype=np.float32)
+    T, S, C, L = templates.shape
+    N = data.shape[-1]
+    nch = S * C
+    n_corr = int((N - L) / step + 1)
+    k0, k1 = (0, n_corr) if k_range is None else k_range
+    tp = templates.reshape(T, nch, L).astype(np.float64)
+    nt = np.asarray(n_samples_template).reshape(T, nch).astype(np.int64)
+    mo = np.asarray(moveouts).reshape(T, nch).astype(np.int64)
+    w = np.asarray(weights, dtype=np.float32).reshape(T, nch).astype(np.float64)
+    d = np.asarray(data, dtype=np.float32).reshape(nch, N).astype(np.float64)
+    out = np.zeros((T, k1 - k0))
+    scale = np.cumsum(w.sum(axis=1))
+    for t in range(T):
+        z = np.sqrt(nt[t] - 3.0) * w[t]
+        used = int(np.count_nonzero(w[t]))
+        lo, hi = min(0, int(mo[t].min())), max(0, int(mo[t].max()))
+        start = int(np.ceil(abs(lo) / float(step))) * step
+        stop = N - L - hi - step
+        a = max(k0, -(-start // step))
+        b = min(k1, -(-stop // step) if stop > start else a)
+        acc = np.zeros(k1 - k0)
+        for c0 in range(a, b, chunk):
+            c1 = min(b, c0 + chunk)
+            part = np.zeros(c1 - c0)
+            for ch in range(nch):
+                if w[t, ch] == 0.0:
+                    continue
+                n = int(nt[t, ch])
+                x = tp[t, ch, :n]
+                first = c0 * step + mo[t, ch]
+                last = (c1 - 1) * step + mo[t, ch]
+                win = sliding_window_view(d[ch, first:last + n], n)[::step]
+                if normalize == "full":
+                    win = win - win.mean(axis=1)[:, None]
+                num = win @ x
+                den = np.sqrt(np.sum(x * x) * np.sum(win * win, axis=1))
+                cc = np.where(den > THRESHOLD, num / np.where(den > THRESHOLD, den, 1.0), 0.0)
+                part += np.arctanh(cc - 10 * eps) * z[ch]
+            acc[c0 - k0:c1 - k0] = part
+        out[t] = (np.tanh(acc / z.sum()) + used * eps * 10) * scale[t]
+    return out

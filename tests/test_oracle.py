@@ -55,6 +55,21 @@ def test_oracle_variable_matches_golden_bit_exact(oracle_built, name):
     assert np.array_equal(got, expected.reshape(got.shape))
 
 
+@pytest.mark.parametrize("name", golden_names_variable())
+def test_fp64_variable_close_to_golden(name):
+    """The FP64 per-channel-length evaluation against the reference library's
+    own outputs, relative to each row's output scale."""
+    from oracle import fp64
+    inputs, opts, expected = load_golden(name)
+    tp, nt, mo, w, d = variable_inputs(inputs)
+    got = fp64.fp64_matched_filter_variable(tp, nt, mo, w, d, inputs["step"], opts["normalize"])
+    exp = expected.reshape(got.shape).astype(np.float64)
+    scale = np.cumsum(w.reshape(w.shape[0], -1).sum(axis=1))[:, None]
+    assert np.array_equal(np.isnan(got), np.isnan(exp))
+    ok = ~np.isnan(exp)
+    assert (np.abs(got - exp) / scale)[ok].max() < 2e-6
+
+
 def test_golden_fixtures_cover_the_reference_options():
     names = golden_names()
     assert len(names) >= 10
