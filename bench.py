@@ -564,21 +564,32 @@ def run_frontend(cfg, precision, args):
     on the workload's numpy arrays (pageable host memory, a fresh numpy output
     per call, check_zeros='first' as the reference's default), wall clock per
     call after one untimed call."""
+    import ctypes as ct
     import torch
     import fast_matched_filter_gb300 as fmf
+    from fast_matched_filter_gb300 import _lib
+    lib = _lib.load()
     secs, got = [], None
+    ms = (ct.c_double * 5)()
     for i in range(1 + args.steps):
         got = None  # free the previous output first
         torch.cuda.synchronize()
+        if i == 1:
+            lib.fmf_timing_begin()
         t = time.perf_counter()
         got = fmf.matched_filter(cfg["templates"], cfg["moveouts"], cfg["weights"], cfg["data"],
                                  cfg["step"], arch="gpu", check_zeros="first",
                                  normalize=cfg["normalize"], network_sum=cfg["network_sum"],
                                  precision=precision)
         secs.append(time.perf_counter() - t)
+    lib.fmf_timing_end_ex(ms, 5, None)
     med = float(np.median(secs[1:]))
+    n = max(1, args.steps)
+    parts = {k: ms[i] / n for i, k in enumerate(("preprocessing_ms", "kernel_ms", "input_copies_ms",
+                                                 "output_copies_ms", "output_tail_ms"))}
     return {"value": cfg["macs"] / med / 1e12, "unit": UNIT, "seconds": secs[1:],
             "first_call_s": secs[0], "output_shape": list(got.shape),
+            "breakdown_per_call": parts,
             "api": "fmf.matched_filter(..., arch='gpu') on numpy arrays (pageable host memory)"}
 
 

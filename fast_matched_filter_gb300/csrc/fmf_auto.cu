@@ -22,6 +22,18 @@
 // products are of the centred data d - c, whose window mean m adds to every
 // product's size: D_ch = 1 + max over windows of L m^2 / V (V the window's
 // centred energy), sampled every kAutoStride windows.
+//
+// Per-channel lengths sum atanh(cc_ch) * z_ch (z_ch = sqrt(n - 3) w_ch) and
+// map the sum through tanh (matched_filter.c:596-601, 405-408): an error in
+// cc_ch grows by 1 / (1 - cc_ch^2) there, so each channel's s_ch is scaled by
+//   A_ch = max(M^(2 / (n - 1)), 1 / (1 - 0.9^2))
+// -- the first the amplification at the largest |cc| that n-tap windows of
+// noise reach among M channel windows (P(|cc| > c) ~ (1 - c^2)^((n-1)/2)),
+// the second at a detection of |cc| = 0.9 -- and the estimate is
+//   est = k * sqrt(sum_ch (z_ch A_ch s_ch)^2) / sum_ch |z_ch|
+// (the tanh has slope at most 1; the output scale is the weight sum).
+// Channels of 4 taps or fewer always run in FP32.  The bound holds while
+// every channel's |cc| stays at or below max(0.9, the noise maximum).
 #include <cmath>
 #include <cstring>
 
@@ -33,6 +45,7 @@ constexpr float kSplitRms = 4.4e-6f;   // RMS relative error of one split-bf16 p
 constexpr float kSplitBias = 2.8e-6f;  // bias per unit |cc| at a power-of-two copy
 constexpr float kAutoTol = 1e-5f;
 constexpr int kAutoStride = 7;
+constexpr float kFisherAmp = 1.0f / (1.0f - 0.9f * 0.9f);  // 1 / (1 - cc^2) at |cc| = 0.9
 
 // grid = SC, 256 threads: D_ch - 1 of 'full' from the (centred energy, mean)
 // window statistics of the fixed-length path.
@@ -92,11 +105,12 @@ __global__ void auto_dc_prefix_kernel(const long long *__restrict__ pre2q,
 
 // grid = T, 256 threads (8 warps, one channel per warp at a time): the
 // estimate of template t divided by its bar, as float bits into *worst
-// (atomicMax: the ratios are non-negative).
+// (atomicMax: the ratios are non-negative).  ntap non-null: the Fisher-z
+// network sum of per-channel lengths, ln_m = ln(channel windows).
 __global__ void auto_template_kernel(const float *__restrict__ tpl, const float *__restrict__ w,
                                      const int *__restrict__ ntap, int SC, int L,
                                      const float *__restrict__ dc, int network_sum, float k,
-                                     unsigned *__restrict__ worst)
+                                     float ln_m, unsigned *__restrict__ worst)
 {
     __shared__ float sw[8], sv[8], smax[8];
     const int t = blockIdx.x, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -118,13 +132,22 @@ __global__ void auto_template_kernel(const float *__restrict__ tpl, const float 
             s2 += __shfl_xor_sync(0xffffffffu, s2, o);
             s4 += __shfl_xor_sync(0xffffffffu, s4, o);
         }
-        if (lane == 0 && s4 > 0.0f) {
+        if (lane == 0 && ntap && n <= 4) {
+            ch_max = INFINITY;  // Fisher z of a few taps: FP32
+        } else if (lane == 0 && s4 > 0.0f) {
             const float leff = s2 * s2 / s4;
             const float d = 1.0f + (dc ? dc[ch] : 0.0f);
             const float s = kSplitRms * sqrtf(d / leff);  // per-channel standard deviation
-            sum_w += fabsf(wc);
-            var += wc * wc * s * s;
-            ch_max = fmaxf(ch_max, (kSplitBias + k * s) / kAutoTol);
+            if (ntap) {  // Fisher z: weight z = sqrt(n - 3) w, amplification A
+                const float z = sqrtf((float)(n - 3)) * wc;
+                const float amp = fmaxf(expf(2.0f * ln_m / (float)(n - 1)), kFisherAmp);
+                sum_w += fabsf(z);
+                var += (z * amp * s) * (z * amp * s);
+            } else {
+                sum_w += fabsf(wc);
+                var += wc * wc * s * s;
+                ch_max = fmaxf(ch_max, (kSplitBias + k * s) / kAutoTol);
+            }
         }
     }
     if (lane == 0) {
@@ -140,9 +163,11 @@ __global__ void auto_template_kernel(const float *__restrict__ tpl, const float 
             V += sv[i];
             M = fmaxf(M, smax[i]);
         }
-        const float ratio = network_sum
-                                ? (kSplitBias * W + k * sqrtf(V)) / (kAutoTol * fmaxf(1.0f, W))
-                                : M;
+        float ratio = M;
+        if (ntap)
+            ratio = M > 0.0f ? M : (W > 0.0f ? k * sqrtf(V) / (kAutoTol * W) : 0.0f);
+        else if (network_sum)
+            ratio = (kSplitBias * W + k * sqrtf(V)) / (kAutoTol * fmaxf(1.0f, W));
         atomicMax(worst, __float_as_uint(ratio));
     }
 }
@@ -169,11 +194,13 @@ int choose_auto_precision(const Problem &P, Scratch &ws, cudaStream_t s, int *pr
     }
     const double outputs = (double)P.T * P.n_corr * (P.network_sum ? 1 : P.SC);
     const float k = (float)(std::sqrt(2.0 * std::log(outputs > 2.0 ? outputs : 2.0)) + 3.0);
+    const double windows = (double)P.T * P.n_corr * P.SC;
+    const float ln_m = (float)std::log(windows > 2.0 ? windows : 2.0);
     for (int t0 = 0; t0 < P.T; t0 += 65535) {
         const int nt = P.T - t0 < 65535 ? P.T - t0 : 65535;
         const size_t o = (size_t)t0 * P.SC;
         auto_template_kernel<<<nt, 256, 0, s>>>(P.tpl + o * P.L, P.w + o, P.ntap ? P.ntap + o : nullptr,
-                                                P.SC, P.L, dc, P.network_sum, k, worst);
+                                                P.SC, P.L, dc, P.network_sum, k, ln_m, worst);
         count_launch();
     }
     unsigned bits = 0;
