@@ -2,7 +2,7 @@
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
                     [--workload config4|config1|config2|config0|config3|variable|variable_full]
-                    [--precision ...] [--templates T] [--samples N] [--frontend]
+                    [--precision ...] [--templates T] [--samples N] [--no-frontend]
 
 One *step* is one complete search of the workload (every template against
 every channel and output index: preprocessing kernels + correlation
@@ -16,7 +16,7 @@ kernel).  Metric: template*lag*channel multiply-accumulates per second
             pinned host buffers: H2D of every input and D2H of the whole
             output inside each timed step.
   roofline  the correlation kernel, event-timed inside the timed region.
-  frontend_numpy  (--frontend) the drop-in Python call on the workload's
+  frontend_numpy  the drop-in Python call on the workload's
             numpy arrays (pageable host memory), wall clock per call.
   cpu_baseline  the oracle's C port of the reference CPU algorithm (OpenMP,
             all host cores) on a bounded sample of the same workload.
@@ -70,8 +70,8 @@ def parse_args(argv=None):
                    help="skip the FP64 error report on a subset")
     p.add_argument("--no-detect", action="store_true",
                    help="skip the detection leg (threshold + peaks on the search output)")
-    p.add_argument("--frontend", action="store_true",
-                   help="also time the drop-in Python call on numpy (pageable) arrays")
+    p.add_argument("--no-frontend", action="store_true",
+                   help="skip timing the drop-in Python call on numpy (pageable) arrays")
     p.add_argument("--templates", type=int, default=0, help="override T (smaller runs)")
     p.add_argument("--samples", type=int, default=0, help="override N (smaller runs)")
     return p.parse_args(argv)
@@ -410,7 +410,7 @@ def run_ours(args):
             line["e2e_search_detect"] = run_e2e_detect(cfg, precision, args, world, lib)
     del out
     torch.cuda.empty_cache()
-    if args.frontend and world == 1:
+    if not args.no_frontend and world == 1:
         line["frontend_numpy"] = run_frontend(cfg, precision, args)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(cfg)
@@ -617,27 +617,28 @@ def run_e2e(cfg, dev_out, precision, args, world, lib):
         call()
     barrier(world)
     n = max(5, args.steps)
-    per_step = []
-    lib.fmf_timing_begin()
-    t0 = time.perf_counter()
-    for _ in range(n):
+    per_step, step_parts = [], []
+    ms = (ct.c_double * 5)()
+    for _ in range(n):  # each step is one call; its copy/kernel spans are read after it
+        lib.fmf_timing_begin()
         t = time.perf_counter()
         call()
         per_step.append(time.perf_counter() - t)
-    secs = dist_max(time.perf_counter() - t0, world)
-    ms = (ct.c_double * 5)()
-    calls = ct.c_int()
-    lib.fmf_timing_end_ex(ms, 5, ct.byref(calls))
+        lib.fmf_timing_end_ex(ms, 5, None)
+        step_parts.append(list(ms))
+    secs = dist_max(sum(per_step), world)
     h2d = sum(int(v.numel() * v.element_size()) for v in pinned.values())
     d2h = int(host_out.numel() * 4)
     wall_ms = 1e3 * secs / n
-    parts = {k: ms[i] / n for i, k in enumerate(("preprocessing_ms", "kernel_ms", "input_copies_ms",
-                                                 "output_copies_ms", "output_tail_ms"))}
+    parts = {k: sum(p[i] for p in step_parts) / n
+             for i, k in enumerate(("preprocessing_ms", "kernel_ms", "input_copies_ms",
+                                    "output_copies_ms", "output_tail_ms"))}
     parts["host_and_other_ms"] = wall_ms - (parts["input_copies_ms"] + parts["preprocessing_ms"]
                                             + parts["kernel_ms"] + parts["output_tail_ms"])
     return {"value": cfg["macs"] * n * world / secs / 1e12, "unit": UNIT,
             "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "steps": n,
             "ms_per_step": wall_ms, "step_ms": [round(1e3 * x, 2) for x in per_step],
+            "step_input_copies_ms": [round(p[2], 2) for p in step_parts],
             "breakdown_per_step": parts,
             "h2d_gbs": h2d / (parts["input_copies_ms"] / 1e3) / 1e9 if parts["input_copies_ms"] else None,
             "d2h_window_gbs": d2h / (parts["output_copies_ms"] / 1e3) / 1e9

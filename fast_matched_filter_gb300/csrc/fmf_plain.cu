@@ -169,7 +169,7 @@ plain_kernel(const Problem P, const PlainGeom g)
     // templates fastest: the CTAs running at any time share a few tiles, so
     // their data windows and window statistics are read from L2
     const int t = (int)(blockIdx.x % (unsigned)P.T);
-    const long long k0 = (long long)(blockIdx.x / (unsigned)P.T) * PL_TILE;
+    const int k0 = (int)(blockIdx.x / (unsigned)P.T) * PL_TILE;  // < n_corr <= INT_MAX
     const int klo = P.k_lo[t], khi = P.k_hi[t];
     const int tid = threadIdx.x;
     const float *w = P.w + (size_t)t * P.SC;
@@ -224,9 +224,9 @@ plain_kernel(const Problem P, const PlainGeom g)
                 const float2 *p1 = FULL ? P.pre1f + (size_t)ch * (P.N + 1) : nullptr;
 #pragma unroll
                 for (int r = 0; r < PL_R; r++) {
-                    long long k = k0 + tid * PL_R + r;
+                    const int k = k0 + tid * PL_R + r;
                     if (k >= klo && k < khi) {
-                        const long long u = k * P.step + mo[ch];
+                        const int u = k * P.step + mo[ch];  // a window inside [0, N - n]
                         float num = acc[r], ssd;
                         if (FULL) {
                             float mean;
@@ -252,9 +252,9 @@ plain_kernel(const Problem P, const PlainGeom g)
                 const float2 *sem = reinterpret_cast<const float2 *>(P.stat_e) + (size_t)ch * P.N;
 #pragma unroll
                 for (int r = 0; r < PL_R; r++) {
-                    long long k = k0 + tid * PL_R + r;
+                    const int k = k0 + tid * PL_R + r;
                     if (k >= klo && k < khi) {
-                        long long u = k * P.step + mo[ch];
+                        const int u = k * P.step + mo[ch];  // a window inside [0, N - L]
                         float num = acc[r], energy;
                         if (FULL) {  // (centred energy, mean) pairs
                             const float2 em = sem[u];
@@ -264,7 +264,7 @@ plain_kernel(const Problem P, const PlainGeom g)
                             energy = se[u];
                         }
                         float den = sst * energy;
-                        float cc = den > kThreshold ? num / sqrtf(den) : 0.0f;
+                        float cc = den > kThreshold ? num * rsqrtf(den) : 0.0f;
                         if (P.network_sum)
                             net[r * PL_THREADS + tid] = fmaf(cc, wc, net[r * PL_THREADS + tid]);
                         else
@@ -283,7 +283,7 @@ plain_kernel(const Problem P, const PlainGeom g)
         float *o = P.out + (size_t)t * P.n_corr;
 #pragma unroll
         for (int r = 0; r < PL_R; r++) {
-            long long k = k0 + tid * PL_R + r;
+            const int k = k0 + tid * PL_R + r;
             if (k < P.n_corr)
                 o[k] = net[r * PL_THREADS + tid];
         }
