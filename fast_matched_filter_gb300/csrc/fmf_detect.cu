@@ -31,10 +31,14 @@
 //      match the bits chosen so far) runs over the candidates only; if not --
 //      heavy ties, an adversarial row -- the same radix selection runs over
 //      the whole row.  Rows no longer than the sample are sorted whole.
-// So a call reads the rows three times (median, MAD, peaks) in the usual case.
-// Peaks are gathered into a list per template (capacity kDetCap) and filtered
-// by one thread block per template: a sort by lag, a sort by height, and the
-// greedy distance filter.
+// The MAD pass's read of the row also gathers the local maxima at or above a
+// lower bound of the threshold (from the MAD window: thr = med + n_mad * mad
+// is monotone in mad), so a call reads the rows twice (median, MAD + peaks)
+// in the usual case; rows whose MAD window missed get a peak pass of their
+// own.  Peaks are gathered into a list per template (capacity kDetCap) and
+// filtered by one thread block per template: the candidates below the exact
+// threshold dropped, a sort by lag, a sort by height, and the greedy distance
+// filter.
 //
 // Every launch is stream-ordered and the state lives on the device, so a
 // detection run needs no host round trip and can be captured in a graph.
@@ -65,6 +69,8 @@ struct DetState {
     int rank[2];           // rank still to find inside the chosen bucket
     float med, mad, thr;
     int n_cand;            // local maxima at or above thr (may exceed the capacity)
+    float thr_lo;          // a lower bound of thr known before the MAD pass
+    int peaks_ready;       // 1: the MAD counting pass gathered the local maxima >= thr_lo
     int src;               // kSrcRow / kSrcCand / kSrcDone
     unsigned klo, khi;     // sample window of the keys
     int n_lt, n_in;        // keys below klo, keys inside [klo, khi]
@@ -128,6 +134,8 @@ __global__ void det_init_kernel(DetState *__restrict__ st, int T, int n_corr,
     s.rank[1] = n / 2;
     s.med = s.mad = s.thr = __int_as_float(0x7fc00000);  // NaN until computed
     s.n_cand = 0;
+    s.thr_lo = __int_as_float(0x7fc00000);
+    s.peaks_ready = 0;
     s.src = kSrcRow;
     s.klo = s.khi = 0u;
     s.n_lt = s.n_in = 0;
@@ -276,15 +284,62 @@ det_sample_kernel(const float *__restrict__ cc, size_t ld, DetState *__restrict_
         s.klo = k0;
         s.khi = k1;
         s.src = kSrcCand;
+        if (mode == 1) {
+            // thr = med + n_mad * mad rises with mad (for n_mad >= 0; falls otherwise) and
+            // float rounding keeps that order, so a MAD inside the window [klo, khi] gives
+            // thr >= thr_lo: the counting pass gathers the local maxima >= thr_lo, a
+            // superset of the peaks, and the filter keeps those >= thr
+            const float d = key_value(n_mad >= 0.0f ? k0 : k1);
+            s.thr_lo = __fadd_rn(s.med, __fmul_rn(n_mad, d));
+            s.peaks_ready = 1;
+        }
     }
     st[t] = s;
 }
 
+// A local maximum at row[i] = x (absolute index i in the window [b, e))
+// at or above thr, appended (unordered) to the template's candidate list.
+__device__ __forceinline__ void peak_at(const float *row, long long i, long long b, long long e, float x,
+                                        float thr, DetState *st, int2 *cand, int cap, int t)
+{
+    if (!(x >= thr) || i < b + 1 || i >= e - 1)
+        return;  // a flat top has the value of its rising sample
+    if (!(row[i - 1] < x))
+        return;
+    long long j = i + 1;
+    while (j < e - 1 && row[j] == x)
+        j++;
+    if (row[j] < x) {
+        const int peak = (int)((i + j - 1) >> 1);
+        const int slot = atomicAdd(&st[t].n_cand, 1);
+        if (slot < cap)
+            cand[(size_t)t * cap + slot] = make_int2(peak, __float_as_int(x));
+    }
+}
+
+// The local maxima among the four values at window offsets [o, o + 4) of row
+// t: the rare path of the counting pass (row bounds and threshold re-read
+// from the state, so that the pass keeps only the threshold in registers).
+__device__ __forceinline__ void peaks_of4(const float *cc, size_t ld, DetState *st, int t, long long o,
+                                       float4 v, int2 *pcand, int pcap)
+{
+    const long long b = st[t].begin, e = st[t].end;
+    const float thr_lo = st[t].thr_lo;
+    const float *row = cc + (size_t)t * ld;
+    peak_at(row, b + o, b, e, v.x, thr_lo, st, pcand, pcap, t);
+    peak_at(row, b + o + 1, b, e, v.y, thr_lo, st, pcand, pcap, t);
+    peak_at(row, b + o + 2, b, e, v.z, thr_lo, st, pcand, pcap, t);
+    peak_at(row, b + o + 3, b, e, v.w, thr_lo, st, pcand, pcap, t);
+}
+
 // Step 2: one pass over the row: keys below klo counted, keys inside
-// [klo, khi] appended to the row's candidate list (up to cap).
-__global__ void __launch_bounds__(kDetThreads, 4)  // 32 warps per SM: enough loads in flight
+// [klo, khi] appended to the row's candidate list (up to cap).  In the MAD
+// pass (mode 1) the same read gathers the local maxima at or above thr_lo
+// into the peak list (pcand), so that no third read of the row is needed.
+__global__ void __launch_bounds__(kDetThreads, 3)  // 24 warps per SM: loads in flight, no spills
 det_count_kernel(const float *__restrict__ cc, size_t ld, DetState *__restrict__ st,
-                 unsigned *__restrict__ cand, long long cap, int mode)
+                 unsigned *__restrict__ cand, long long cap, int mode, int2 *__restrict__ pcand,
+                 int pcap)
 {
     const int t = blockIdx.y;
     const int src = st[t].src;
@@ -293,6 +348,8 @@ det_count_kernel(const float *__restrict__ cc, size_t ld, DetState *__restrict__
         return;
     const unsigned klo = st[t].klo, khi = st[t].khi;
     const float med = st[t].med;
+    const bool peaks = mode == 1 && st[t].peaks_ready != 0;
+    const float thr_lo = st[t].thr_lo;
     const float *row = cc + (size_t)t * ld + st[t].begin;
     unsigned *list = cand + (size_t)t * cap;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -342,7 +399,12 @@ det_count_kernel(const float *__restrict__ cc, size_t ld, DetState *__restrict__
         bool ok[kK];
         const long long i = lane < rs.head ? lane : rs.head + 4 * rs.nvec + (lane - rs.head);
         ok[0] = lane < rs.head + rs.tail;
-        key[0] = ok[0] ? sel_key(row[i], mode, med) : 0u;
+        const float x = ok[0] ? row[i] : 0.0f;
+        key[0] = ok[0] ? sel_key(x, mode, med) : 0u;
+        if (peaks && ok[0] && x >= thr_lo) {
+            const long long b = st[t].begin, e = st[t].end;
+            peak_at(cc + (size_t)t * ld, b + i, b, e, x, thr_lo, st, pcand, pcap, t);
+        }
 #pragma unroll
         for (int u = 1; u < kK; u++) {
             ok[u] = false;
@@ -371,6 +433,15 @@ det_count_kernel(const float *__restrict__ cc, size_t ld, DetState *__restrict__
         for (int u = 0; u < 4; u++)
             v[u] = nv[u];
         load4(c + cstride, nv);  // the next step's values are in flight while this one is counted
+        if (peaks) {  // local maxima at or above thr_lo (rare: out of line)
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                const long long q = c * 128 + u * 32 + lane;
+                const float mx = fmaxf(fmaxf(v[u].x, v[u].y), fmaxf(v[u].z, v[u].w));
+                if (q < rs.nvec && mx >= thr_lo)
+                    peaks_of4(cc, ld, st, t, rs.head + 4 * q, v[u], pcand, pcap);
+            }
+        }
 #pragma unroll
         for (int u = 0; u < 4; u++) {
             const bool okv = c * 128 + u * 32 + lane < rs.nvec;
@@ -392,8 +463,10 @@ det_count_kernel(const float *__restrict__ cc, size_t ld, DetState *__restrict__
 }
 
 // Step 3: does the window hold both middle ranks?  Then select among the
-// candidates; else fall back to the whole row.
-__global__ void det_check_kernel(DetState *__restrict__ st, int T, long long cap)
+// candidates; else fall back to the whole row -- and in the MAD pass, leave
+// the peaks to a pass of their own (the gathered superset may miss some, or
+// have overflowed its list).
+__global__ void det_check_kernel(DetState *__restrict__ st, int T, long long cap, int mode, int pcap)
 {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= T || st[t].src != kSrcCand)
@@ -408,6 +481,12 @@ __global__ void det_check_kernel(DetState *__restrict__ st, int T, long long cap
         s.src = kSrcRow;
         s.rank[0] = (int)a;
         s.rank[1] = (int)b;
+        if (mode == 1)
+            s.peaks_ready = 0;
+    }
+    if (mode == 1 && (!s.peaks_ready || s.n_cand > pcap)) {
+        s.peaks_ready = 0;
+        s.n_cand = 0;
     }
     s.prefix[0] = s.prefix[1] = 0u;
     st[t] = s;
@@ -574,27 +653,11 @@ __global__ void det_resolve_kernel(DetState *__restrict__ st, unsigned *__restri
 }
 
 // Local maxima at or above the threshold, appended (unordered) to the
-// template's candidate list.  Grid: (blocks per row, templates).  Samples are
-// read with 16-byte loads; the rare sample at or above the threshold is
-// examined with scalar loads.
-__device__ __forceinline__ void peak_at(const float *row, long long i, long long b, long long e, float x,
-                                        float thr, DetState *st, int2 *cand, int cap, int t)
-{
-    if (!(x >= thr) || i < b + 1 || i >= e - 1)
-        return;  // a flat top has the value of its rising sample
-    if (!(row[i - 1] < x))
-        return;
-    long long j = i + 1;
-    while (j < e - 1 && row[j] == x)
-        j++;
-    if (row[j] < x) {
-        const int peak = (int)((i + j - 1) >> 1);
-        const int slot = atomicAdd(&st[t].n_cand, 1);
-        if (slot < cap)
-            cand[(size_t)t * cap + slot] = make_int2(peak, __float_as_int(x));
-    }
-}
-
+// template's candidate list, for the rows whose MAD pass did not gather them
+// (rows sorted whole by the sample, MAD windows that missed, overflowing
+// supersets).  Grid: (blocks per row, templates).  Samples are read with
+// 16-byte loads; the rare sample at or above the threshold is examined with
+// scalar loads.
 __global__ void __launch_bounds__(kDetThreads)
 det_peaks_kernel(const float *__restrict__ cc, size_t ld, DetState *__restrict__ st,
                  int2 *__restrict__ cand, int cap)
@@ -602,7 +665,7 @@ det_peaks_kernel(const float *__restrict__ cc, size_t ld, DetState *__restrict__
     const int t = blockIdx.y;
     const long long b = st[t].begin, e = st[t].end;
     const float thr = st[t].thr;
-    if (e - b < 3)
+    if (e - b < 3 || st[t].peaks_ready)
         return;
     const float *row = cc + (size_t)t * ld;
     const RowSplit rs = split_row(row + b, e - b);
@@ -672,20 +735,28 @@ det_select_kernel(const DetState *__restrict__ st, const int2 *__restrict__ cand
         if (thr_out)
             thr_out[t] = s.thr;
     }
-    const int m = s.n_cand;
-    if (m > cap) {
+    const int m0 = s.n_cand;
+    if (m0 > cap) {
         if (threadIdx.x == 0)
             count_out[t] = -1;  // capacity exceeded: no peaks reported for this row
         return;
     }
     int P = 1;
-    while (P < m)
+    while (P < m0)
         P <<= 1;
     const int2 *c = cand + (size_t)t * cap;
-    // 1. order by lag (lags are distinct)
-    for (int i = threadIdx.x; i < P; i += blockDim.x)
-        sk[i] = i < m ? ((unsigned long long)(unsigned)c[i].x << 32) | (unsigned)c[i].y : ~0ull;
-    __syncthreads();
+    // 1. the candidates at or above thr (the MAD pass gathers a superset: those at or
+    // above a lower bound of thr), ordered by lag (lags are distinct); the others
+    // sort last
+    int kept = 0;
+    for (int i0 = 0; i0 < P; i0 += blockDim.x) {
+        const int i = i0 + threadIdx.x;
+        const bool ok = i < m0 && __int_as_float(c[i].y) >= s.thr;
+        if (i < P)
+            sk[i] = ok ? ((unsigned long long)(unsigned)c[i].x << 32) | (unsigned)c[i].y : ~0ull;
+        kept += __syncthreads_count(ok);
+    }
+    const int m = kept;
     bitonic_sort(sk, P);
     // 2. order by height, then by lag (position in lag order)
     for (int i = threadIdx.x; i < P; i += blockDim.x) {
@@ -819,8 +890,9 @@ int detect_device(const float *cc, int T, int n_corr, size_t ld, const int *begi
         for (int mode = 0; mode < 2; mode++) {
             det_sample_kernel<<<nt, 1024, kDetSample * sizeof(unsigned), s>>>(rows, ld, st, mode, n_mad,
                                                                                saved);
-            det_count_kernel<<<grid, kDetThreads, 0, s>>>(rows, ld, st, keys, key_cap, mode);
-            det_check_kernel<<<(nt + 127) / 128, 128, 0, s>>>(st, nt, key_cap);
+            det_count_kernel<<<grid, kDetThreads, 0, s>>>(rows, ld, st, keys, key_cap, mode, cand,
+                                                          kDetCap);
+            det_check_kernel<<<(nt + 127) / 128, 128, 0, s>>>(st, nt, key_cap, mode, kDetCap);
             for (int pass = 0; pass < 3; pass++) {
                 det_hist_kernel<<<grid, kDetThreads, 0, s>>>(rows, ld, st, hist, keys, key_cap, pass,
                                                              mode);

@@ -285,15 +285,18 @@ struct StatLayout {
 size_t window_stats_smem(int L, bool full) { return (size_t)StatLayout(L, full).total * sizeof(float); }
 
 // grid = (ceil(N / kStatWindows), SC), kStatThreads threads, dynamic smem =
-// window_stats_smem(L, full).  short: stat_e[ch][u] = sum of d^2 over
-// [u, u + L); full: (centred energy, mean) of d' = d - mu[ch] as float pairs,
-// and the centred data into dcen.  Windows past N - L are not written.
-__global__ void __launch_bounds__(kStatThreads)
+// window_stats_smem(L, FULL).  short: stat_e[ch][u] = sum of d^2 over
+// [u, u + L); FULL: (centred energy, mean) of d' = d - mu[ch] as float pairs,
+// and the centred data into dcen.  Windows past N - L are not written.  One
+// instantiation per mode: the 'short' one keeps no sums of d' in registers,
+// so three blocks share an SM.
+template <bool FULL>
+__global__ void __launch_bounds__(kStatThreads, FULL ? 2 : 3)
 window_stats_kernel(const float *__restrict__ data, int N, int L, const float *__restrict__ mu,
                     float *__restrict__ dcen, float *__restrict__ stat_e)
 {
     extern __shared__ float4 stat_smem[];
-    const bool full = mu != nullptr;
+    constexpr bool full = FULL;
     const StatLayout lay(L, full);
     float *base = reinterpret_cast<float *>(stat_smem);
     float2 *s2 = reinterpret_cast<float2 *>(base + lay.s2);
@@ -310,17 +313,27 @@ window_stats_kernel(const float *__restrict__ data, int N, int L, const float *_
     const int span = stat_span(L), nq = span >> 5;
     const float m = full ? mu[ch] : 0.0f;
     const float *src = data + (size_t)ch * N + c0;
-    for (int i = threadIdx.x; i < span; i += kStatThreads) {
-        float v = 0.0f;
-        if (i < len) {
-            v = src[i] - m;
-            if (full && i < kStatWindows)
-                dcen[(size_t)ch * N + c0 + i] = v;
+    constexpr int kLoads = 4;  // loads in flight per thread before their use
+    for (int i0 = threadIdx.x; i0 < span; i0 += kLoads * kStatThreads) {
+        float x[kLoads];
+#pragma unroll
+        for (int j = 0; j < kLoads; j++) {
+            const int i = i0 + j * kStatThreads;
+            x[j] = i < len ? __ldg(src + i) : 0.0f;
         }
-        const float sq = v * v;
-        s2[stat_pad(i)] = make_float2(sq, fmaf(v, v, -sq));  // v^2 exactly
-        if (full)
-            s1[stat_pad(i)] = v;
+#pragma unroll
+        for (int j = 0; j < kLoads; j++) {
+            const int i = i0 + j * kStatThreads;
+            if (i < span) {
+                const float v = i < len ? x[j] - m : 0.0f;
+                if (full && i < kStatWindows && i < len)
+                    dcen[(size_t)ch * N + c0 + i] = v;
+                const float sq = v * v;
+                s2[stat_pad(i)] = make_float2(sq, fmaf(v, v, -sq));  // v^2 exactly
+                if (full)
+                    s1[stat_pad(i)] = v;
+            }
+        }
     }
     __syncthreads();
     for (int k = threadIdx.x; k < nq; k += kStatThreads) {  // chunk sums
@@ -443,14 +456,16 @@ window_stats_kernel(const float *__restrict__ data, int N, int L, const float *_
 int launch_window_stats(const float *data, int N, int L, int SC, const float *mu, float *dcen,
                         float *stat_e, cudaStream_t s)
 {
-    const size_t smem = window_stats_smem(L, mu != nullptr);
-    cudaError_t e = cudaFuncSetAttribute(window_stats_kernel,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    const bool full = mu != nullptr;
+    const size_t smem = window_stats_smem(L, full);
+    void (*kern)(const float *, int, int, const float *, float *, float *) =
+        full ? window_stats_kernel<true> : window_stats_kernel<false>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess)
         return set_error(FMF_ERR_CUDA, "window statistics shared memory (%zu bytes): %s", smem,
                          cudaGetErrorString(e));
     dim3 grid((N + kStatWindows - 1) / kStatWindows, SC);
-    window_stats_kernel<<<grid, kStatThreads, smem, s>>>(data, N, L, mu, dcen, stat_e);
+    kern<<<grid, kStatThreads, smem, s>>>(data, N, L, mu, dcen, stat_e);
     count_launch();
     return FMF_OK;
 }
