@@ -79,7 +79,31 @@ __device__ __forceinline__ float2 pair_normalise(float h, float l)
     return make_float2(hi, l - (hi - h));
 }
 
-// 'short': sum of d^2 over the window [a, b) from the fixed-point running sums.
+// A non-negative 64-bit integer d < 2^63 as a normalised float pair h + l
+// (about 48 significant bits) with FP32/INT32 operations only: its 23-bit
+// digits become exact floats by the 2^23 magic-number trick, the top two are
+// added by TwoSum and the low one joins the error word.  (Forming the pair with
+// int64 <-> float conversions takes three of them, which run at a fraction of
+// the FP32 rate: the 'full' per-channel-length search ran 95 TMAC/s with them,
+// 124 with this.)
+__device__ __forceinline__ void fixed_pair(long long d, float &h, float &l)
+{
+    const unsigned long long x = d > 0 ? (unsigned long long)d : 0ull;
+    const unsigned lo = (unsigned)x & 0x7fffffu, mid = (unsigned)(x >> 23) & 0x7fffffu;
+    const unsigned top = (unsigned)(x >> 46);  // < 2^17
+    const float magic = 8388608.0f;           // 2^23
+    const float fl = __int_as_float(0x4b000000u | lo) - magic;
+    const float fm = (__int_as_float(0x4b000000u | mid) - magic) * magic;
+    const float ft = (__int_as_float(0x4b000000u | top) - magic) * (magic * magic);
+    float e;
+    const float s = two_diff(ft, -fm, e);  // ft + fm = s + e exactly
+    const float t = e + fl;
+    h = s + t;
+    l = t - (h - s);
+}
+
+// 'short': sum of d^2 over the window [a, b) from the fixed-point running sums
+// (one rounding: the conversion instruction is cheaper here than the split).
 __device__ __forceinline__ float window_energy(long long pa, long long pb, float unit)
 {
     return __ll2float_rn(pb - pa) * unit;
@@ -110,9 +134,9 @@ __device__ __forceinline__ void window_centred_sums(float s2h, float s2l, float 
 __device__ __forceinline__ void window_centred(long long a2, long long b2, float unit, float2 a1,
                                                float2 b1, float nf, float inv_n, float &v, float &mean)
 {
-    const long long d2 = b2 - a2;
-    const float dh = __ll2float_rn(d2);  // an integer value: d2 - dh is exact
-    const float s2h = dh * unit, s2l = __ll2float_rn(d2 - __float2ll_rz(dh)) * unit;
+    float dh, dl;
+    fixed_pair(b2 - a2, dh, dl);
+    const float s2h = dh * unit, s2l = dl * unit;
     float e1;
     const float s1h = two_diff(b1.x, a1.x, e1);
     const float s1l = e1 + (b1.y - a1.y);
