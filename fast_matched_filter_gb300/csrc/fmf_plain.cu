@@ -49,19 +49,32 @@ struct PlainGeom {
     int lq_pad;       // taps per phase, padded to a multiple of PL_U
     int dw;           // data window length (logical floats)
     int data_floats;  // padded data floats
-    int stage_floats; // data + template floats, multiple of 4
+    int stat_off;     // offset of the staged window energies ('short', fixed lengths), else 0
+    int stage_floats; // data + template (+ energies) floats, multiple of 4
     size_t smem;      // dynamic shared memory bytes
 };
 
-inline PlainGeom plain_geom(int L, int step)
+// stage_energies: 'short' with fixed template lengths also stages the tile's
+// window energies (padded like the data, so that 16-byte reads of threads 16
+// outputs apart hit distinct banks)
+inline PlainGeom plain_geom(int L, int step, bool stage_energies)
 {
     PlainGeom g;
     int lq = (L + step - 1) / step;
     g.lq_pad = (lq + PL_U - 1) / PL_U * PL_U;
     g.dw = PL_TILE + g.lq_pad;
     g.data_floats = padx(g.dw) + 4;
+    g.stat_off = 0;
     g.stage_floats = (g.data_floats + g.lq_pad + 3) & ~3;
     g.smem = (size_t)(2 * g.stage_floats + PL_R * PL_THREADS) * sizeof(float);
+    // only while two CTAs still share an SM (228 KB, 1 KB reserved per CTA)
+    const int staged = g.stage_floats + ((padx(PL_TILE) + 3) & ~3);
+    const size_t smem_staged = (size_t)(2 * staged + PL_R * PL_THREADS) * sizeof(float);
+    if (stage_energies && 2 * (smem_staged + 1024) <= 228 * 1024) {
+        g.stat_off = g.stage_floats;
+        g.stage_floats = staged;
+        g.smem = smem_staged;
+    }
     return g;
 }
 
@@ -98,6 +111,18 @@ __device__ __forceinline__ void load_stage(float *buf, const Problem &P, const P
         int j = P.step * q + phi;
         bool ok = j < P.L;
         cp_async4(tb + q, ok ? tc + j : tc, ok);
+    }
+    if (g.stat_off && phi == P.step - 1) {
+        // the window energies of the tile's valid outputs (its epilogue follows this
+        // phase); the others are zero-filled and never used
+        float *sb = buf + g.stat_off;
+        const float *se = P.stat_e + (size_t)ch * P.N;
+        const int klo = P.k_lo[t], khi = P.k_hi[t];
+        for (int x = threadIdx.x; x < PL_TILE; x += PL_THREADS) {
+            const long long k = k0 + x;
+            const bool ok = k >= klo && k < khi;
+            cp_async4(sb + padx(x), ok ? se + (k * P.step + mo) : se, ok);
+        }
     }
 }
 
@@ -250,6 +275,18 @@ plain_kernel(const Problem P, const PlainGeom g)
                 const float ts = FULL ? P.tsum[row] : 0.0f;
                 const float *se = P.stat_e + (size_t)ch * P.N;
                 const float2 *sem = reinterpret_cast<const float2 *>(P.stat_e) + (size_t)ch * P.N;
+                float staged[PL_R];  // 'short': this thread's energies from the stage, if staged
+                if (!FULL && g.stat_off) {
+                    const float *sb = smem + b * g.stage_floats + g.stat_off + padx(tid * PL_R);
+#pragma unroll
+                    for (int i = 0; i < PL_R; i += 4) {
+                        const float4 v = *reinterpret_cast<const float4 *>(sb + i);
+                        staged[i] = v.x;
+                        staged[i + 1] = v.y;
+                        staged[i + 2] = v.z;
+                        staged[i + 3] = v.w;
+                    }
+                }
 #pragma unroll
                 for (int r = 0; r < PL_R; r++) {
                     const int k = k0 + tid * PL_R + r;
@@ -261,7 +298,7 @@ plain_kernel(const Problem P, const PlainGeom g)
                             num = fmaf(-em.y, ts, num);
                             energy = em.x;
                         } else {
-                            energy = se[u];
+                            energy = g.stat_off ? staged[r] : se[u];
                         }
                         float den = sst * energy;
                         float cc = den > kThreshold ? num * rsqrtf(den) : 0.0f;
@@ -293,7 +330,7 @@ plain_kernel(const Problem P, const PlainGeom g)
 // Host launcher.  Returns FMF status.
 int launch_plain(const Problem &P, cudaStream_t stream)
 {
-    PlainGeom g = plain_geom(P.L, P.step);
+    PlainGeom g = plain_geom(P.L, P.step, !P.ntap && !P.normalize);
     if (g.smem > 227 * 1024)
         return set_error(FMF_ERR_SMEM,
                          "template length %d with step %d needs %zu bytes of shared memory (max 232448)",
