@@ -194,19 +194,33 @@ constexpr int kPrefixBlock = 2048;
 //    energy multiplied by the window mean, so its cancellation error stays far
 //    below float rounding of the energy.
 
-// grid = SC blocks of 1024 threads: the fixed-point unit q[ch] of the running
-// sums of d'^2: 2^(e - 60) with the channel energy below 2^e, so that no
-// running sum exceeds 2^61 units (clamped to the normal float range).
-__global__ void channel_unit_kernel(const float *__restrict__ data, int N, const float *__restrict__ mu,
-                                    float *__restrict__ unit)
+// The fixed-point unit q[ch] of the running sums of d'^2: 2^(e - 60) with the
+// channel energy below 2^e, so that no running sum exceeds 2^61 units
+// (clamped to the normal float range).  Two kernels: the energy of every
+// block of kPrefixBlock samples (double-float, all SMs busy), then the sum of
+// a channel's block energies in block order (so the unit does not depend on
+// scheduling) and the unit.
+// grid (blocks, SC), 256 threads
+__global__ void channel_energy_kernel(const float *__restrict__ data, int N, const float *__restrict__ mu,
+                                      float *__restrict__ part, int nblk)
 {
-    __shared__ float2 red[32];
-    const float m = mu ? mu[blockIdx.x] : 0.0f;
-    const float *src = data + (size_t)blockIdx.x * N;
+    __shared__ float2 red[8];
+    const int ch = blockIdx.y, blk = blockIdx.x;
+    const float m = mu ? mu[ch] : 0.0f;
+    const float *src = data + (size_t)ch * N;
+    const int i0 = blk * kPrefixBlock, i1 = min(N, i0 + kPrefixBlock);
+    constexpr int per = kPrefixBlock / 256;  // loads in flight per thread
+    float x[per];
+#pragma unroll
+    for (int e = 0; e < per; e++) {
+        const int i = i0 + e * 256 + threadIdx.x;
+        x[e] = i < i1 ? __ldg(src + i) - m : 0.0f;
+    }
     float h = 0.0f, l = 0.0f;
-    for (int i = threadIdx.x; i < N; i += blockDim.x) {
-        const float v = src[i] - m, sq = v * v;
-        pair_add(h, l, sq, fmaf(v, v, -sq));
+#pragma unroll
+    for (int e = 0; e < per; e++) {
+        const float sq = x[e] * x[e];
+        pair_add(h, l, sq, fmaf(x[e], x[e], -sq));
     }
     for (int o = 16; o > 0; o >>= 1) {
         const float yh = __shfl_down_sync(0xffffffffu, h, o), yl = __shfl_down_sync(0xffffffffu, l, o);
@@ -217,12 +231,32 @@ __global__ void channel_unit_kernel(const float *__restrict__ data, int N, const
     __syncthreads();
     if (threadIdx.x == 0) {
         float th = 0.0f, tl = 0.0f;
-        for (int i = 0; i < (int)(blockDim.x >> 5); i++)
+        for (int i = 0; i < 8; i++)
             pair_add(th, tl, red[i].x, red[i].y);
+        part[(size_t)ch * nblk + blk] = th + tl;
+    }
+}
+
+// grid SC, 32 threads: the channel's block energies summed in block order (each
+// lane a contiguous run, then the lanes in order), and its unit
+__global__ void channel_unit_kernel(const float *__restrict__ part, int nblk, float *__restrict__ unit)
+{
+    const int ch = blockIdx.x, lane = threadIdx.x;
+    const float *p = part + (size_t)ch * nblk;
+    const int per = (nblk + 31) / 32, b0 = lane * per, b1 = min(nblk, b0 + per);
+    float h = 0.0f, l = 0.0f;
+    for (int b = b0; b < b1; b++)
+        pair_add(h, l, p[b], 0.0f);
+    for (int o = 1; o < 32; o <<= 1) {  // lane 0 ends with lanes 0..31 in order
+        const float yh = __shfl_down_sync(0xffffffffu, h, o), yl = __shfl_down_sync(0xffffffffu, l, o);
+        if ((lane & (2 * o - 1)) == 0)
+            pair_add(h, l, yh, yl);
+    }
+    if (lane == 0) {
         int e = 0;
         // the sum rounded up by a margin, so that the float total cannot undershoot it
-        frexpf((th + tl) * 1.0001f, &e);
-        unit[blockIdx.x] = th + tl > 0.0f ? ldexpf(1.0f, max(e - 60, -126)) : 1.0f;
+        frexpf((h + l) * 1.0001f, &e);
+        unit[ch] = h + l > 0.0f ? ldexpf(1.0f, max(e - 60, -126)) : 1.0f;
     }
 }
 
@@ -245,10 +279,18 @@ __global__ void prefix_block_kernel(const float *__restrict__ data, int N, const
     const float *src = data + (size_t)ch * N;
     long long s2 = 0;
     float h1 = 0.0f, l1 = 0.0f;
-    for (int i = blk * kPrefixBlock + threadIdx.x; i < min(N, (blk + 1) * kPrefixBlock); i += blockDim.x) {
-        const float v = src[i] - m;
-        s2 += fixed_square(v, inv_unit);
-        pair_add(h1, l1, v, 0.0f);
+    const int i0 = blk * kPrefixBlock, i1 = min(N, i0 + kPrefixBlock);
+    constexpr int per = kPrefixBlock / 256;  // loads in flight per thread
+    float x[per];
+#pragma unroll
+    for (int e = 0; e < per; e++) {
+        const int i = i0 + e * 256 + threadIdx.x;
+        x[e] = i < i1 ? __ldg(src + i) - m : 0.0f;
+    }
+#pragma unroll
+    for (int e = 0; e < per; e++) {
+        s2 += fixed_square(x[e], inv_unit);
+        pair_add(h1, l1, x[e], 0.0f);
     }
     for (int o = 16; o > 0; o >>= 1) {
         s2 += __shfl_down_sync(0xffffffffu, s2, o);
@@ -272,36 +314,53 @@ __global__ void prefix_block_kernel(const float *__restrict__ data, int N, const
     }
 }
 
-// Phase 2, one thread per channel: exclusive scan of the block sums (the
-// float pairs renormalised at every step).
+// Phase 2, one warp per channel: exclusive scan of the block sums -- each lane
+// a contiguous run of blocks, the run totals scanned across the lanes (fixed
+// order, so the float pairs round the same way every time).
 __global__ void prefix_offsets_kernel(long long *bs2, float2 *bs1, int nblk, int SC)
 {
-    const int ch = blockIdx.x * blockDim.x + threadIdx.x;
+    const int ch = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
     if (ch >= SC)
-        return;
-    long long a = 0;
-    float2 b = make_float2(0.0f, 0.0f);
+        return;  // whole warps
     long long *p2 = bs2 + (size_t)ch * nblk;
     float2 *p1 = bs1 + (size_t)ch * nblk;
-    constexpr int G = 8;  // loads of a group issued before the dependent additions
-    for (int i0 = 0; i0 < nblk; i0 += G) {
-        long long x[G];
-        float2 y[G];
-#pragma unroll
-        for (int j = 0; j < G; j++) {
-            x[j] = i0 + j < nblk ? p2[i0 + j] : 0;
-            y[j] = i0 + j < nblk ? p1[i0 + j] : make_float2(0.0f, 0.0f);
+    const int per = (nblk + 31) / 32, b0 = min(nblk, lane * per), b1 = min(nblk, b0 + per);
+    long long a = 0;
+    float h = 0.0f, l = 0.0f;
+    for (int b = b0; b < b1; b++) {  // this lane's run total
+        a += p2[b];
+        const float2 y = p1[b];
+        pair_add(h, l, y.x, y.y);
+    }
+    // inclusive scan of the run totals over the lanes, then this lane's exclusive offset
+    long long ia = a;
+    float ih = h, il = l;
+    for (int o = 1; o < 32; o <<= 1) {
+        const long long ya = __shfl_up_sync(0xffffffffu, ia, o);
+        const float yh = __shfl_up_sync(0xffffffffu, ih, o), yl = __shfl_up_sync(0xffffffffu, il, o);
+        if (lane >= o) {
+            ia += ya;
+            float th = yh, tl = yl;  // earlier lanes first
+            pair_add(th, tl, ih, il);
+            ih = th;
+            il = tl;
         }
-#pragma unroll
-        for (int j = 0; j < G; j++) {
-            if (i0 + j < nblk) {
-                p2[i0 + j] = a;
-                p1[i0 + j] = b;
-            }
-            a += x[j];
-            pair_add(b.x, b.y, y[j].x, y[j].y);
-            b = pair_normalise(b.x, b.y);
-        }
+    }
+    long long ea = __shfl_up_sync(0xffffffffu, ia, 1);
+    float eh = __shfl_up_sync(0xffffffffu, ih, 1), el = __shfl_up_sync(0xffffffffu, il, 1);
+    if (lane == 0) {
+        ea = 0;
+        eh = el = 0.0f;
+    }
+    float2 b = pair_normalise(eh, el);
+    for (int k = b0; k < b1; k++) {
+        const long long x = p2[k];
+        const float2 y = p1[k];
+        p2[k] = ea;
+        p1[k] = b;
+        ea += x;
+        pair_add(b.x, b.y, y.x, y.y);
+        b = pair_normalise(b.x, b.y);
     }
 }
 
@@ -478,7 +537,7 @@ static int variable_device(const VArgs &a, int L, cudaStream_t s, float *host_ou
     float *zweight, *consts, *tmask, *tsum = nullptr, *mu = nullptr, *dcen = nullptr;
     long long *bs2, *pre2q;
     float2 *bs1, *pre1f = nullptr;
-    float *unit;
+    float *unit, *epart;
     const int nblk = (N + kPrefixBlock - 1) / kPrefixBlock;
     if ((rc = ws.get(&k_lo, 2 * (size_t)T, "template ranges")) ||
         (rc = ws.get(&zweight, (size_t)T * SC, "Fisher-z weights")) ||
@@ -486,6 +545,7 @@ static int variable_device(const VArgs &a, int L, cudaStream_t s, float *host_ou
         (rc = ws.get(&tmask, (size_t)T * SC * L, "masked templates")) ||
         (rc = ws.get(&pre2q, (size_t)SC * (N + 1), "running sums of d^2")) ||
         (rc = ws.get(&unit, (size_t)SC, "fixed-point units")) ||
+        (rc = ws.get(&epart, (size_t)SC * nblk, "block energies")) ||
         (rc = ws.get(&bs2, (size_t)SC * nblk, "block sums")) ||
         (rc = ws.get(&bs1, (size_t)SC * nblk, "block sums")))
         return rc;
@@ -505,12 +565,13 @@ static int variable_device(const VArgs &a, int L, cudaStream_t s, float *host_ou
     vp_template_kernel<<<(unsigned)((size_t)T * SC), 128, 0, s>>>(a.tpl, a.ntap, L, full ? 1 : 0, tmask, tsum);
     if (full)
         channel_centre_kernel<<<SC, 1024, 0, s>>>(a.data, N, mu);
-    channel_unit_kernel<<<SC, 1024, 0, s>>>(a.data, N, mu, unit);
+    channel_energy_kernel<<<dim3(nblk, SC), 256, 0, s>>>(a.data, N, mu, epart, nblk);
+    channel_unit_kernel<<<SC, 32, 0, s>>>(epart, nblk, unit);
     prefix_block_kernel<<<dim3(nblk, SC), 256, 0, s>>>(a.data, N, mu, unit, bs2, bs1, nblk);
-    prefix_offsets_kernel<<<(SC + 127) / 128, 128, 0, s>>>(bs2, bs1, nblk, SC);
+    prefix_offsets_kernel<<<(SC + 3) / 4, 128, 0, s>>>(bs2, bs1, nblk, SC);  // a warp per channel
     prefix_write_kernel<<<dim3(nblk, SC), 256, 0, s>>>(a.data, N, mu, unit, bs2, bs1, nblk, pre2q,
                                                         pre1f, dcen);
-    count_launch(full ? 9 : 8);
+    count_launch(full ? 10 : 9);
     if ((rc = check_launch("variable-length preprocessing")))
         return rc;
 

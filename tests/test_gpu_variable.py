@@ -137,8 +137,9 @@ def test_variable_tensor_core_short_channels(oracle_built, step, normalize):
 def test_variable_full_with_drift(oracle_built, precision):
     """'full' on data whose window means dominate their spread (a DC offset
     and a slow drift 50x the noise): the centred window energies
-    S2 - S1^2 / n are formed from float-pair prefix sums in double-float
-    arithmetic and must keep float accuracy despite the cancellation."""
+    S2 - S1^2 / n are formed from the running sums (d^2 exact fixed point, d
+    float pairs) in double-float arithmetic and must keep float accuracy
+    despite the cancellation."""
     rng = np.random.default_rng(44)
     tp, mo, w, d = random_search(45, 3, 3, 2, 160, 9000, -20, 120, zero_weights=1)
     i = np.arange(d.shape[-1])
@@ -206,7 +207,7 @@ def test_variable_launch_count_per_call():
                            precision=precision)
         counts.append(lib.fmf_last_launch_count())
     assert counts[0] == counts[1] and counts[2] == counts[3], counts
-    assert 0 < counts[0] <= 12 and 0 < counts[2] <= 12, counts
+    assert 0 < counts[0] <= 14 and 0 < counts[2] <= 14, counts
 
 
 @pytest.mark.parametrize("precision", ["fp32", "split_bf16"])
