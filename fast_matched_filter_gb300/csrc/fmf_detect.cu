@@ -70,7 +70,8 @@ struct DetState {
     float med, mad, thr;
     int n_cand;            // local maxima at or above thr (may exceed the capacity)
     float thr_lo;          // a lower bound of thr known before the MAD pass
-    int peaks_ready;       // 1: the MAD counting pass gathered the local maxima >= thr_lo
+    int peaks_ready;       // 1: the MAD counting pass noted the values >= thr_lo
+    int n_hot;             // values >= thr_lo noted (may exceed the capacity)
     int src;               // kSrcRow / kSrcCand / kSrcDone
     unsigned klo, khi;     // sample window of the keys
     int n_lt, n_in;        // keys below klo, keys inside [klo, khi]
@@ -136,6 +137,7 @@ __global__ void det_init_kernel(DetState *__restrict__ st, int T, int n_corr,
     s.n_cand = 0;
     s.thr_lo = __int_as_float(0x7fc00000);
     s.peaks_ready = 0;
+    s.n_hot = 0;
     s.src = kSrcRow;
     s.klo = s.khi = 0u;
     s.n_lt = s.n_in = 0;
@@ -317,29 +319,26 @@ __device__ __forceinline__ void peak_at(const float *row, long long i, long long
     }
 }
 
-// The local maxima among the four values at window offsets [o, o + 4) of row
-// t: the rare path of the counting pass (row bounds and threshold re-read
-// from the state, so that the pass keeps only the threshold in registers).
-__device__ __forceinline__ void peaks_of4(const float *cc, size_t ld, DetState *st, int t, long long o,
-                                       float4 v, int2 *pcand, int pcap)
+// A value of row t at window offset o at or above thr_lo, noted in the row's
+// hot list (the rare path of the MAD counting pass: one atomic, one store;
+// det_hot_kernel examines the neighbours later).
+__device__ __forceinline__ void note_hot(DetState *st, int t, long long o, int *hot, int cap)
 {
-    const long long b = st[t].begin, e = st[t].end;
-    const float thr_lo = st[t].thr_lo;
-    const float *row = cc + (size_t)t * ld;
-    peak_at(row, b + o, b, e, v.x, thr_lo, st, pcand, pcap, t);
-    peak_at(row, b + o + 1, b, e, v.y, thr_lo, st, pcand, pcap, t);
-    peak_at(row, b + o + 2, b, e, v.z, thr_lo, st, pcand, pcap, t);
-    peak_at(row, b + o + 3, b, e, v.w, thr_lo, st, pcand, pcap, t);
+    const int slot = atomicAdd(&st[t].n_hot, 1);
+    if (slot < cap)
+        hot[(size_t)t * cap + slot] = (int)o;
 }
 
 // Step 2: one pass over the row: keys below klo counted, keys inside
 // [klo, khi] appended to the row's candidate list (up to cap).  In the MAD
-// pass (mode 1) the same read gathers the local maxima at or above thr_lo
-// into the peak list (pcand), so that no third read of the row is needed.
-__global__ void __launch_bounds__(kDetThreads, 3)  // 24 warps per SM: loads in flight, no spills
+// pass (mode 1, PEAKS) the same read notes the offsets of the values at or
+// above thr_lo in the row's hot list, so that no third read of the row is
+// needed for the peaks.
+template <bool PEAKS>
+__global__ void __launch_bounds__(kDetThreads, 4)  // 32 warps per SM: enough loads in flight
 det_count_kernel(const float *__restrict__ cc, size_t ld, DetState *__restrict__ st,
-                 unsigned *__restrict__ cand, long long cap, int mode, int2 *__restrict__ pcand,
-                 int pcap)
+                 unsigned *__restrict__ cand, long long cap, int mode, int *__restrict__ hot,
+                 int hcap)
 {
     const int t = blockIdx.y;
     const int src = st[t].src;
@@ -348,7 +347,7 @@ det_count_kernel(const float *__restrict__ cc, size_t ld, DetState *__restrict__
         return;
     const unsigned klo = st[t].klo, khi = st[t].khi;
     const float med = st[t].med;
-    const bool peaks = mode == 1 && st[t].peaks_ready != 0;
+    const bool peaks = PEAKS && mode == 1 && st[t].peaks_ready != 0;
     const float thr_lo = st[t].thr_lo;
     const float *row = cc + (size_t)t * ld + st[t].begin;
     unsigned *list = cand + (size_t)t * cap;
@@ -401,10 +400,8 @@ det_count_kernel(const float *__restrict__ cc, size_t ld, DetState *__restrict__
         ok[0] = lane < rs.head + rs.tail;
         const float x = ok[0] ? row[i] : 0.0f;
         key[0] = ok[0] ? sel_key(x, mode, med) : 0u;
-        if (peaks && ok[0] && x >= thr_lo) {
-            const long long b = st[t].begin, e = st[t].end;
-            peak_at(cc + (size_t)t * ld, b + i, b, e, x, thr_lo, st, pcand, pcap, t);
-        }
+        if (peaks && ok[0] && x >= thr_lo)
+            note_hot(st, t, i, hot, hcap);
 #pragma unroll
         for (int u = 1; u < kK; u++) {
             ok[u] = false;
@@ -433,13 +430,22 @@ det_count_kernel(const float *__restrict__ cc, size_t ld, DetState *__restrict__
         for (int u = 0; u < 4; u++)
             v[u] = nv[u];
         load4(c + cstride, nv);  // the next step's values are in flight while this one is counted
-        if (peaks) {  // local maxima at or above thr_lo (rare: out of line)
+        if (peaks) {  // values at or above thr_lo (rare)
 #pragma unroll
             for (int u = 0; u < 4; u++) {
                 const long long q = c * 128 + u * 32 + lane;
                 const float mx = fmaxf(fmaxf(v[u].x, v[u].y), fmaxf(v[u].z, v[u].w));
-                if (q < rs.nvec && mx >= thr_lo)
-                    peaks_of4(cc, ld, st, t, rs.head + 4 * q, v[u], pcand, pcap);
+                if (q < rs.nvec && mx >= thr_lo) {
+                    const long long o = rs.head + 4 * q;
+                    if (v[u].x >= thr_lo)
+                        note_hot(st, t, o, hot, hcap);
+                    if (v[u].y >= thr_lo)
+                        note_hot(st, t, o + 1, hot, hcap);
+                    if (v[u].z >= thr_lo)
+                        note_hot(st, t, o + 2, hot, hcap);
+                    if (v[u].w >= thr_lo)
+                        note_hot(st, t, o + 3, hot, hcap);
+                }
             }
         }
 #pragma unroll
@@ -484,7 +490,7 @@ __global__ void det_check_kernel(DetState *__restrict__ st, int T, long long cap
         if (mode == 1)
             s.peaks_ready = 0;
     }
-    if (mode == 1 && (!s.peaks_ready || s.n_cand > pcap)) {
+    if (mode == 1 && (!s.peaks_ready || s.n_hot > pcap)) {
         s.peaks_ready = 0;
         s.n_cand = 0;
     }
@@ -650,6 +656,32 @@ __global__ void det_resolve_kernel(DetState *__restrict__ st, unsigned *__restri
         finish_select(s, mode, middle_value(s.prefix[0], s.prefix[1], n), n_mad);
     if (lane == 0)
         st[t] = s;
+}
+
+// The local maxima among a row's hot values (at or above thr_lo), one block
+// per row: appended to the candidate list, a superset of the peaks that the
+// select kernel filters by the exact threshold.  A superset that overflows
+// the list hands the row to det_peaks_kernel (exact threshold).
+__global__ void __launch_bounds__(kDetThreads)
+det_hot_kernel(const float *__restrict__ cc, size_t ld, DetState *__restrict__ st,
+               const int *__restrict__ hot, int hcap, int2 *__restrict__ cand, int cap)
+{
+    const int t = blockIdx.x;
+    if (!st[t].peaks_ready)
+        return;  // uniform over the block
+    const long long b = st[t].begin, e = st[t].end;
+    const float thr_lo = st[t].thr_lo;
+    const float *row = cc + (size_t)t * ld;
+    const int n = min(st[t].n_hot, hcap);
+    for (int j = threadIdx.x; j < n; j += blockDim.x) {
+        const long long i = b + hot[(size_t)t * hcap + j];
+        peak_at(row, i, b, e, row[i], thr_lo, st, cand, cap, t);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0 && st[t].n_cand > cap) {
+        st[t].peaks_ready = 0;
+        st[t].n_cand = 0;
+    }
 }
 
 // Local maxima at or above the threshold, appended (unordered) to the
@@ -855,6 +887,7 @@ int detect_device(const float *cc, int T, int n_corr, size_t ld, const int *begi
     DetState *st;
     unsigned *hist, *keys;
     int2 *cand;
+    int *hot;
     float *saved;
     // candidate keys per row: the sample window holds about 5 % of a row
     const long long key_cap = n_corr < 65536 ? n_corr : std::max(65536LL, (long long)n_corr / 8);
@@ -862,6 +895,7 @@ int detect_device(const float *cc, int T, int n_corr, size_t ld, const int *begi
         (rc = ws.get(&hist, (size_t)chunk * 2 * kDetBins, "detection histograms")) ||
         (rc = ws.get(&keys, (size_t)chunk * key_cap, "candidate keys")) ||
         (rc = ws.get(&cand, (size_t)chunk * kDetCap, "candidate peaks")) ||
+        (rc = ws.get(&hot, (size_t)chunk * kDetCap, "values above the threshold bound")) ||
         (rc = ws.get(&saved, (size_t)chunk * kDetSample, "sampled values")))
         return rc;
     cudaError_t e = cudaFuncSetAttribute(det_select_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -890,8 +924,12 @@ int detect_device(const float *cc, int T, int n_corr, size_t ld, const int *begi
         for (int mode = 0; mode < 2; mode++) {
             det_sample_kernel<<<nt, 1024, kDetSample * sizeof(unsigned), s>>>(rows, ld, st, mode, n_mad,
                                                                                saved);
-            det_count_kernel<<<grid, kDetThreads, 0, s>>>(rows, ld, st, keys, key_cap, mode, cand,
-                                                          kDetCap);
+            if (mode == 1)
+                det_count_kernel<true><<<grid, kDetThreads, 0, s>>>(rows, ld, st, keys, key_cap, mode,
+                                                                    hot, kDetCap);
+            else
+                det_count_kernel<false><<<grid, kDetThreads, 0, s>>>(rows, ld, st, keys, key_cap, mode,
+                                                                     hot, kDetCap);
             det_check_kernel<<<(nt + 127) / 128, 128, 0, s>>>(st, nt, key_cap, mode, kDetCap);
             for (int pass = 0; pass < 3; pass++) {
                 det_hist_kernel<<<grid, kDetThreads, 0, s>>>(rows, ld, st, hist, keys, key_cap, pass,
@@ -899,12 +937,13 @@ int detect_device(const float *cc, int T, int n_corr, size_t ld, const int *begi
                 det_resolve_kernel<<<nt, 32, 0, s>>>(st, hist, pass, mode, n_mad);
             }
         }
+        det_hot_kernel<<<nt, kDetThreads, 0, s>>>(rows, ld, st, hot, kDetCap, cand, kDetCap);
         det_peaks_kernel<<<grid, kDetThreads, 0, s>>>(rows, ld, st, cand, kDetCap);
         det_select_kernel<<<nt, kDetSelectThreads, select_smem(kDetCap), s>>>(
             st, cand, kDetCap, min_sep, max_det, med_out ? med_out + t0 : nullptr,
             mad_out ? mad_out + t0 : nullptr, thr_out ? thr_out + t0 : nullptr, count_out + t0,
             lag_out + (size_t)t0 * max_det, val_out + (size_t)t0 * max_det);
-        count_launch(21);
+        count_launch(22);
         if ((rc = check_launch("detection kernels")))
             return rc;
     }
