@@ -31,14 +31,14 @@
 //      match the bits chosen so far) runs over the candidates only; if not --
 //      heavy ties, an adversarial row -- the same radix selection runs over
 //      the whole row.  Rows no longer than the sample are sorted whole.
-// The MAD pass's read of the row also gathers the local maxima at or above a
-// lower bound of the threshold (from the MAD window: thr = med + n_mad * mad
-// is monotone in mad), so a call reads the rows twice (median, MAD + peaks)
-// in the usual case; rows whose MAD window missed get a peak pass of their
-// own.  Peaks are gathered into a list per template (capacity kDetCap) and
-// filtered by one thread block per template: the candidates below the exact
-// threshold dropped, a sort by lag, a sort by height, and the greedy distance
-// filter.
+// The MAD pass's read of the row also notes the values at or above a lower
+// bound of the threshold (from the MAD window: thr = med + n_mad * mad is
+// monotone in mad) in a hot list, whose local maxima a small kernel gathers,
+// so a call reads the rows twice (median, MAD + peaks) in the usual case; rows
+// whose MAD window missed get a peak pass of their own.  Peaks are gathered
+// into a list per template (capacity kDetCap) and filtered by one thread
+// block per template: the candidates below the exact threshold dropped, a
+// sort by lag, a sort by height, and the greedy distance filter.
 //
 // Every launch is stream-ordered and the state lives on the device, so a
 // detection run needs no host round trip and can be captured in a graph.
