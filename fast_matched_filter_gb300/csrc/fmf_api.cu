@@ -143,6 +143,18 @@ void populate_host(void *p, size_t bytes)
 #endif
 }
 
+// Page-locked (or registered) host memory is mapped already: populate_host
+// would only walk its page tables.
+bool host_is_pinned(const void *p)
+{
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return at.type == cudaMemoryTypeHost;
+}
+
 int check_launch(const char *what)
 {
     cudaError_t e = cudaGetLastError();
@@ -551,6 +563,7 @@ static int run_streamed(const Args &d, float *host_out, cudaStream_t s)
         // end of the last correlation kernel (twice: each span owns its events)
         cudaEvent_t ev_kern1 = mark(s), ev_kern1b = mark(s), ev_out0 = nullptr;
         span(ev_kern0, ev_kern1, kSpanKernel);
+        const bool pinned = host_is_pinned(host_out);
         for (int c = 0; c < launched && rc == FMF_OK && e == cudaSuccess; c++) {
             const int t0 = bounds[c], nt = bounds[c + 1] - bounds[c];
             if (nt <= 0)
@@ -560,7 +573,8 @@ static int run_streamed(const Args &d, float *host_out, cudaStream_t s)
                 break;
             if (!ev_out0)
                 ev_out0 = mark(s2);
-            populate_host(host_out + off, n);  // while the kernels run
+            if (!pinned)
+                populate_host(host_out + off, n);  // while the kernels run
             if ((e = cudaMemcpyAsync(host_out + off, P.out + off, n, cudaMemcpyDeviceToHost, s2)) !=
                 cudaSuccess)
                 break;

@@ -157,6 +157,7 @@ int check_launch(const char *what);
 // Maps the host pages of a result buffer for writing before a copy into it
 // (parallel; a no-op where the kernel refuses).
 void populate_host(void *p, size_t bytes);
+bool host_is_pinned(const void *p);  // page-locked or registered host memory
 
 // Stream-ordered scratch allocations (cudaMallocAsync from the device's
 // default pool).  The pool keeps freed blocks for reuse by later calls;

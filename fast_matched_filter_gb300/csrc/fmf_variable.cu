@@ -670,11 +670,13 @@ static int variable_device(const VArgs &a, int L, cudaStream_t s, float *host_ou
     }
     if (!host_out)
         return FMF_OK;
+    const bool out_pinned = host_is_pinned(host_out);
     for (int c = 0; c < n_chunks; c++) {
         const int t0 = bounds[c], nt = bounds[c + 1] - bounds[c];
         if (nt <= 0)
             continue;
-        populate_host(host_out + (size_t)t0 * a.n_corr, (size_t)nt * row_bytes);  // while kernels run
+        if (!out_pinned)
+            populate_host(host_out + (size_t)t0 * a.n_corr, (size_t)nt * row_bytes);  // while kernels run
         if ((e = cudaStreamWaitEvent(cs.s2, cs.ev[c], 0)) != cudaSuccess ||
             (e = cudaMemcpyAsync(host_out + (size_t)t0 * a.n_corr, a.out + (size_t)t0 * a.n_corr,
                                  (size_t)nt * row_bytes, cudaMemcpyDeviceToHost, cs.s2)) != cudaSuccess)
