@@ -4,8 +4,8 @@
 // batch records any number of searches (device pointers, each with its own
 // T, S, C, L, N, step, normalisation and output layout) and runs them as one
 // CUDA graph: every search's preprocessing kernels, then, for the tensor-core
-// precisions, ONE persistent launch per 64 searches over a shared tile queue
-// (fmf_tc.cu), or, for FP32, the plain kernel per search.  The graph is
+// precisions, one persistent launch per normalisation and 64 searches over a
+// shared tile queue (fmf_tc.cu), or, for FP32, the plain kernel per search.  The graph is
 // captured on the first run (on a stream the batch owns, joined to the
 // caller's stream with events) and replayed afterwards; its scratch lives in
 // graph memory nodes.  The searches' preprocessing (and the FP32 searches)
@@ -93,13 +93,23 @@ static int batch_record(fmf_batch *b, cudaStream_t s)
         if (status == FMF_OK && tc) {
             unsigned *err = nullptr;
             if ((status = device_error_word(&err)) == FMF_OK) {
-                for (size_t i0 = 0; i0 < n && status == FMF_OK; i0 += TC_MAX_PROBS) {
-                    unsigned long long *queue;
-                    if ((status = ws.get(&queue, 1, "tile queue")))
-                        break;
-                    const int m = (int)(n - i0 < (size_t)TC_MAX_PROBS ? n - i0 : TC_MAX_PROBS);
-                    status = tc_run(reinterpret_cast<const TcProb *>(probs.data() + psz * i0), m, split,
-                                    queue, err, s);
+                // one persistent launch per normalisation (each runs the epilogue
+                // instantiation of its own mode: a mixed launch carries both modes' code),
+                // 64 searches at most per launch
+                for (int norm = 0; norm < 2 && status == FMF_OK; norm++) {
+                    std::vector<unsigned char> grp;
+                    for (size_t i = 0; i < n; i++)
+                        if (P[i].normalize == norm)
+                            grp.insert(grp.end(), probs.begin() + psz * i, probs.begin() + psz * (i + 1));
+                    const size_t ng = grp.size() / psz;
+                    for (size_t i0 = 0; i0 < ng && status == FMF_OK; i0 += TC_MAX_PROBS) {
+                        unsigned long long *queue;
+                        if ((status = ws.get(&queue, 1, "tile queue")))
+                            break;
+                        const int m = (int)(ng - i0 < (size_t)TC_MAX_PROBS ? ng - i0 : TC_MAX_PROBS);
+                        status = tc_run(reinterpret_cast<const TcProb *>(grp.data() + psz * i0), m, split,
+                                        queue, err, s);
+                    }
                 }
             }
         }
