@@ -377,7 +377,8 @@ def run_ours(args):
     main = timed(requested, args.steps, args.warmup, True)
     precision = _lib.PRECISION_NAMES[lib.fmf_last_precision()]  # the form that ran
     value = main["value"]
-    roof = roofline(cfg, precision, main["kernel_ms_avg"], main["prep_ms_avg"])
+    roof = roofline(cfg, precision, main["kernel_ms_avg"], main["prep_ms_avg"],
+                    measured_fp32_tflops(lib) if precision == "fp32" else None)
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": main["ms_per_step"],
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -394,7 +395,8 @@ def run_ours(args):
                               "kernel_ms_avg": plain["kernel_ms_avg"],
                               "speedup_of_headline": value / plain["value"],
                               "roofline": roofline(cfg, "fp32", plain["kernel_ms_avg"],
-                                                   plain["prep_ms_avg"])}
+                                                   plain["prep_ms_avg"],
+                                                   fp32_measured=measured_fp32_tflops(lib))}
 
     if rank == 0 and not args.no_precision_report:
         line["precision_vs_fp64"] = precision_report(cfg)
@@ -489,16 +491,35 @@ def profiled_traffic(kernel_prefix, cfg):
     return None, None
 
 
-def roofline(cfg, precision, kern_ms, prep_ms):
+def measured_fp32_tflops(lib):
+    """The FP32 FMA rate measured in this run (fmf_measure_fp32_fma: independent
+    FMA chains on every SM), in TFLOP/s, or None."""
+    import ctypes as ct
+    v = ct.c_double()
+    return v.value if lib.fmf_measure_fp32_fma(ct.byref(v)) == 0 and v.value > 0 else None
+
+
+def fp32_peak(measured):
+    """(peak, nominal, source) of the FP32 FMA roofline: the rate measured in this run
+    when there is one, else the nominal 152 SMs x 128 lanes x max SM clock."""
+    peaks, src = load_peaks()
+    mhz = float(peaks.get("sm_max_mhz", 2070.0))
+    nominal = N_SM * 128 * 2 * mhz * 1e6 / 1e12
+    if measured:
+        return measured, nominal, ("measured in this run: FP32 FMA kernel of independent chains on "
+                                   "every SM (fmf_measure_fp32_fma)")
+    return nominal, nominal, ("nominal FP32 FMA rate: 152 SMs x 128 lanes x %.0f MHz (%s max SM "
+                              "clock)" % (mhz, src))
+
+
+def roofline(cfg, precision, kern_ms, prep_ms, fp32_measured=None):
     peaks, src = load_peaks()
     algo_tflops = 2.0 * cfg["macs"] / (kern_ms / 1e3) / 1e12
     if precision == "fp32":
-        mhz = float(peaks.get("sm_max_mhz", 2070.0))
-        peak = N_SM * 128 * 2 * mhz * 1e6 / 1e12
+        peak, nominal, psrc = fp32_peak(fp32_measured)
         roof = {"bound": "fp32_fma", "achieved": algo_tflops, "peak": peak, "unit": "TFLOP/s",
-                "frac": algo_tflops / peak, "traffic": None, "kernel": "plain_kernel",
-                "peak_source": "nominal FP32 FMA rate: 152 SMs x 128 lanes x %.0f MHz (%s max "
-                               "SM clock); no measured FP32 peak exists" % (mhz, src)}
+                "frac": algo_tflops / peak, "nominal_peak": nominal, "nominal_frac": algo_tflops / nominal,
+                "traffic": None, "kernel": "plain_kernel", "peak_source": psrc}
     else:
         bf16 = float(peaks.get("bf16_tflops_sustained", peaks["bf16_tflops"]))
         products = 3 if precision == "split_bf16" else 1
@@ -799,18 +820,18 @@ def run_variable(args):
         return ms, launches, (clocks.summary() if sample_clocks else None)
 
     peaks, kind = load_peaks()
-    fma_peak = N_SM * 128 * 2 * peaks.get("sm_max_mhz", 2070.0) * 1e6 / 1e12  # TFLOP/s
+    fma_peak, fma_nominal, fma_src = fp32_peak(measured_fp32_tflops(lib))  # TFLOP/s
 
     def plain_roofline(ms):
         # the kernel runs each channel over its own taps rounded up to its 20-tap unroll
         executed = int(n_corr) * int(((nt.astype(np.int64) + 19) // 20 * 20).sum())
         achieved = 2 * cfg["macs"] / (ms / 1e3) / 1e12
         return {"bound": "fp32_fma", "achieved": achieved, "peak": fma_peak, "unit": "TFLOP/s",
-                "frac": achieved / fma_peak,
+                "frac": achieved / fma_peak, "nominal_peak": fma_nominal,
+                "nominal_frac": achieved / fma_nominal,
                 "executed_frac": 2 * executed / (ms / 1e3) / 1e12 / fma_peak,
                 "traffic": None, "kernel": "plain_kernel (per-channel lengths)",
-                "peak_source": "nominal FP32 FMA rate: 152 SMs x 128 lanes x max SM clock; "
-                               "no measured FP32 peak exists"}
+                "peak_source": fma_src}
 
     def tc_roofline(ms):
         bf16 = peaks.get("bf16_tflops_sustained", FALLBACK_PEAKS["bf16_tflops_sustained"])

@@ -64,7 +64,7 @@ EXPORTS = ("fmf_matched_filter", "matched_filter", "fmf_matched_filter_ex",
            "fmf_batch_destroy", "fmf_selftest_wait_timeout", "fmf_matched_filter_variable",
            "fmf_matched_filter_variable_ex", "fmf_detect", "fmf_matched_filter_detect",
            "fmf_template_energies", "fmf_matched_filter_check_zeros", "fmf_eval_atanh",
-           "fmf_last_precision")
+           "fmf_last_precision", "fmf_measure_fp32_fma")
 
 DETECT_CAPACITY = 16384  # FMF_DETECT_CAPACITY
 # detection arguments after the rows: n_mad, min_separation, max_detections, six outputs,
@@ -105,6 +105,8 @@ def load(path=None):
     lib.fmf_version.restype = ct.c_char_p
     lib.fmf_last_launch_count.restype = ct.c_int
     lib.fmf_last_precision.restype = ct.c_int
+    lib.fmf_measure_fp32_fma.argtypes = [ct.POINTER(ct.c_double)]
+    lib.fmf_measure_fp32_fma.restype = ct.c_int
     lib.fmf_release_cache.restype = ct.c_int
     lib.fmf_timing_begin.restype = ct.c_int
     lib.fmf_device_errors.restype = ct.c_int

@@ -1060,6 +1060,69 @@ int fmf_selftest_wait_timeout(unsigned ms)
     return fmf_device_errors();
 }
 
+namespace fmf {
+// 16 independent multiply-add chains per thread: the FP32 FMA rate the SMs
+// sustain on register operands, the denominator of the plain kernel's roofline.
+__global__ void __launch_bounds__(256) fma_rate_kernel(float *sink, int iters, float a, float b)
+{
+    float x[16];
+#pragma unroll
+    for (int i = 0; i < 16; i++)
+        x[i] = threadIdx.x * 1e-3f + (float)i;
+    for (int it = 0; it < iters; it++) {
+#pragma unroll
+        for (int i = 0; i < 16; i++)
+            x[i] = fmaf(x[i], a, b);
+    }
+    float s = 0.0f;
+#pragma unroll
+    for (int i = 0; i < 16; i++)
+        s += x[i];
+    if (s == -1.0f)  // never: keeps the chains live
+        sink[0] = s;
+}
+}  // namespace fmf
+
+int fmf_measure_fp32_fma(double *tflops)
+{
+    fmf::clear_error();
+    if (!tflops)
+        return fmf::set_error(FMF_ERR_ARG, "null output");
+    int dev = 0, sms = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess)
+        e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    float *sink = nullptr;
+    cudaEvent_t a = nullptr, b = nullptr;
+    if (e == cudaSuccess)
+        e = cudaMalloc(&sink, sizeof(float));
+    if (e == cudaSuccess)
+        e = cudaEventCreate(&a);
+    if (e == cudaSuccess)
+        e = cudaEventCreate(&b);
+    const int iters = 20000, grid = 4 * sms;
+    float ms = 0.0f, best = 0.0f;
+    for (int rep = 0; rep < 3 && e == cudaSuccess; rep++) {  // the first run warms the clocks
+        fmf::fma_rate_kernel<<<grid, 256>>>(sink, iters, 0.999f, 0.001f);
+        cudaEventRecord(a);
+        fmf::fma_rate_kernel<<<grid, 256>>>(sink, iters, 0.999f, 0.001f);
+        cudaEventRecord(b);
+        if ((e = cudaEventSynchronize(b)) == cudaSuccess && (e = cudaEventElapsedTime(&ms, a, b)) == cudaSuccess)
+            best = (best == 0.0f || ms < best) ? ms : best;
+    }
+    if (a)
+        cudaEventDestroy(a);
+    if (b)
+        cudaEventDestroy(b);
+    if (sink)
+        cudaFree(sink);
+    if (e != cudaSuccess)
+        return fmf::cuda_status(e, "fmf_measure_fp32_fma");
+    const double fma = (double)grid * 256 * 16 * iters;
+    *tflops = 2.0 * fma / (best * 1e-3) / 1e12;
+    return FMF_OK;
+}
+
 int fmf_eval_atanh(const float *y, float *out, size_t n, void *stream)
 {
     fmf::clear_error();

@@ -310,6 +310,13 @@ FMF_API int fmf_device_errors(void);
  * and reported it as the library's kernels do; the device stays usable. */
 FMF_API int fmf_selftest_wait_timeout(unsigned ms);
 
+/* Measurement helper (no reference counterpart): the FP32 multiply-add rate
+ * of the current device in TFLOP/s (2 flops per FMA), from a kernel of
+ * independent FMA chains on every SM, best of three timed runs (about 10 ms
+ * in all; synchronizes the device).  The denominator of the plain FP32
+ * kernel's roofline. */
+FMF_API int fmf_measure_fp32_fma(double *tflops);
+
 /* Accuracy check of the atanh used by the tensor-core form of the per-channel
  * length search (no reference counterpart): out[i] = atanh(y[i]) as that
  * epilogue computes it, for n device floats, asynchronous on `stream`. */

@@ -32,3 +32,15 @@ def test_selftest_rejects_bad_limits():
     lib = _lib.load()
     assert lib.fmf_selftest_wait_timeout(0) == _lib.FMF_ERR_ARG
     assert lib.fmf_selftest_wait_timeout(100000) == _lib.FMF_ERR_ARG
+
+
+def test_fp32_fma_rate_measurement():
+    """fmf_measure_fp32_fma, the plain kernel's roofline denominator: a rate
+    between half and 1.05 times the nominal 152 SMs x 128 lanes x 2.07 GHz."""
+    import ctypes as ct
+    from fast_matched_filter_gb300 import _lib
+    lib = _lib.load()
+    v = ct.c_double()
+    assert lib.fmf_measure_fp32_fma(ct.byref(v)) == 0
+    nominal = 152 * 128 * 2 * 2.07e9 / 1e12
+    assert 0.5 * nominal < v.value < 1.05 * nominal, v.value
