@@ -154,6 +154,11 @@ void count_launch(int n = 1);
 void reset_launch_count();  // at the start of every entry point (fmf_last_launch_count)
 void keep_pool_cached();    // at the start of every entry point that allocates scratch
 int check_launch(const char *what);
+// The dynamic shared memory every variable-size kernel is allowed: the
+// attribute is set to the largest a CTA may have, never to one call's need, so
+// that calls from several host threads with different needs cannot lower it
+// under one another's launch.
+constexpr int kMaxDynamicSmem = 227 * 1024;
 // Maps the host pages of a result buffer for writing before a copy into it
 // (parallel; a no-op where the kernel refuses).
 void populate_host(void *p, size_t bytes);

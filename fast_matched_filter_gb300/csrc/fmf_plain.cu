@@ -338,7 +338,7 @@ int launch_plain(const Problem &P, cudaStream_t stream)
     void (*kern)(const Problem, const PlainGeom) =
         P.ntap ? (P.normalize ? plain_kernel<true, true> : plain_kernel<false, true>)
                : (P.normalize ? plain_kernel<true, false> : plain_kernel<false, false>);
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)g.smem);
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxDynamicSmem);
     if (e != cudaSuccess)
         return set_error(FMF_ERR_CUDA, "plain kernel shared memory (%zu bytes): %s", g.smem,
                          cudaGetErrorString(e));

@@ -460,7 +460,7 @@ int launch_window_stats(const float *data, int N, int L, int SC, const float *mu
     const size_t smem = window_stats_smem(L, full);
     void (*kern)(const float *, int, int, const float *, float *, float *) =
         full ? window_stats_kernel<true> : window_stats_kernel<false>;
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxDynamicSmem);
     if (e != cudaSuccess)
         return set_error(FMF_ERR_CUDA, "window statistics shared memory (%zu bytes): %s", smem,
                          cudaGetErrorString(e));

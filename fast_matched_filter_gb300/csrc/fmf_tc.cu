@@ -1264,7 +1264,7 @@ int tc_run(const TcProb *probs, int n, int split, unsigned long long *queue, uns
     else
         kern = norm == 0 ? tc_persistent<false, false, 0>
                          : (norm == 1 ? tc_persistent<false, false, 1> : tc_persistent<false, false, -1>);
-    e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxDynamicSmem);
     if (e != cudaSuccess)
         return set_error(FMF_ERR_CUDA, "tc_persistent shared memory (%zu bytes): %s", smem,
                          cudaGetErrorString(e));
