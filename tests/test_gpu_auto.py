@@ -111,3 +111,75 @@ def test_variable_lengths(oracle_built, normalize, lengths, expect):
 def test_auto_is_rejected_by_batches():
     with pytest.raises(fmf.FMFError):
         fmf.Batch("auto")
+
+
+def _random_case(seed):
+    """A seeded search drawn over the shapes and value ranges callers meet:
+    1-6 templates, 1-8 stations, 1-3 components, 4-700 taps (log-uniform),
+    step 1-3, 'short' or 'full', channel amplitudes 1e-3..1e3, DC offsets up
+    to 1e3 for 'full', weights normalised to sum 1 with some zero; planted
+    copies at amplitudes from 0.05 to exact (scaled by a power of two, where
+    the split products' rounding errors share a sign), on the channel's DC."""
+    rng = np.random.default_rng(1000 + seed)
+    T, S, C = int(rng.integers(1, 7)), int(rng.integers(1, 9)), int(rng.integers(1, 4))
+    L = int(np.exp(rng.uniform(np.log(4), np.log(700))))
+    step = int(rng.integers(1, 4))
+    normalize = "full" if rng.random() < 0.5 else "short"
+    N = L + int(rng.integers(2000, 40000))
+    amp = 10.0 ** rng.uniform(-3, 3, (S, C, 1))
+    dc = np.zeros((S, C, 1))
+    if normalize == "full" and rng.random() < 0.5:
+        dc = rng.uniform(-1e3, 1e3, (S, C, 1))
+    d = rng.standard_normal((S, C, N)) * amp + dc
+    tp = rng.standard_normal((T, S, C, L)) * np.hanning(L + 2)[1:-1]
+    mo = rng.integers(0, 60, (T, S, C))
+    w = rng.uniform(0, 1, (T, S, C))
+    w[rng.random((T, S, C)) < 0.15] = 0.0
+    w[:, 0, 0] += 0.1  # at least one live channel
+    w /= w.sum(axis=(1, 2), keepdims=True)
+    for t in range(T):
+        k = int(rng.integers(0, max(1, (N - L - 60) // step)))
+        scale = 2.0 ** int(rng.integers(-3, 4)) if rng.random() < 0.5 else rng.uniform(0.05, 1.0)
+        for s in range(S):
+            for c in range(C):
+                a = k * step + mo[t, s, c]
+                if a + L <= N:
+                    if scale >= 0.125 and rng.random() < 0.5:  # an exact copy (on the DC)
+                        d[s, c, a:a + L] = dc[s, c, 0] + scale * tp[t, s, c] * amp[s, c, 0]
+                    else:
+                        d[s, c, a:a + L] += scale * tp[t, s, c] * amp[s, c, 0]
+    return (tp.astype(np.float32), mo.astype(np.int32), w.astype(np.float32), d.astype(np.float32),
+            step, normalize)
+
+
+@pytest.mark.parametrize("seed", range(24))
+def test_auto_holds_the_bar_on_random_searches(seed):
+    """precision='auto' within 1e-5 of FP64 on every output of 24 random
+    searches (whichever form it picks)."""
+    tp, mo, w, d, step, normalize = _random_case(seed)
+    got = fmf.matched_filter(tp, mo, w, d, step, check_zeros=False, normalize=normalize,
+                             precision="auto")
+    ref = fp64.fp64_matched_filter(tp, mo, w, d, step, normalize, True)
+    err = np.abs(got.astype(np.float64) - ref).max()
+    assert err <= TOL, "seed %d (%s): max %.3g with %s" % (seed, normalize, err, fmf.last_precision())
+
+
+def test_full_level_shift_holds_the_bar():
+    """A quiet stretch 100 noise-sigmas away from the channel's centre (a level
+    shift): every product of a window there carries the offset, so split
+    products would err by ~1e-4 and auto runs FP32, whose error grows as
+    ~6e-8 x the offset in sigmas (4.6e-6 here); within 1e-5 of FP64."""
+    rng = np.random.default_rng(26)
+    L, N = 300, 40000
+    tp = (rng.standard_normal((2, 1, 1, L)) * np.hanning(L + 2)[1:-1]).astype(np.float32)
+    mo = np.zeros((2, 1, 1), np.int32)
+    w = np.ones((2, 1, 1), np.float32)
+    d = rng.standard_normal((1, 1, N)) * 1e-3 + 5.0
+    d[..., 20000:24000] += 0.1
+    d[0, 0, 21000:21000 + L] += 3e-3 * tp[0, 0, 0]
+    d = d.astype(np.float32)
+    got = fmf.matched_filter(tp, mo, w, d, 1, check_zeros=False, normalize="full",
+                             precision="auto")
+    assert fmf.last_precision() == "fp32"
+    ref = fp64.fp64_matched_filter(tp, mo, w, d, 1, "full", True)
+    assert np.abs(got.astype(np.float64) - ref).max() <= TOL
