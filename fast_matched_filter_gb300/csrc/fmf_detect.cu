@@ -20,25 +20,37 @@
 //            first), each peak still kept removes the peaks closer than
 //            min_separation lags on either side.
 //
-// The order statistics are exact.  Each (median, then MAD) is a sample-select:
-//   1. one block per row sorts a strided sample of the row's 32-bit
-//      order-preserving keys and brackets the two middle ranks with a key
-//      window [klo, khi] six binomial standard deviations wide;
+// The order statistics are exact, from one read of each row in the usual
+// case (a sample-select):
+//   1. one block per row sorts a strided sample of the row: the key window
+//      [klo, khi] around the two middle ranks (three binomial standard
+//      deviations wide), so the median lies in [m_lo, m_hi], the values of
+//      those keys; and from the sample's |x - m| about the window's middle, a
+//      window [a_lo, a_hi] the MAD lies in, widened by the median's own
+//      uncertainty;
 //   2. one pass over the row counts the keys below klo and gathers the keys
-//      inside the window (about 5 % of the row) into a candidate list;
-//   3. if the window holds both middle ranks, a radix selection (three passes
-//      of 11, 11 and 10 bits, each a shared-memory histogram of the keys that
-//      match the bits chosen so far) runs over the candidates only; if not --
-//      heavy ties, an adversarial row -- the same radix selection runs over
-//      the whole row.  Rows no longer than the sample are sorted whole.
-// The MAD pass's read of the row also notes the values at or above a lower
-// bound of the threshold (from the MAD window: thr = med + n_mad * mad is
-// monotone in mad) in a hot list, whose local maxima a small kernel gathers,
-// so a call reads the rows twice (median, MAD + peaks) in the usual case; rows
-// whose MAD window missed get a peak pass of their own.  Peaks are gathered
-// into a list per template (capacity kDetCap) and filtered by one thread
-// block per template: the candidates below the exact threshold dropped, a
-// sort by lag, a sort by height, and the greedy distance filter.
+//      inside [klo, khi] (about 2.5 % of the row), and classifies every value
+//      for the MAD before the median is known: |x - m| < a_lo for every m in
+//      [m_lo, m_hi] (counted), |x - m| > a_hi for every such m (dropped), or
+//      either (listed: about 10 % of a Gaussian row); the same read notes the
+//      values at or above a lower bound of the threshold
+//      (m_lo + n_mad * a_lo: thr = med + n_mad * mad is monotone in both);
+//   3. the median: if the window holds both middle ranks, a radix selection
+//      over the candidates (passes of up to 11 bits over the key bits the
+//      window's keys do not share, each a shared-memory histogram of the keys
+//      that match the bits chosen so far); if not -- heavy ties, an
+//      adversarial row -- the same selection over the whole row;
+//   4. the MAD: the sample keyed by |x - med| narrows [a_lo, a_hi]; the listed
+//      values keyed by |x - med| are counted below the window or gathered in
+//      it, and selected as in 3.  A row whose median or MAD window missed, or
+//      whose list overflowed, selects its MAD over the whole row and takes its
+//      peaks in a pass of its own.  Rows no longer than the sample are sorted
+//      whole.
+// The values noted in step 2 are examined by a small kernel for the local
+// maximum and plateau rules: a superset of the peaks, gathered into a list
+// per template (capacity kDetCap) and filtered by one thread block per
+// template: the candidates below the exact threshold dropped, a sort by lag,
+// a sort by height, and the greedy distance filter.
 //
 // Every launch is stream-ordered and the state lives on the device, so a
 // detection run needs no host round trip and can be captured in a graph.
@@ -57,6 +69,7 @@ constexpr int kDetSelectThreads = 1024;   // per-template filter kernel
 constexpr int kDetChunk = 1024;           // templates per round of scratch
 constexpr int kDetCap = 16384;            // candidate peaks per template row
 constexpr int kDetSample = 16384;         // sampled keys per row (sample-select)
+constexpr int kDetBlocks = 152 * 8 * 8;   // blocks of a row pass: 8 waves of 8 per SM
 
 // source of a row's radix selection
 constexpr int kSrcRow = 0;   // the row itself (fallback)
@@ -67,14 +80,36 @@ struct DetState {
     int begin, end;        // lag window of the row
     unsigned prefix[2];    // key bits chosen so far for the lower / upper middle rank
     int rank[2];           // rank still to find inside the chosen bucket
+    int top;               // key bits below the window's common high bits (0..32)
     float med, mad, thr;
     int n_cand;            // local maxima at or above thr (may exceed the capacity)
-    float thr_lo;          // a lower bound of thr known before the MAD pass
-    int peaks_ready;       // 1: the MAD counting pass noted the values >= thr_lo
+    float thr_lo;          // a lower bound of thr known before the counting pass
+    int peaks_ready;       // 1: the counting pass noted the values >= thr_lo
     int n_hot;             // values >= thr_lo noted (may exceed the capacity)
     int src;               // kSrcRow / kSrcCand / kSrcDone
-    unsigned klo, khi;     // sample window of the keys
+    unsigned klo, khi;     // key window of the current selection
     int n_lt, n_in;        // keys below klo, keys inside [klo, khi]
+    // the MAD classes of the counting pass (one_read = 1): the median lies in
+    // [m_lo, m_hi] and the MAD in [a_lo, a_hi] when both windows hold
+    int one_read;
+    float m_lo, m_hi, a_lo, a_hi;
+    int has_below;         // [kb0, kb1] is not empty
+    unsigned kb0, kb1;     // value keys with |x - m| < a_lo for every m in [m_lo, m_hi]
+    unsigned kn0, kn1;     // value keys with |x - m| <= a_hi for some m in [m_lo, m_hi]
+    int n_below;           // values in [kb0, kb1]
+    int over_k, over_a;    // a lane's column of candidates / undecided values overflowed
+};
+
+// The lists of a row are written in columns, one per thread of the counting
+// pass, so that appending takes no scan and no shared counter: thread l of
+// warp w of block b puts its k-th entry at list + t * cap + ((b * 8 + w) *
+// (C + 1) + k) * 32 + (l & 31), up to C entries (row C of the warp's region
+// takes the overflow, unread), and its count at cnt[(t * S + b) * 256 + l].
+// Equal counts across a warp make coalesced stores and loads.
+struct Lanes {
+    int S;                 // counting blocks per row
+    int Ck, Ca;            // column capacity: candidates of a selection / undecided values
+    int *cnt_k, *cnt_a;    // entries per column (may exceed the capacity)
 };
 
 // Order-preserving image of a float: a < b  <=>  key(a) < key(b) (for non-NaN
@@ -90,13 +125,23 @@ __device__ __forceinline__ float key_value(unsigned k)
     return __uint_as_float((k & 0x80000000u) ? (k & 0x7fffffffu) : ~k);
 }
 
-// Digit of pass p: bits [shift, shift + width) of the key.
-__device__ __forceinline__ int pass_shift(int p) { return p == 0 ? 21 : (p == 1 ? 10 : 0); }
-__device__ __forceinline__ unsigned pass_bins(int p) { return p == 2 ? 1024u : 2048u; }
-__device__ __forceinline__ unsigned pass_high_mask(int p)
+// Digit of selection pass p over the low `top` bits of the keys (the bits
+// above are common to every key selected among): up to 11 bits at a time from
+// the top; width 0 once the key is complete.
+__device__ __forceinline__ void pass_digit(int top, int p, int &shift, int &width)
 {
-    return p == 0 ? 0u : (p == 1 ? 0xffe00000u : 0xfffffc00u);
+    int hi = top;
+    shift = hi;
+    width = 0;
+    for (int q = 0; q <= p; q++) {
+        width = hi < 11 ? hi : 11;
+        shift = hi - width;
+        hi = shift;
+    }
 }
+
+// The bits at and above `bit` (none for bit 32).
+__device__ __forceinline__ unsigned above_mask(int bit) { return bit >= 32 ? 0u : ~0u << bit; }
 
 // Split of a row at its first 16-byte boundary: `head` scalar elements, then
 // `nvec` float4s, then `tail` scalar elements.
@@ -133,6 +178,7 @@ __global__ void det_init_kernel(DetState *__restrict__ st, int T, int n_corr,
     s.prefix[0] = s.prefix[1] = 0u;
     s.rank[0] = n > 0 ? (n - 1) / 2 : 0;
     s.rank[1] = n / 2;
+    s.top = 32;
     s.med = s.mad = s.thr = __int_as_float(0x7fc00000);  // NaN until computed
     s.n_cand = 0;
     s.thr_lo = __int_as_float(0x7fc00000);
@@ -141,6 +187,12 @@ __global__ void det_init_kernel(DetState *__restrict__ st, int T, int n_corr,
     s.src = kSrcRow;
     s.klo = s.khi = 0u;
     s.n_lt = s.n_in = 0;
+    s.one_read = 0;
+    s.m_lo = s.m_hi = s.a_lo = s.a_hi = 0.0f;
+    s.has_below = 0;
+    s.kb0 = s.kb1 = s.kn0 = s.kn1 = 0u;
+    s.n_below = 0;
+    s.over_k = s.over_a = 0;
     st[t] = s;
 }
 
@@ -167,134 +219,281 @@ __device__ __forceinline__ void finish_select(DetState &s, int mode, float v, fl
     }
 }
 
-// The key of rank r (0-based, ascending) among the first P keys of sk, by the
-// block: three radix passes (11, 11 and 10 bits), each a shared-memory
-// histogram of the keys that match the bits chosen so far, then one warp
-// finding the bucket that holds the rank.  All threads of the block call it.
-__device__ unsigned block_select(const unsigned *sk, int P, int r, unsigned *hist, int *shared_pick)
+// The keys of ranks r0 <= r1 (0-based, ascending) among the first P keys of
+// sk, by the block: three radix passes (11, 11 and 10 bits), each a
+// shared-memory histogram per rank of the keys that match that rank's bits so
+// far (one histogram while both ranks share them; warp-aggregated in the
+// first pass, whose digits sampled keys mostly share), then one warp per rank
+// finding the bucket that holds it.  All threads of the block call it.
+__device__ void block_select2(const unsigned *sk, int P, int r0, int r1, unsigned *hist, int *pick,
+                              unsigned &k0, unsigned &k1)
 {
-    unsigned prefix = 0u;
+    unsigned pre[2] = {0u, 0u};
+    int r[2] = {r0, r1};
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (int pass = 0; pass < 3; pass++) {
-        const int shift = pass_shift(pass);
-        const unsigned bins = pass_bins(pass), high = pass_high_mask(pass);
-        for (int i = threadIdx.x; i < (int)bins; i += blockDim.x)
+        int shift, width;
+        pass_digit(32, pass, shift, width);
+        const unsigned dmask = (1u << width) - 1u, high = above_mask(shift + width);
+        const bool two = pre[0] != pre[1];
+        for (int i = threadIdx.x; i < 2 * kDetBins; i += blockDim.x)
             hist[i] = 0u;
         __syncthreads();
-        for (int i = threadIdx.x; i < P; i += blockDim.x) {
-            const unsigned k = sk[i];
-            if ((k & high) == prefix)
-                atomicAdd(&hist[(k >> shift) & (bins - 1u)], 1u);
+        for (int i0 = 0; i0 < P; i0 += blockDim.x) {  // every lane runs every step
+            const int i = i0 + threadIdx.x;
+            const unsigned k = i < P ? sk[i] : 0u;
+            const unsigned dig = (k >> shift) & dmask;
+            for (int q = 0; q < (two ? 2 : 1); q++) {
+                const bool m = i < P && (k & high) == pre[q];
+                if (pass == 0) {
+                    const unsigned g = __match_any_sync(0xffffffffu, m ? dig : 0xffffffffu);
+                    if (m && (__ffs(g) - 1) == lane)
+                        atomicAdd(&hist[q * kDetBins + dig], __popc(g));
+                } else if (m) {
+                    atomicAdd(&hist[q * kDetBins + dig], 1u);
+                }
+            }
         }
         __syncthreads();
-        if (threadIdx.x < 32) {
-            const int lane = threadIdx.x, per = (int)bins / 32;
+        if (warp < 2) {
+            const unsigned *h = hist + (two ? warp : 0) * kDetBins;
+            const int per = kDetBins / 32;
             unsigned sum = 0;
             for (int i = 0; i < per; i++)
-                sum += hist[lane * per + i];
+                sum += h[lane * per + i];
             unsigned inc = sum;
             for (int o = 1; o < 32; o <<= 1) {
                 const unsigned y = __shfl_up_sync(0xffffffffu, inc, o);
                 if (lane >= o)
                     inc += y;
             }
-            const unsigned exc = inc - sum;
-            if ((unsigned)r >= exc && (unsigned)r < inc) {
+            const unsigned exc = inc - sum, rk = (unsigned)(warp == 0 ? r[0] : r[1]);
+            if (rk >= exc && rk < inc) {
                 unsigned c = exc;
                 int i = 0;
                 for (; i < per - 1; i++) {
-                    if ((unsigned)r < c + hist[lane * per + i])
+                    if (rk < c + h[lane * per + i])
                         break;
-                    c += hist[lane * per + i];
+                    c += h[lane * per + i];
                 }
-                shared_pick[0] = lane * per + i;
-                shared_pick[1] = (int)c;
+                pick[2 * warp] = lane * per + i;
+                pick[2 * warp + 1] = (int)c;
             }
         }
         __syncthreads();
-        prefix |= (unsigned)shared_pick[0] << shift;
-        r -= shared_pick[1];
+        for (int q = 0; q < 2; q++) {
+            pre[q] |= (unsigned)pick[2 * q] << shift;
+            r[q] -= pick[2 * q + 1];
+        }
         __syncthreads();
     }
-    return prefix;
+    k0 = pre[0];
+    k1 = pre[1];
 }
 
-// Step 1 of the sample-select (one block per row): a strided sample of the
-// row's keys, sorted; either the exact answer (row no longer than the
-// sample) or the key window around the two middle ranks.
+// |x - m| in float32, as numpy computes the MAD's deviations.
+__device__ __forceinline__ float dev(float x, float m) { return fabsf(__fsub_rn(x, m)); }
+
+// |x - m| < a for every float m in [m_lo, m_hi]: |x - m| falls, then rises,
+// in m (float rounding keeps both monotone), so the larger of the ends.
+__device__ __forceinline__ bool below_all(float x, float m_lo, float m_hi, float a)
+{
+    return dev(x, m_lo) < a && dev(x, m_hi) < a;
+}
+
+// |x - m| <= a for some float m in [m_lo, m_hi]: 0 inside, else the nearer end.
+__device__ __forceinline__ bool near_some(float x, float m_lo, float m_hi, float a)
+{
+    if (x < m_lo)
+        return __fsub_rn(m_lo, x) <= a;
+    if (x > m_hi)
+        return __fsub_rn(x, m_hi) <= a;
+    return x == x;  // inside (NaN is not)
+}
+
+// Both predicates hold on an interval of values (a sublevel set of a
+// function that falls, then rises): its first and last keys, from a key c
+// inside it, by bisection.
+template <class F>
+__device__ unsigned first_key(unsigned c, F pred)
+{
+    unsigned long long lo = 0, hi = c;  // pred false..true on [0, c], true at c
+    while (lo < hi) {
+        const unsigned long long mid = (lo + hi) >> 1;
+        if (pred(key_value((unsigned)mid)))
+            hi = mid;
+        else
+            lo = mid + 1;
+    }
+    return (unsigned)hi;
+}
+template <class F>
+__device__ unsigned last_key(unsigned c, F pred)
+{
+    unsigned long long lo = c, hi = 0xffffffffull;  // pred true..false on [c, 2^32)
+    while (lo < hi) {
+        const unsigned long long mid = (lo + hi + 1) >> 1;
+        if (pred(key_value((unsigned)mid)))
+            lo = mid;
+        else
+            hi = mid - 1;
+    }
+    return (unsigned)lo;
+}
+
+// Step 1 and 4 of the sample-select (one block per row).  Mode 0: a strided
+// sample of the row (kept in `saved`), sorted: the exact median and MAD for a
+// row no longer than the sample; else the median's key window, the MAD's
+// window about the median window's middle, and the MAD classes of the
+// counting pass.  Mode 1 (the median now exact): the sample keyed by
+// |x - med| narrows the MAD window for the listed values; rows that cannot
+// use the list select their MAD over the whole row.
+constexpr int kPad = 3 * 64 + 16;  // sample positions either side of the middle ranks
+
 __global__ void __launch_bounds__(1024)
 det_sample_kernel(const float *__restrict__ cc, size_t ld, DetState *__restrict__ st, int mode,
                   float n_mad, float *__restrict__ saved)
 {
     extern __shared__ unsigned long long sample_smem[];
     unsigned *sk = reinterpret_cast<unsigned *>(sample_smem);  // kDetSample keys
+    __shared__ unsigned hist[2 * kDetBins];
+    __shared__ int pick[4];
     const int t = blockIdx.x;
-    DetState s = st[t];
-    const long long n = s.end - s.begin;
+    const int begin = st[t].begin;
+    const long long n = st[t].end - begin;
     if (n <= 0)
         return;
-    const float *row = cc + (size_t)t * ld + s.begin;
+    const float *row = cc + (size_t)t * ld + begin;
     const int m = n < kDetSample ? (int)n : kDetSample;
     int P = 1;
     while (P < m)
         P <<= 1;
-    // sample positions floor(i * n / m) from a fixed-point step (no 64-bit division
-    // per sample); any spread of positions serves, the selection is exact.  The
-    // median pass gathers the sampled values from the row (scattered reads) and
-    // keeps them in `saved`; the MAD pass reads them back contiguously.
-    const unsigned long long stepq = ((unsigned long long)n << 20) / (unsigned long long)m;
+    const long long a = (n - 1) / 2, b = n / 2;
     float *sv = saved + (size_t)t * kDetSample;
+    const float med = st[t].med;  // mode 1: exact
+    // thread 0 alone updates the row's state, at the end (fields read here, at the top,
+    // by every thread, are not written)
+    auto whole_row_mad = [&]() {  // the MAD over the whole row, the peaks by a pass of their own
+        DetState s = st[t];
+        s.src = kSrcRow;
+        s.top = 32;
+        s.prefix[0] = s.prefix[1] = 0u;
+        s.rank[0] = (int)a;
+        s.rank[1] = (int)b;
+        s.peaks_ready = 0;
+        st[t] = s;
+    };
+    if (mode == 1) {
+        const bool whole = m == n;  // sorted whole by the median's sample
+        const bool list = !whole && st[t].one_read && !st[t].over_a && med >= st[t].m_lo &&
+                          med <= st[t].m_hi;
+        if (!whole && !list) {
+            if (threadIdx.x == 0)
+                whole_row_mad();
+            return;
+        }
+    }
+    // sample positions floor(i * n / m) from a fixed-point step (no 64-bit division
+    // per sample); any spread of positions serves, the selection is exact
+    const unsigned long long stepq = ((unsigned long long)n << 20) / (unsigned long long)m;
     for (int i = threadIdx.x; i < P; i += blockDim.x) {
-        unsigned key = 0xffffffffu;
+        unsigned key = 0xffffffffu;  // padding: ranks last
         if (i < m) {
             float v;
             if (mode == 0) {
-                long long pos = (long long)(((unsigned long long)i * stepq) >> 20);
+                const long long pos = (long long)(((unsigned long long)i * stepq) >> 20);
                 v = row[pos < n ? pos : n - 1];
                 sv[i] = v;
             } else {
                 v = sv[i];
             }
-            key = sel_key(v, mode, s.med);
+            key = order_key(mode == 0 ? v : dev(v, med));
         }
         sk[i] = key;
     }
     __syncthreads();
-    // two order statistics of the sample (the padding keys, all ones, rank last):
-    // the exact middle values when the sample is the whole row; otherwise the keys
-    // bracketing the two middle ranks -- the sample position of rank r is about
-    // r*m/n, with a binomial standard deviation of at most sqrt(m)/2 = 64 positions:
-    // bracket by 6 of them
-    __shared__ unsigned hist[kDetBins];
-    __shared__ int pick[2];
-    const long long a = (n - 1) / 2, b = n / 2;
-    constexpr int kPad = 6 * 64 + 16;
+    // ranks of the window: the sample position of rank r is about r*m/n, with a
+    // binomial standard deviation of at most sqrt(m)/2 = 64 positions
     const long long pa = a * m / n, pb = (b * m + n - 1) / n;
     const int r0 = m == n ? (int)a : (int)(pa - kPad > 0 ? pa - kPad : 0);
     const int r1 = m == n ? (int)b : (int)(pb + kPad < m - 1 ? pb + kPad : m - 1);
-    const unsigned k0 = block_select(sk, P, r0, hist, pick);
-    const unsigned k1 = r1 == r0 ? k0 : block_select(sk, P, r1, hist, pick);
+    unsigned k0, k1;
+    block_select2(sk, P, r0, r1, hist, pick, k0, k1);
+    if (m == n) {  // the whole row: exact
+        if (threadIdx.x == 0) {
+            DetState s = st[t];
+            finish_select(s, mode, middle_value(k0, k1, (int)n), n_mad);
+            s.src = kSrcDone;
+            s.one_read = 0;
+            s.peaks_ready = 0;
+            st[t] = s;
+        }
+        return;
+    }
+    if (mode == 1) {  // the listed values' window: the sample's, inside [a_lo, a_hi]
+        if (threadIdx.x == 0) {
+            const unsigned klo = max(k0, order_key(st[t].a_lo)), khi = min(k1, order_key(st[t].a_hi));
+            if (klo > khi) {  // cannot hold the MAD: the whole row
+                whole_row_mad();
+            } else {
+                DetState s = st[t];
+                s.klo = klo;
+                s.khi = khi;
+                s.src = kSrcCand;
+                s.n_lt = s.n_below;
+                s.n_in = 0;
+                s.over_k = 0;
+                st[t] = s;
+            }
+        }
+        return;
+    }
+    // mode 0: the median lies in [m_lo, m_hi] if the window holds; the sample's
+    // deviations from its middle give the MAD's window, widened by how far the
+    // median can be from that middle
+    // window ends without -0 (x + 0 is +0 for x = -0): the counting pass compares
+    // floats, where -0 and +0 are one value, and keys its candidates as x + 0
+    const float m_lo = __fadd_rn(key_value(k0), 0.0f), m_hi = __fadd_rn(key_value(k1), 0.0f);
+    const float mid = __fadd_rn(__fmul_rn(0.5f, m_lo), __fmul_rn(0.5f, m_hi));
+    __syncthreads();  // every thread is past its last read of the value keys
+    for (int i = threadIdx.x; i < P; i += blockDim.x)
+        sk[i] = i < m ? order_key(dev(sv[i], mid)) : 0xffffffffu;
+    __syncthreads();
+    unsigned ka0, ka1;
+    block_select2(sk, P, r0, r1, hist, pick, ka0, ka1);
     if (threadIdx.x != 0)
         return;
-    s.prefix[0] = s.prefix[1] = 0u;
-    s.rank[0] = (int)a;
-    s.rank[1] = (int)b;
+    DetState s = st[t];
+    s.klo = order_key(m_lo);
+    s.khi = order_key(m_hi);
+    s.src = kSrcCand;
     s.n_lt = s.n_in = 0;
-    if (m == n) {  // the whole row
-        finish_select(s, mode, middle_value(k0, k1, (int)n), n_mad);
-        s.src = kSrcDone;
-    } else {
-        s.klo = k0;
-        s.khi = k1;
-        s.src = kSrcCand;
-        if (mode == 1) {
-            // thr = med + n_mad * mad rises with mad (for n_mad >= 0; falls otherwise) and
-            // float rounding keeps that order, so a MAD inside the window [klo, khi] gives
-            // thr >= thr_lo: the counting pass gathers the local maxima >= thr_lo, a
-            // superset of the peaks, and the filter keeps those >= thr
-            const float d = key_value(n_mad >= 0.0f ? k0 : k1);
-            s.thr_lo = __fadd_rn(s.med, __fmul_rn(n_mad, d));
-            s.peaks_ready = 1;
+    s.n_below = 0;
+    s.over_k = s.over_a = 0;
+    const float wide = fmaxf(__fsub_rn(mid, m_lo), __fsub_rn(m_hi, mid));
+    const float a_lo = fmaxf(__fsub_rn(key_value(ka0), wide), 0.0f);
+    const float a_hi = __fadd_rn(key_value(ka1), wide);
+    s.one_read = isfinite(m_lo) && isfinite(m_hi) && isfinite(a_lo) && isfinite(a_hi);
+    if (s.one_read) {
+        s.m_lo = m_lo;
+        s.m_hi = m_hi;
+        s.a_lo = a_lo;
+        s.a_hi = a_hi;
+        auto near = [&](float x) { return near_some(x, m_lo, m_hi, a_hi); };
+        s.kn0 = first_key(order_key(m_lo), near);
+        s.kn1 = last_key(order_key(m_lo), near);
+        auto below = [&](float x) { return below_all(x, m_lo, m_hi, a_lo); };
+        s.has_below = below(mid);  // the middle minimises the larger distance
+        if (s.has_below) {
+            s.kb0 = first_key(order_key(mid), below);
+            s.kb1 = last_key(order_key(mid), below);
         }
+        // thr = med + n_mad * mad rises with med and with mad (for n_mad >= 0; falls
+        // with mad otherwise) and float rounding keeps that order, so med >= m_lo and
+        // a MAD in [a_lo, a_hi] give thr >= thr_lo: the counting pass notes the values
+        // >= thr_lo, whose local maxima are a superset of the peaks
+        s.thr_lo = __fadd_rn(m_lo, __fmul_rn(n_mad, n_mad >= 0.0f ? a_lo : a_hi));
+        s.peaks_ready = s.thr_lo == s.thr_lo;
     }
     st[t] = s;
 }
@@ -329,150 +528,174 @@ __device__ __forceinline__ void note_hot(DetState *st, int t, long long o, int *
         hot[(size_t)t * cap + slot] = (int)o;
 }
 
-// Step 2: one pass over the row: keys below klo counted, keys inside
-// [klo, khi] appended to the row's candidate list (up to cap).  In the MAD
-// pass (mode 1, PEAKS) the same read notes the offsets of the values at or
-// above thr_lo in the row's hot list, so that no third read of the row is
-// needed for the peaks.
-template <bool PEAKS>
-__global__ void __launch_bounds__(kDetThreads, 4)  // 32 warps per SM: enough loads in flight
+// Step 2, the one read of a row (ROW = true): values below the median window
+// counted, values inside it appended to the thread's candidate column; the
+// MAD classes (values in [b_lo, b_hi] counted, values in [n_lo, n_hi] outside
+// it appended to the thread's column of undecided values); the offsets of the
+// values at or above thr_lo noted in the row's hot list.  ROW = false, step 4:
+// each thread walks its own column of undecided values keyed |x - med|: below
+// the window counted, inside it appended to its candidate column.  Windows
+// are compared as floats (rows are free of NaN; -0 compares as +0, and the
+// readers key a candidate x as x + 0).  The per-value work is predicated, with
+// no branch: the pass stays at the rate of the row's read.
+template <bool ROW>
+__global__ void __launch_bounds__(kDetThreads, 3)  // 24 warps per SM, 16 values per lane in flight
 det_count_kernel(const float *__restrict__ cc, size_t ld, DetState *__restrict__ st,
-                 unsigned *__restrict__ cand, long long cap, int mode, int *__restrict__ hot,
-                 int hcap)
+                 float *__restrict__ cand, long long cap, float *__restrict__ amb, long long amb_cap,
+                 Lanes g, int *__restrict__ hot, int hcap)
 {
     const int t = blockIdx.y;
-    const int src = st[t].src;
-    const long long n = st[t].end - st[t].begin;
-    if (src != kSrcCand || n <= 0)
-        return;
-    const unsigned klo = st[t].klo, khi = st[t].khi;
-    const float med = st[t].med;
-    const bool peaks = PEAKS && mode == 1 && st[t].peaks_ready != 0;
-    const float thr_lo = st[t].thr_lo;
-    const float *row = cc + (size_t)t * ld + st[t].begin;
-    unsigned *list = cand + (size_t)t * cap;
+    if (st[t].src != kSrcCand)
+        return;  // uniform over the block
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    constexpr int kWarps = kDetThreads / 32;
-    unsigned lt = 0;  // per-lane count of keys below klo
-    // One warp step: each lane's up to 16 keys; the keys inside the window are
-    // appended with one atomic per warp (a warp prefix sum places them).
-    constexpr int kK = 16;
-    const unsigned width = khi - klo;  // key - klo <= width  <=>  klo <= key <= khi
-    // a lane's keys inside the window wait here (its own column), so that only
-    // the few candidates are written out, in a loop over the set bits
-    __shared__ unsigned stash[kWarps][kK][32];
-    auto take = [&](const unsigned (&key)[kK], const bool (&ok)[kK], auto all_ok) {
-        constexpr bool ALL = decltype(all_ok)::value;  // every key of the step is in the row
-        unsigned in_mask = 0;
-#pragma unroll
-        for (int u = 0; u < kK; u++) {
-            const bool o = ALL || ok[u];
-            lt += (o && key[u] < klo) ? 1u : 0u;
-            if (o && key[u] - klo <= width) {
-                in_mask |= 1u << u;
-                stash[warp][u][lane] = key[u];
-            }
-        }
-        const int cnt = __popc(in_mask);
-        int inc = cnt;
-        for (int o = 1; o < 32; o <<= 1) {
-            const int y = __shfl_up_sync(0xffffffffu, inc, o);
-            if (lane >= o)
-                inc += y;
-        }
-        const int total = __shfl_sync(0xffffffffu, inc, 31);
-        if (total == 0)
-            return;
-        int base = 0;
-        if (lane == 31)
-            base = atomicAdd(&st[t].n_in, total);
-        base = __shfl_sync(0xffffffffu, base, 31);
-        long long pos = (long long)base + inc - cnt;
-        for (unsigned m = in_mask; m; m &= m - 1u, pos++)
-            if (pos < cap)
-                list[pos] = stash[warp][__ffs(m) - 1][lane];
-    };
-    const RowSplit rs = split_row(row, n);
-    if (blockIdx.x == 0 && warp == 0) {
-        unsigned key[kK];
-        bool ok[kK];
-        const long long i = lane < rs.head ? lane : rs.head + 4 * rs.nvec + (lane - rs.head);
-        ok[0] = lane < rs.head + rs.tail;
-        const float x = ok[0] ? row[i] : 0.0f;
-        key[0] = ok[0] ? sel_key(x, mode, med) : 0u;
-        if (peaks && ok[0] && x >= thr_lo)
-            note_hot(st, t, i, hot, hcap);
-#pragma unroll
-        for (int u = 1; u < kK; u++) {
-            ok[u] = false;
-            key[u] = 0u;
-        }
-        take(key, ok, std::false_type{});
-    }
-    const float4 *vrow = reinterpret_cast<const float4 *>(row + rs.head);
-    const long long steps = (rs.nvec + 127) / 128;  // 128 float4s per warp step
-    const long long cstride = (long long)gridDim.x * kWarps;
-    auto load4 = [&](long long c, float4 (&v)[4]) {
-#pragma unroll
-        for (int u = 0; u < 4; u++) {
-            const long long i = c * 128 + u * 32 + lane;
-            v[u] = (c < steps && i < rs.nvec) ? vrow[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const size_t col = ((size_t)t * g.S + blockIdx.x) * kDetThreads + threadIdx.x;
+    const size_t region = (size_t)blockIdx.x * (kDetThreads / 32) + warp;
+    float *kc = cand + (size_t)t * cap + region * (size_t)(g.Ck + 1) * 32 + lane;
+    float *ac = amb + (size_t)t * amb_cap + region * (size_t)(g.Ca + 1) * 32 + lane;
+    const float lo = key_value(st[t].klo), hi = key_value(st[t].khi);
+    const float med = st[t].med;
+    const bool classes = ROW && st[t].one_read;
+    const bool has_below = classes && st[t].has_below;
+    const float b_lo = key_value(st[t].kb0), b_hi = key_value(st[t].kb1);
+    const float n_lo = key_value(st[t].kn0), n_hi = key_value(st[t].kn1);
+    const bool peaks = ROW && st[t].peaks_ready;
+    const float thr_lo = st[t].thr_lo;
+    unsigned lt = 0, nb = 0;
+    int nk = 0, na = 0;  // entries of this thread's columns (past the capacity: row C, unread)
+    auto take = [&](float x, bool ok) {
+        lt += (unsigned)(ok & (x < lo));
+        const bool in = ok & (x >= lo) & (x <= hi);
+        if (in)
+            kc[(size_t)min(nk, g.Ck) * 32] = x;
+        nk += (int)in;
+        if constexpr (ROW) {
+            const bool below = has_below & ok & (x >= b_lo) & (x <= b_hi);
+            nb += (unsigned)below;
+            const bool un = classes & ok & !below & (x >= n_lo) & (x <= n_hi);
+            if (un)
+                ac[(size_t)min(na, g.Ca) * 32] = x;
+            na += (int)un;
         }
     };
-    float4 nv[4];
-    long long c = (long long)blockIdx.x * kWarps + warp;
-    load4(c, nv);
-    for (; c < steps; c += cstride) {
-        unsigned key[kK];
-        bool ok[kK];
-        float4 v[4];
-#pragma unroll
-        for (int u = 0; u < 4; u++)
-            v[u] = nv[u];
-        load4(c + cstride, nv);  // the next step's values are in flight while this one is counted
-        if (peaks) {  // values at or above thr_lo (rare)
+    if constexpr (ROW) {
+        const float *row = cc + (size_t)t * ld + st[t].begin;
+        const long long n = st[t].end - st[t].begin;
+        const RowSplit rs = split_row(row, n);
+        if (blockIdx.x == 0 && warp == 0) {  // the unaligned ends, at most 3 + 3 values
+            const long long i = lane < rs.head ? lane : rs.head + 4 * rs.nvec + (lane - rs.head);
+            const bool ok = lane < rs.head + rs.tail;
+            const float x = ok ? row[i] : 0.0f;
+            if (peaks && ok && x >= thr_lo)
+                note_hot(st, t, i, hot, hcap);
+            take(x, ok);
+        }
+        const float4 *vrow = reinterpret_cast<const float4 *>(row + rs.head);
+        const long long steps = (rs.nvec + 127) / 128;  // 128 float4s per warp step
+        const long long cstride = (long long)gridDim.x * (kDetThreads / 32);
+        auto load4 = [&](long long c, float4 (&v)[4]) {
 #pragma unroll
             for (int u = 0; u < 4; u++) {
-                const long long q = c * 128 + u * 32 + lane;
-                const float mx = fmaxf(fmaxf(v[u].x, v[u].y), fmaxf(v[u].z, v[u].w));
-                if (q < rs.nvec && mx >= thr_lo) {
-                    const long long o = rs.head + 4 * q;
-                    if (v[u].x >= thr_lo)
-                        note_hot(st, t, o, hot, hcap);
-                    if (v[u].y >= thr_lo)
-                        note_hot(st, t, o + 1, hot, hcap);
-                    if (v[u].z >= thr_lo)
-                        note_hot(st, t, o + 2, hot, hcap);
-                    if (v[u].w >= thr_lo)
-                        note_hot(st, t, o + 3, hot, hcap);
+                const long long i = c * 128 + u * 32 + lane;
+                v[u] = (c < steps && i < rs.nvec) ? vrow[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+            }
+        };
+        float4 nv[4];
+        long long c = (long long)blockIdx.x * (kDetThreads / 32) + warp;
+        load4(c, nv);
+        for (; c < steps; c += cstride) {
+            float4 v[4];
+#pragma unroll
+            for (int u = 0; u < 4; u++)
+                v[u] = nv[u];
+            load4(c + cstride, nv);  // the next step's values are in flight while this one is counted
+            // values at or above thr_lo (rare): one vote per step on the lanes' largest
+            // values (the zeros loaded past the row's end can only cost the slow path)
+            float mx = -INFINITY;
+#pragma unroll
+            for (int u = 0; u < 4; u++)
+                mx = fmaxf(mx, fmaxf(fmaxf(v[u].x, v[u].y), fmaxf(v[u].z, v[u].w)));
+            if (peaks && __any_sync(0xffffffffu, mx >= thr_lo)) {
+#pragma unroll
+                for (int u = 0; u < 4; u++) {
+                    const long long q = c * 128 + u * 32 + lane;
+                    const float m4 = fmaxf(fmaxf(v[u].x, v[u].y), fmaxf(v[u].z, v[u].w));
+                    if (q < rs.nvec && m4 >= thr_lo) {
+                        const long long o = rs.head + 4 * q;
+                        if (v[u].x >= thr_lo)
+                            note_hot(st, t, o, hot, hcap);
+                        if (v[u].y >= thr_lo)
+                            note_hot(st, t, o + 1, hot, hcap);
+                        if (v[u].z >= thr_lo)
+                            note_hot(st, t, o + 2, hot, hcap);
+                        if (v[u].w >= thr_lo)
+                            note_hot(st, t, o + 3, hot, hcap);
+                    }
+                }
+            }
+            if (c * 128 + 128 <= rs.nvec) {  // a whole step inside the row (warp-uniform)
+#pragma unroll
+                for (int u = 0; u < 4; u++) {
+                    take(v[u].x, true);
+                    take(v[u].y, true);
+                    take(v[u].z, true);
+                    take(v[u].w, true);
+                }
+            } else {
+#pragma unroll
+                for (int u = 0; u < 4; u++) {
+                    const bool ok = c * 128 + u * 32 + lane < rs.nvec;
+                    take(v[u].x, ok);
+                    take(v[u].y, ok);
+                    take(v[u].z, ok);
+                    take(v[u].w, ok);
                 }
             }
         }
+    } else {
+        // this thread's own column of undecided values, four loads in flight
+        const int m = min(g.cnt_a[col], g.Ca);
+        const int mw = __reduce_max_sync(0xffffffffu, m);
+        for (int k = 0; k < mw; k += 4) {
+            float x[4];
 #pragma unroll
-        for (int u = 0; u < 4; u++) {
-            const bool okv = c * 128 + u * 32 + lane < rs.nvec;
-            key[4 * u + 0] = sel_key(v[u].x, mode, med);
-            key[4 * u + 1] = sel_key(v[u].y, mode, med);
-            key[4 * u + 2] = sel_key(v[u].z, mode, med);
-            key[4 * u + 3] = sel_key(v[u].w, mode, med);
-            ok[4 * u + 0] = ok[4 * u + 1] = ok[4 * u + 2] = ok[4 * u + 3] = okv;
+            for (int j = 0; j < 4; j++)
+                x[j] = k + j < m ? ac[(size_t)(k + j) * 32] : 0.0f;
+#pragma unroll
+            for (int j = 0; j < 4; j++)
+                take(dev(x[j], med), k + j < m);
         }
-        if (c * 128 + 128 <= rs.nvec)  // a whole step inside the row (warp-uniform)
-            take(key, ok, std::true_type{});
-        else
-            take(key, ok, std::false_type{});
     }
-    for (int o = 16; o > 0; o >>= 1)
+    g.cnt_k[col] = nk;
+    if (ROW)
+        g.cnt_a[col] = na;
+    const bool over_k = __any_sync(0xffffffffu, nk > g.Ck);
+    const bool over_a = ROW && __any_sync(0xffffffffu, na > g.Ca);
+    const int sum_k = __reduce_add_sync(0xffffffffu, (unsigned)nk);
+    for (int o = 16; o > 0; o >>= 1) {
         lt += __shfl_down_sync(0xffffffffu, lt, o);
-    if (lane == 0 && lt)
-        atomicAdd(&st[t].n_lt, (int)lt);
+        nb += __shfl_down_sync(0xffffffffu, nb, o);
+    }
+    if (lane == 0) {
+        if (lt)
+            atomicAdd(&st[t].n_lt, (int)lt);
+        if (nb)
+            atomicAdd(&st[t].n_below, (int)nb);
+        if (sum_k)
+            atomicAdd(&st[t].n_in, sum_k);
+        if (over_k)
+            atomicOr(&st[t].over_k, 1);
+        if (over_a)
+            atomicOr(&st[t].over_a, 1);
+    }
 }
 
-// Step 3: does the window hold both middle ranks?  Then select among the
-// candidates; else fall back to the whole row -- and in the MAD pass, leave
-// the peaks to a pass of their own (the gathered superset may miss some, or
-// have overflowed its list).
-__global__ void det_check_kernel(DetState *__restrict__ st, int T, long long cap, int mode, int pcap)
+// Step 3 (and 4): does the window hold both middle ranks?  Then select among
+// the candidates, over the key bits they do not share; else fall back to the
+// whole row -- for the median that also gives up the MAD classes of the
+// counting pass (they assume the median inside [m_lo, m_hi]) and its hot
+// values; for the MAD, the hot values (the superset may miss some, or have
+// overflowed its list).
+__global__ void det_check_kernel(DetState *__restrict__ st, int T, int mode, int pcap, float n_mad)
 {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= T || st[t].src != kSrcCand)
@@ -480,21 +703,30 @@ __global__ void det_check_kernel(DetState *__restrict__ st, int T, long long cap
     DetState s = st[t];
     const long long n = s.end - s.begin;
     const long long a = (n - 1) / 2, b = n / 2;
-    if (s.n_in <= cap && s.n_lt <= a && b < (long long)s.n_lt + s.n_in) {
+    if (!s.over_k && s.n_lt <= a && b < (long long)s.n_lt + s.n_in) {
         s.rank[0] = (int)(a - s.n_lt);
         s.rank[1] = (int)(b - s.n_lt);
+        const unsigned diff = s.klo ^ s.khi;
+        s.top = diff ? 32 - __clz(diff) : 0;
+        s.prefix[0] = s.prefix[1] = s.klo & above_mask(s.top);
+        if (s.top == 0) {  // every candidate has the key klo
+            finish_select(s, mode, middle_value(s.klo, s.klo, (int)n), n_mad);
+            s.src = kSrcDone;
+        }
     } else {
         s.src = kSrcRow;
+        s.top = 32;
+        s.prefix[0] = s.prefix[1] = 0u;
         s.rank[0] = (int)a;
         s.rank[1] = (int)b;
-        if (mode == 1)
-            s.peaks_ready = 0;
-    }
-    if (mode == 1 && (!s.peaks_ready || s.n_hot > pcap)) {
         s.peaks_ready = 0;
-        s.n_cand = 0;
+        if (mode == 0)
+            s.one_read = 0;
     }
-    s.prefix[0] = s.prefix[1] = 0u;
+    if (mode == 1 && (!s.peaks_ready || s.n_hot > pcap))
+        s.peaks_ready = 0;
+    if (!s.peaks_ready)
+        s.n_cand = 0;
     st[t] = s;
 }
 
@@ -507,7 +739,9 @@ __device__ __forceinline__ void hist_add(unsigned *h, float v, bool ok, int mode
                                          unsigned dmask, unsigned high, unsigned p0, unsigned p1,
                                          bool two, int lane, bool aggregate)
 {
-    const unsigned key = mode == 2 ? __float_as_uint(v) : sel_key(v, mode, med);
+    // mode 2: a candidate, keyed as v + 0 (the counting pass compares floats, where
+    // -0 and +0 are one value)
+    const unsigned key = mode == 2 ? order_key(__fadd_rn(v, 0.0f)) : sel_key(v, mode, med);
     const unsigned dig = (key >> shift) & dmask;
     const bool m0 = ok && (key & high) == p0;
     const bool m1 = two && ok && (key & high) == p1;
@@ -533,62 +767,82 @@ __device__ __forceinline__ void hist_add(unsigned *h, float v, bool ok, int mode
 }
 
 // One selection pass: histogram of the current digit over the elements whose
-// higher key bits equal a rank's prefix.  mode 0 keys the values, mode 1 keys
-// |x - median|.  Grid: (blocks per row, templates).  The row is read with
-// 16-byte loads, two per lane in flight per step.
+// higher key bits equal a rank's prefix: the candidates (each thread its own
+// column, as the counting pass wrote it) or, for a row that fell back, the
+// row (mode 0 keys the values, mode 1 |x - median|; 16-byte loads strided over
+// the row's blocks, two per lane in flight per step).  Grid: (blocks per row,
+// templates), as the counting pass.
 __global__ void __launch_bounds__(kDetThreads)
 det_hist_kernel(const float *__restrict__ cc, size_t ld, const DetState *__restrict__ st,
-                unsigned *__restrict__ hist, const unsigned *__restrict__ cand, long long cap, int pass,
-                int mode)
+                unsigned *__restrict__ hist, const float *__restrict__ cand, long long cap, Lanes g,
+                int pass, int mode)
 {
     __shared__ unsigned h[2 * kDetBins];
     const int t = blockIdx.y;
     const DetState s = st[t];
     if (s.src == kSrcDone || s.end - s.begin <= 0)
         return;  // uniform over the block, before any barrier
-    const bool keys = s.src == kSrcCand;  // candidate keys instead of row values
-    const long long n = keys ? s.n_in : s.end - s.begin;
+    if (pass > 0 && s.top <= 11 * pass)
+        return;  // the key is complete
     for (int i = threadIdx.x; i < 2 * kDetBins; i += kDetThreads)
         h[i] = 0u;
     __syncthreads();
-    const int shift = pass_shift(pass);
-    const unsigned dmask = pass_bins(pass) - 1u;
-    const unsigned high = pass_high_mask(pass);
+    int shift, width;
+    pass_digit(s.top, pass, shift, width);
+    const unsigned dmask = (1u << width) - 1u;
+    const unsigned high = above_mask(shift + width);
     const unsigned p0 = s.prefix[0], p1 = s.prefix[1];
     const bool two = p0 != p1;  // the two middle ranks sit in different buckets
     const float med = s.med;
-    // candidate keys are stored as the bits of a float whose order key they
-    // are: key_value() turns them back, so both sources run the same code
-    const float *row = keys ? reinterpret_cast<const float *>(cand + (size_t)t * cap)
-                            : cc + (size_t)t * ld + s.begin;
-    const int kmode = keys ? 2 : mode;
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
     constexpr int kWarps = kDetThreads / 32;
-    const RowSplit rs = split_row(row, n);
-    if (blockIdx.x == 0 && warp == 0) {  // the unaligned ends, at most 3 + 3 values
-        const long long i = lane < rs.head ? lane : rs.head + 4 * rs.nvec + (lane - rs.head);
-        const bool ok = lane < rs.head + rs.tail;
-        const float v = ok ? row[i] : 0.f;
-        hist_add(h, v, ok, kmode, med, shift, dmask, high, p0, p1, two, lane, pass == 0);
-    }
-    const float4 *vrow = reinterpret_cast<const float4 *>(row + rs.head);
-    const long long steps = (rs.nvec + 63) / 64;  // 64 float4s per warp step
-    for (long long c = (long long)blockIdx.x * kWarps + warp; c < steps; c += (long long)gridDim.x * kWarps) {
-        float4 v[2];
-        bool ok[2];
+    if (s.src == kSrcCand) {
+        const size_t col = ((size_t)t * g.S + blockIdx.x) * kDetThreads + threadIdx.x;
+        const size_t region = (size_t)blockIdx.x * kWarps + warp;
+        const float *kc = cand + (size_t)t * cap + region * (size_t)(g.Ck + 1) * 32 + lane;
+        const int m = g.cnt_k[col];  // <= Ck: no column overflowed
+        const int mw = __reduce_max_sync(0xffffffffu, m);
+        for (int k = 0; k < mw; k += 4) {
+            float x[4];
 #pragma unroll
-        for (int u = 0; u < 2; u++) {
-            const long long i = c * 64 + u * 32 + lane;
-            ok[u] = i < rs.nvec;
-            v[u] = ok[u] ? vrow[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+            for (int j = 0; j < 4; j++)
+                x[j] = k + j < m ? kc[(size_t)(k + j) * 32] : 0.0f;
+#pragma unroll
+            for (int j = 0; j < 4; j++)
+                hist_add(h, x[j], k + j < m, 2, med, shift, dmask, high, p0, p1, two, lane, false);
         }
+    } else {
+        // equal digits aggregated per warp in the first pass (a row's keys share their
+        // high digits)
+        const bool agg = pass == 0;
+        const float *row = cc + (size_t)t * ld + s.begin;
+        const RowSplit rs = split_row(row, s.end - s.begin);
+        if (blockIdx.x == 0 && warp == 0) {  // the unaligned ends, at most 3 + 3 values
+            const long long i = lane < rs.head ? lane : rs.head + 4 * rs.nvec + (lane - rs.head);
+            const bool ok = lane < rs.head + rs.tail;
+            const float v = ok ? row[i] : 0.f;
+            hist_add(h, v, ok, mode, med, shift, dmask, high, p0, p1, two, lane, agg);
+        }
+        const float4 *vrow = reinterpret_cast<const float4 *>(row + rs.head);
+        const long long steps = (rs.nvec + 63) / 64;  // 64 float4s per warp step
+        for (long long c = (long long)blockIdx.x * kWarps + warp; c < steps;
+             c += (long long)gridDim.x * kWarps) {
+            float4 v[2];
+            bool ok[2];
 #pragma unroll
-        for (int u = 0; u < 2; u++) {
-            hist_add(h, v[u].x, ok[u], kmode, med, shift, dmask, high, p0, p1, two, lane, pass == 0);
-            hist_add(h, v[u].y, ok[u], kmode, med, shift, dmask, high, p0, p1, two, lane, pass == 0);
-            hist_add(h, v[u].z, ok[u], kmode, med, shift, dmask, high, p0, p1, two, lane, pass == 0);
-            hist_add(h, v[u].w, ok[u], kmode, med, shift, dmask, high, p0, p1, two, lane, pass == 0);
+            for (int u = 0; u < 2; u++) {
+                const long long i = c * 64 + u * 32 + lane;
+                ok[u] = i < rs.nvec;
+                v[u] = ok[u] ? vrow[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+            }
+#pragma unroll
+            for (int u = 0; u < 2; u++) {
+                hist_add(h, v[u].x, ok[u], mode, med, shift, dmask, high, p0, p1, two, lane, agg);
+                hist_add(h, v[u].y, ok[u], mode, med, shift, dmask, high, p0, p1, two, lane, agg);
+                hist_add(h, v[u].z, ok[u], mode, med, shift, dmask, high, p0, p1, two, lane, agg);
+                hist_add(h, v[u].w, ok[u], mode, med, shift, dmask, high, p0, p1, two, lane, agg);
+            }
         }
     }
     __syncthreads();
@@ -612,9 +866,12 @@ __global__ void det_resolve_kernel(DetState *__restrict__ st, unsigned *__restri
     const int n = s.end - s.begin;
     if (n <= 0 || s.src == kSrcDone)
         return;
+    int shift, width;
+    pass_digit(s.top, pass, shift, width);
+    if (width == 0)
+        return;  // the key was complete after an earlier pass
     unsigned *gh = hist + (size_t)t * 2 * kDetBins;
-    const int per = (int)pass_bins(pass) / 32;  // bins per lane
-    const int shift = pass_shift(pass);
+    const int per = kDetBins / 32;  // bins per lane (digits of fewer bits leave the rest empty)
     const bool two = s.prefix[0] != s.prefix[1];
     for (int r = 0; r < 2; r++) {
         const unsigned *h = gh + (two ? r : 0) * kDetBins;
@@ -652,7 +909,7 @@ __global__ void det_resolve_kernel(DetState *__restrict__ st, unsigned *__restri
     __syncwarp();
     for (int i = lane; i < 2 * kDetBins; i += 32)
         gh[i] = 0u;
-    if (pass == 2)
+    if (shift == 0)
         finish_select(s, mode, middle_value(s.prefix[0], s.prefix[1], n), n_mad);
     if (lane == 0)
         st[t] = s;
@@ -885,18 +1142,23 @@ int detect_device(const float *cc, int T, int n_corr, size_t ld, const int *begi
     int rc;
     const int chunk = T < kDetChunk ? T : kDetChunk;
     DetState *st;
-    unsigned *hist, *keys;
+    unsigned *hist;
     int2 *cand;
-    int *hot;
-    float *saved;
-    // candidate keys per row: the sample window holds about 5 % of a row
-    const long long key_cap = n_corr < 65536 ? n_corr : std::max(65536LL, (long long)n_corr / 8);
+    int *hot, *col_cnt;
+    float *saved, *amb, *keys;
+    // candidates per row: a sample window holds about 2.5 % of a row; the values whose
+    // MAD class waits for the median, about 10 % of a Gaussian row
+    // (at least 512: two rows of every warp's columns, so a row's columns always fit)
+    const long long key_cap = std::max(512LL, n_corr < 65536 ? n_corr : std::max(65536LL, (long long)n_corr / 8));
+    const long long amb_cap = std::max(512LL, n_corr < 65536 ? n_corr : std::max(65536LL, (long long)n_corr / 4));
     if ((rc = ws.get(&st, (size_t)chunk, "detection state")) ||
         (rc = ws.get(&hist, (size_t)chunk * 2 * kDetBins, "detection histograms")) ||
         (rc = ws.get(&keys, (size_t)chunk * key_cap, "candidate keys")) ||
+        (rc = ws.get(&amb, (size_t)chunk * amb_cap, "values of undecided MAD class")) ||
         (rc = ws.get(&cand, (size_t)chunk * kDetCap, "candidate peaks")) ||
         (rc = ws.get(&hot, (size_t)chunk * kDetCap, "values above the threshold bound")) ||
-        (rc = ws.get(&saved, (size_t)chunk * kDetSample, "sampled values")))
+        (rc = ws.get(&saved, (size_t)chunk * kDetSample, "sampled values")) ||
+        (rc = ws.get(&col_cnt, 2 * ((size_t)kDetBlocks + chunk) * kDetThreads, "list column counts")))
         return rc;
     cudaError_t e = cudaFuncSetAttribute(det_select_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)select_smem(kDetCap));
@@ -911,31 +1173,43 @@ int detect_device(const float *cc, int T, int n_corr, size_t ld, const int *begi
         const int nt = T - t0 < chunk ? T - t0 : chunk;
         const float *rows = cc + (size_t)t0 * ld;
         // enough blocks per row to fill the 152 SMs (8 resident blocks each) about eight
-        // times over, so that the last, partial wave of blocks costs little
-        long long per_row = (152LL * 8 * 8 + nt - 1) / nt;
-        const long long row_cap = ((long long)n_corr + 1023) / 1024;
+        // times over, so that the last, partial wave of blocks costs little -- but at
+        // least 256 values per thread, so that its list columns are deep enough
+        long long per_row = ((long long)kDetBlocks + nt - 1) / nt;
+        const long long row_cap = std::max(1LL, (long long)n_corr / (256LL * kDetThreads));
         if (per_row > row_cap)
             per_row = row_cap;
         if (per_row < 1)
             per_row = 1;
         const dim3 grid((unsigned)per_row, (unsigned)nt);
+        // one column per counting thread (nt * per_row <= kDetBlocks + nt blocks); row C
+        // of each warp's region takes the overflow
+        Lanes g;
+        g.S = (int)per_row;
+        g.Ck = (int)std::max(0LL, key_cap / (per_row * kDetThreads) - 1);
+        g.Ca = (int)std::max(0LL, amb_cap / (per_row * kDetThreads) - 1);
+        g.cnt_k = col_cnt;
+        g.cnt_a = col_cnt + ((size_t)kDetBlocks + chunk) * kDetThreads;
+        const int check_blocks = (nt + 127) / 128;
         det_init_kernel<<<(nt + 127) / 128, 128, 0, s>>>(st, nt, n_corr, begin ? begin + t0 : nullptr,
                                                          end ? end + t0 : nullptr);
-        for (int mode = 0; mode < 2; mode++) {
-            det_sample_kernel<<<nt, 1024, kDetSample * sizeof(unsigned), s>>>(rows, ld, st, mode, n_mad,
-                                                                               saved);
-            if (mode == 1)
-                det_count_kernel<true><<<grid, kDetThreads, 0, s>>>(rows, ld, st, keys, key_cap, mode,
-                                                                    hot, kDetCap);
-            else
-                det_count_kernel<false><<<grid, kDetThreads, 0, s>>>(rows, ld, st, keys, key_cap, mode,
-                                                                     hot, kDetCap);
-            det_check_kernel<<<(nt + 127) / 128, 128, 0, s>>>(st, nt, key_cap, mode, kDetCap);
-            for (int pass = 0; pass < 3; pass++) {
-                det_hist_kernel<<<grid, kDetThreads, 0, s>>>(rows, ld, st, hist, keys, key_cap, pass,
-                                                             mode);
-                det_resolve_kernel<<<nt, 32, 0, s>>>(st, hist, pass, mode, n_mad);
-            }
+        // the median: sample, the one read of the rows, selection over the candidates
+        det_sample_kernel<<<nt, 1024, kDetSample * sizeof(unsigned), s>>>(rows, ld, st, 0, n_mad, saved);
+        det_count_kernel<true><<<grid, kDetThreads, 0, s>>>(rows, ld, st, keys, key_cap, amb, amb_cap, g, hot,
+                                                            kDetCap);
+        det_check_kernel<<<check_blocks, 128, 0, s>>>(st, nt, 0, kDetCap, n_mad);
+        for (int pass = 0; pass < 3; pass++) {
+            det_hist_kernel<<<grid, kDetThreads, 0, s>>>(rows, ld, st, hist, keys, key_cap, g, pass, 0);
+            det_resolve_kernel<<<nt, 32, 0, s>>>(st, hist, pass, 0, n_mad);
+        }
+        // the MAD: the sample about the exact median, the listed values, selection
+        det_sample_kernel<<<nt, 1024, kDetSample * sizeof(unsigned), s>>>(rows, ld, st, 1, n_mad, saved);
+        det_count_kernel<false><<<grid, kDetThreads, 0, s>>>(rows, ld, st, keys, key_cap, amb, amb_cap, g, hot,
+                                                             kDetCap);
+        det_check_kernel<<<check_blocks, 128, 0, s>>>(st, nt, 1, kDetCap, n_mad);
+        for (int pass = 0; pass < 3; pass++) {
+            det_hist_kernel<<<grid, kDetThreads, 0, s>>>(rows, ld, st, hist, keys, key_cap, g, pass, 1);
+            det_resolve_kernel<<<nt, 32, 0, s>>>(st, hist, pass, 1, n_mad);
         }
         det_hot_kernel<<<nt, kDetThreads, 0, s>>>(rows, ld, st, hot, kDetCap, cand, kDetCap);
         det_peaks_kernel<<<grid, kDetThreads, 0, s>>>(rows, ld, st, cand, kDetCap);

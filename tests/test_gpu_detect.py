@@ -145,3 +145,54 @@ def test_search_and_detect_in_template_chunks(monkeypatch):
     for t in range(tp.shape[0]):
         assert np.array_equal(whole.lags[t], chunked.lags[t])
         assert np.array_equal(whole.values[t], chunked.values[t])
+
+
+def _sampled_rows(n, seed):
+    """Rows of n = 8 x 16,384 samples whose values at every 8th position (the
+    positions the 16,384-value sample of each row reads) differ from the rest:
+    row 0 shifted there (the sample's median window misses the median), row 1
+    spread ten-fold there (the median window holds, the MAD window misses),
+    row 2 plain (both hold)."""
+    rng = np.random.default_rng(seed)
+    x = rng.standard_normal((3, n))
+    x[0, ::8] += 3.0
+    x[1, ::8] *= 10.0
+    for t in range(3):
+        x[t, rng.choice(n - 200, 4, replace=False) + 100] += 12.0
+    return x.astype(np.float32)
+
+
+@pytest.mark.parametrize("n_mad", [4.0, 8.0])
+def test_detect_when_the_sample_windows_miss(n_mad):
+    """A median window that misses: median and MAD over the whole row, peaks
+    by a pass of their own; a MAD window that misses: the MAD over the whole
+    row."""
+    cc = _sampled_rows(8 * 16384, 61)
+    det = fmf.detect(cc, n_mad=n_mad, min_separation=400, max_detections=4096)
+    assert_matches(det, cc, n_mad, 400, 4096)
+
+
+def test_detect_negative_n_mad():
+    """n_mad < 0: the threshold falls with the MAD, so the hot values of the
+    one read are bounded with the MAD window's upper end."""
+    cc = cc_rows(64, 3, 60000)
+    det = fmf.detect(cc, n_mad=-0.5, min_separation=30, max_detections=4096)
+    assert_matches(det, cc, -0.5, 30, 4096)
+
+
+def test_detect_ties_and_constant_rows():
+    """A row 40 % zeros (the median's candidates nearly all one key), a constant
+    row (MAD 0), and a row of three values (every deviation near the MAD
+    undecided until the median is known: the list of such values overflows)."""
+    rng = np.random.default_rng(62)
+    n = 300000
+    x = rng.standard_normal((4, n)).astype(np.float32) * 0.1
+    x[0, rng.random(n) < 0.4] = 0.0
+    x[1] = 0.25
+    x[2] = rng.choice(np.array([-1.0, 0.0, 1.0], np.float32), n) + \
+        rng.standard_normal(n).astype(np.float32) * 1e-4
+    x[3, rng.random(n) < 0.3] = 0.5
+    for t in (0, 2, 3):
+        x[t, rng.choice(n - 200, 3, replace=False) + 100] += 5.0
+    det = fmf.detect(x, n_mad=30.0, min_separation=1000, max_detections=256)
+    assert_matches(det, x, 30.0, 1000, 256)
