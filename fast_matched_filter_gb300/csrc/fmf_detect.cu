@@ -70,6 +70,7 @@ constexpr int kDetChunk = 1024;           // templates per round of scratch
 constexpr int kDetCap = 16384;            // candidate peaks per template row
 constexpr int kDetSample = 16384;         // sampled keys per row (sample-select)
 constexpr int kDetBlocks = 152 * 8 * 8;   // blocks of a row pass: 8 waves of 8 per SM
+constexpr int kSpill = 16;                // rows past a column's capacity (one step's appends)
 
 // source of a row's radix selection
 constexpr int kSrcRow = 0;   // the row itself (fallback)
@@ -103,9 +104,10 @@ struct DetState {
 // The lists of a row are written in columns, one per thread of the counting
 // pass, so that appending takes no scan and no shared counter: thread l of
 // warp w of block b puts its k-th entry at list + t * cap + ((b * 8 + w) *
-// (C + 1) + k) * 32 + (l & 31), up to C entries (row C of the warp's region
-// takes the overflow, unread), and its count at cnt[(t * S + b) * 256 + l].
-// Equal counts across a warp make coalesced stores and loads.
+// (C + kSpill) + k) * 32 + (l & 31), up to C entries (rows C.. of the warp's
+// region take a step's overflow, unread), and its count at
+// cnt[(t * S + b) * 256 + l] (more than C: overflowed).  Equal counts across a
+// warp make coalesced stores and loads.
 struct Lanes {
     int S;                 // counting blocks per row
     int Ck, Ca;            // column capacity: candidates of a selection / undecided values
@@ -550,31 +552,47 @@ det_count_kernel(const float *__restrict__ cc, size_t ld, DetState *__restrict__
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const size_t col = ((size_t)t * g.S + blockIdx.x) * kDetThreads + threadIdx.x;
     const size_t region = (size_t)blockIdx.x * (kDetThreads / 32) + warp;
-    float *kc = cand + (size_t)t * cap + region * (size_t)(g.Ck + 1) * 32 + lane;
-    float *ac = amb + (size_t)t * amb_cap + region * (size_t)(g.Ca + 1) * 32 + lane;
+    float *kc = cand + (size_t)t * cap + region * (size_t)(g.Ck + kSpill) * 32 + lane;
+    float *ac = amb + (size_t)t * amb_cap + region * (size_t)(g.Ca + kSpill) * 32 + lane;
     const float lo = key_value(st[t].klo), hi = key_value(st[t].khi);
     const float med = st[t].med;
+    // the MAD classes as float intervals, empty (x >= +inf never holds) where the
+    // row has none
     const bool classes = ROW && st[t].one_read;
     const bool has_below = classes && st[t].has_below;
-    const float b_lo = key_value(st[t].kb0), b_hi = key_value(st[t].kb1);
-    const float n_lo = key_value(st[t].kn0), n_hi = key_value(st[t].kn1);
+    const float b_lo = has_below ? key_value(st[t].kb0) : INFINITY;
+    const float b_hi = has_below ? key_value(st[t].kb1) : -INFINITY;
+    const float n_lo = classes ? key_value(st[t].kn0) : INFINITY;
+    const float n_hi = classes ? key_value(st[t].kn1) : -INFINITY;
     const bool peaks = ROW && st[t].peaks_ready;
     const float thr_lo = st[t].thr_lo;
     unsigned lt = 0, nb = 0;
-    int nk = 0, na = 0;  // entries of this thread's columns (past the capacity: row C, unread)
+    // offsets (floats) of the next entry of this thread's columns; a step's appends
+    // past the capacity land in the spill rows, and the offset is clamped after it
+    unsigned ko = 0, ao = 0;
+    const unsigned kmax = (unsigned)g.Ck * 32u, amax = (unsigned)g.Ca * 32u;
+    bool ovk = false, ova = false;
     auto take = [&](float x, bool ok) {
         lt += (unsigned)(ok & (x < lo));
         const bool in = ok & (x >= lo) & (x <= hi);
         if (in)
-            kc[(size_t)min(nk, g.Ck) * 32] = x;
-        nk += (int)in;
+            kc[ko] = x;
+        ko += in ? 32u : 0u;
         if constexpr (ROW) {
-            const bool below = has_below & ok & (x >= b_lo) & (x <= b_hi);
+            const bool below = ok & (x >= b_lo) & (x <= b_hi);
             nb += (unsigned)below;
-            const bool un = classes & ok & !below & (x >= n_lo) & (x <= n_hi);
+            const bool un = ok & !below & (x >= n_lo) & (x <= n_hi);
             if (un)
-                ac[(size_t)min(na, g.Ca) * 32] = x;
-            na += (int)un;
+                ac[ao] = x;
+            ao += un ? 32u : 0u;
+        }
+    };
+    auto clamp = [&]() {  // after at most kSpill appends per column
+        ovk |= ko > kmax;
+        ko = min(ko, kmax);
+        if constexpr (ROW) {
+            ova |= ao > amax;
+            ao = min(ao, amax);
         }
     };
     if constexpr (ROW) {
@@ -588,6 +606,7 @@ det_count_kernel(const float *__restrict__ cc, size_t ld, DetState *__restrict__
             if (peaks && ok && x >= thr_lo)
                 note_hot(st, t, i, hot, hcap);
             take(x, ok);
+            clamp();
         }
         const float4 *vrow = reinterpret_cast<const float4 *>(row + rs.head);
         const long long steps = (rs.nvec + 127) / 128;  // 128 float4s per warp step
@@ -650,6 +669,7 @@ det_count_kernel(const float *__restrict__ cc, size_t ld, DetState *__restrict__
                     take(v[u].w, ok);
                 }
             }
+            clamp();
         }
     } else {
         // this thread's own column of undecided values, four loads in flight
@@ -663,13 +683,15 @@ det_count_kernel(const float *__restrict__ cc, size_t ld, DetState *__restrict__
 #pragma unroll
             for (int j = 0; j < 4; j++)
                 take(dev(x[j], med), k + j < m);
+            clamp();
         }
     }
+    const int nk = ovk ? g.Ck + 1 : (int)(ko / 32u);  // past the capacity: overflowed
     g.cnt_k[col] = nk;
     if (ROW)
-        g.cnt_a[col] = na;
-    const bool over_k = __any_sync(0xffffffffu, nk > g.Ck);
-    const bool over_a = ROW && __any_sync(0xffffffffu, na > g.Ca);
+        g.cnt_a[col] = ova ? g.Ca + 1 : (int)(ao / 32u);
+    const bool over_k = __any_sync(0xffffffffu, ovk);
+    const bool over_a = ROW && __any_sync(0xffffffffu, ova);
     const int sum_k = __reduce_add_sync(0xffffffffu, (unsigned)nk);
     for (int o = 16; o > 0; o >>= 1) {
         lt += __shfl_down_sync(0xffffffffu, lt, o);
@@ -800,7 +822,7 @@ det_hist_kernel(const float *__restrict__ cc, size_t ld, const DetState *__restr
     if (s.src == kSrcCand) {
         const size_t col = ((size_t)t * g.S + blockIdx.x) * kDetThreads + threadIdx.x;
         const size_t region = (size_t)blockIdx.x * kWarps + warp;
-        const float *kc = cand + (size_t)t * cap + region * (size_t)(g.Ck + 1) * 32 + lane;
+        const float *kc = cand + (size_t)t * cap + region * (size_t)(g.Ck + kSpill) * 32 + lane;
         const int m = g.cnt_k[col];  // <= Ck: no column overflowed
         const int mw = __reduce_max_sync(0xffffffffu, m);
         for (int k = 0; k < mw; k += 4) {
@@ -1148,9 +1170,11 @@ int detect_device(const float *cc, int T, int n_corr, size_t ld, const int *begi
     float *saved, *amb, *keys;
     // candidates per row: a sample window holds about 2.5 % of a row; the values whose
     // MAD class waits for the median, about 10 % of a Gaussian row
-    // (at least 512: two rows of every warp's columns, so a row's columns always fit)
-    const long long key_cap = std::max(512LL, n_corr < 65536 ? n_corr : std::max(65536LL, (long long)n_corr / 8));
-    const long long amb_cap = std::max(512LL, n_corr < 65536 ? n_corr : std::max(65536LL, (long long)n_corr / 4));
+    // (at least 2 * kSpill rows of every thread's columns, so a row's columns always fit)
+    const long long key_cap = std::max(2LL * kSpill * kDetThreads,
+                                       n_corr < 65536 ? n_corr : std::max(65536LL, (long long)n_corr / 8));
+    const long long amb_cap = std::max(2LL * kSpill * kDetThreads,
+                                       n_corr < 65536 ? n_corr : std::max(65536LL, (long long)n_corr / 4));
     if ((rc = ws.get(&st, (size_t)chunk, "detection state")) ||
         (rc = ws.get(&hist, (size_t)chunk * 2 * kDetBins, "detection histograms")) ||
         (rc = ws.get(&keys, (size_t)chunk * key_cap, "candidate keys")) ||
@@ -1172,22 +1196,22 @@ int detect_device(const float *cc, int T, int n_corr, size_t ld, const int *begi
     for (int t0 = 0; t0 < T; t0 += chunk) {
         const int nt = T - t0 < chunk ? T - t0 : chunk;
         const float *rows = cc + (size_t)t0 * ld;
-        // enough blocks per row to fill the 152 SMs (8 resident blocks each) about eight
-        // times over, so that the last, partial wave of blocks costs little -- but at
-        // least 256 values per thread, so that its list columns are deep enough
+        // enough blocks per row to fill the SMs several times over, so that the last,
+        // partial wave of blocks costs little -- but at least 1,024 values per thread,
+        // so that its list columns hold many standard deviations above their mean fill
         long long per_row = ((long long)kDetBlocks + nt - 1) / nt;
-        const long long row_cap = std::max(1LL, (long long)n_corr / (256LL * kDetThreads));
+        const long long row_cap = std::max(1LL, (long long)n_corr / (1024LL * kDetThreads));
         if (per_row > row_cap)
             per_row = row_cap;
         if (per_row < 1)
             per_row = 1;
         const dim3 grid((unsigned)per_row, (unsigned)nt);
-        // one column per counting thread (nt * per_row <= kDetBlocks + nt blocks); row C
-        // of each warp's region takes the overflow
+        // one column per counting thread (nt * per_row <= kDetBlocks + nt blocks); rows
+        // C .. C + kSpill - 1 of each warp's region take a step's overflow
         Lanes g;
         g.S = (int)per_row;
-        g.Ck = (int)std::max(0LL, key_cap / (per_row * kDetThreads) - 1);
-        g.Ca = (int)std::max(0LL, amb_cap / (per_row * kDetThreads) - 1);
+        g.Ck = (int)(key_cap / (per_row * kDetThreads) - kSpill);
+        g.Ca = (int)(amb_cap / (per_row * kDetThreads) - kSpill);
         g.cnt_k = col_cnt;
         g.cnt_a = col_cnt + ((size_t)kDetBlocks + chunk) * kDetThreads;
         const int check_blocks = (nt + 127) / 128;
