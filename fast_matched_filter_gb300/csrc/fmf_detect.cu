@@ -23,16 +23,16 @@
 // The order statistics are exact, from one read of each row in the usual
 // case (a sample-select):
 //   1. one block per row sorts a strided sample of the row: the key window
-//      [klo, khi] around the two middle ranks (three binomial standard
+//      [klo, khi] around the two middle ranks (four binomial standard
 //      deviations wide), so the median lies in [m_lo, m_hi], the values of
 //      those keys; and from the sample's |x - m| about the window's middle, a
 //      window [a_lo, a_hi] the MAD lies in, widened by the median's own
 //      uncertainty;
 //   2. one pass over the row counts the keys below klo and gathers the keys
-//      inside [klo, khi] (about 2.5 % of the row), and classifies every value
+//      inside [klo, khi] (about 3.3 % of the row), and classifies every value
 //      for the MAD before the median is known: |x - m| < a_lo for every m in
 //      [m_lo, m_hi] (counted), |x - m| > a_hi for every such m (dropped), or
-//      either (listed: about 10 % of a Gaussian row); the same read notes the
+//      either (listed: about 13 % of a Gaussian row); the same read notes the
 //      values at or above a lower bound of the threshold
 //      (m_lo + n_mad * a_lo: thr = med + n_mad * mad is monotone in both);
 //   3. the median: if the window holds both middle ranks, a radix selection
@@ -350,7 +350,10 @@ __device__ unsigned last_key(unsigned c, F pred)
 // counting pass.  Mode 1 (the median now exact): the sample keyed by
 // |x - med| narrows the MAD window for the listed values; rows that cannot
 // use the list select their MAD over the whole row.
-constexpr int kPad = 3 * 64 + 16;  // sample positions either side of the middle ranks
+// sample positions either side of the middle ranks: 4 binomial standard deviations
+// (+16), so that a window misses about one row in 25,000 -- a row whose window
+// missed is selected over the whole row, several reads of it by its own blocks
+constexpr int kPad = 4 * 64 + 16;
 
 __global__ void __launch_bounds__(1024)
 det_sample_kernel(const float *__restrict__ cc, size_t ld, DetState *__restrict__ st, int mode,
@@ -608,14 +611,18 @@ det_count_kernel(const float *__restrict__ cc, size_t ld, DetState *__restrict__
             take(x, ok);
             clamp();
         }
+        // a warp step: 32 float4s from each quarter of the row, so that a lane's four
+        // float4s lie far apart (on a smooth row, neighbouring values share their
+        // class: a lane's appends then come in runs of at most 4)
         const float4 *vrow = reinterpret_cast<const float4 *>(row + rs.head);
-        const long long steps = (rs.nvec + 127) / 128;  // 128 float4s per warp step
+        const long long quarter = (rs.nvec + 3) / 4;
+        const long long steps = (quarter + 31) / 32;
         const long long cstride = (long long)gridDim.x * (kDetThreads / 32);
         auto load4 = [&](long long c, float4 (&v)[4]) {
 #pragma unroll
             for (int u = 0; u < 4; u++) {
-                const long long i = c * 128 + u * 32 + lane;
-                v[u] = (c < steps && i < rs.nvec) ? vrow[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+                const long long q = c * 32 + lane, i = u * quarter + q;
+                v[u] = (c < steps && q < quarter && i < rs.nvec) ? vrow[i] : make_float4(0.f, 0.f, 0.f, 0.f);
             }
         };
         float4 nv[4];
@@ -636,10 +643,10 @@ det_count_kernel(const float *__restrict__ cc, size_t ld, DetState *__restrict__
             if (peaks && __any_sync(0xffffffffu, mx >= thr_lo)) {
 #pragma unroll
                 for (int u = 0; u < 4; u++) {
-                    const long long q = c * 128 + u * 32 + lane;
+                    const long long q = c * 32 + lane, i = u * quarter + q;
                     const float m4 = fmaxf(fmaxf(v[u].x, v[u].y), fmaxf(v[u].z, v[u].w));
-                    if (q < rs.nvec && m4 >= thr_lo) {
-                        const long long o = rs.head + 4 * q;
+                    if (q < quarter && i < rs.nvec && m4 >= thr_lo) {
+                        const long long o = rs.head + 4 * i;
                         if (v[u].x >= thr_lo)
                             note_hot(st, t, o, hot, hcap);
                         if (v[u].y >= thr_lo)
@@ -651,7 +658,7 @@ det_count_kernel(const float *__restrict__ cc, size_t ld, DetState *__restrict__
                     }
                 }
             }
-            if (c * 128 + 128 <= rs.nvec) {  // a whole step inside the row (warp-uniform)
+            if (c * 32 + 32 <= quarter && 3 * quarter + c * 32 + 32 <= rs.nvec) {  // a whole step (warp-uniform)
 #pragma unroll
                 for (int u = 0; u < 4; u++) {
                     take(v[u].x, true);
@@ -662,7 +669,8 @@ det_count_kernel(const float *__restrict__ cc, size_t ld, DetState *__restrict__
             } else {
 #pragma unroll
                 for (int u = 0; u < 4; u++) {
-                    const bool ok = c * 128 + u * 32 + lane < rs.nvec;
+                    const long long q = c * 32 + lane;
+                    const bool ok = q < quarter && u * quarter + q < rs.nvec;
                     take(v[u].x, ok);
                     take(v[u].y, ok);
                     take(v[u].z, ok);
@@ -1168,8 +1176,8 @@ int detect_device(const float *cc, int T, int n_corr, size_t ld, const int *begi
     int2 *cand;
     int *hot, *col_cnt;
     float *saved, *amb, *keys;
-    // candidates per row: a sample window holds about 2.5 % of a row; the values whose
-    // MAD class waits for the median, about 10 % of a Gaussian row
+    // candidates per row: a sample window holds about 3.3 % of a row; the values whose
+    // MAD class waits for the median, about 13 % of a Gaussian row
     // (at least 2 * kSpill rows of every thread's columns, so a row's columns always fit)
     const long long key_cap = std::max(2LL * kSpill * kDetThreads,
                                        n_corr < 65536 ? n_corr : std::max(65536LL, (long long)n_corr / 8));
