@@ -23,16 +23,16 @@
 // The order statistics are exact, from one read of each row in the usual
 // case (a sample-select):
 //   1. one block per row sorts a strided sample of the row: the key window
-//      [klo, khi] around the two middle ranks (four binomial standard
+//      [klo, khi] around the two middle ranks (three binomial standard
 //      deviations wide), so the median lies in [m_lo, m_hi], the values of
 //      those keys; and from the sample's |x - m| about the window's middle, a
 //      window [a_lo, a_hi] the MAD lies in, widened by the median's own
 //      uncertainty;
 //   2. one pass over the row counts the keys below klo and gathers the keys
-//      inside [klo, khi] (about 3.3 % of the row), and classifies every value
+//      inside [klo, khi] (about 2.5 % of the row), and classifies every value
 //      for the MAD before the median is known: |x - m| < a_lo for every m in
 //      [m_lo, m_hi] (counted), |x - m| > a_hi for every such m (dropped), or
-//      either (listed: about 13 % of a Gaussian row); the same read notes the
+//      either (listed: about 10 % of a Gaussian row); the same read notes the
 //      values at or above a lower bound of the threshold
 //      (m_lo + n_mad * a_lo: thr = med + n_mad * mad is monotone in both);
 //   3. the median: if the window holds both middle ranks, a radix selection
@@ -71,6 +71,7 @@ constexpr int kDetCap = 16384;            // candidate peaks per template row
 constexpr int kDetSample = 16384;         // sampled keys per row (sample-select)
 constexpr int kDetBlocks = 152 * 8 * 8;   // blocks of a row pass: 8 waves of 8 per SM
 constexpr int kSpill = 16;                // rows past a column's capacity (one step's appends)
+constexpr int kDetRowBlocks = 152 * 4;    // the fixed grid of the passes over rows that fell back
 
 // source of a row's radix selection
 constexpr int kSrcRow = 0;   // the row itself (fallback)
@@ -350,10 +351,10 @@ __device__ unsigned last_key(unsigned c, F pred)
 // counting pass.  Mode 1 (the median now exact): the sample keyed by
 // |x - med| narrows the MAD window for the listed values; rows that cannot
 // use the list select their MAD over the whole row.
-// sample positions either side of the middle ranks: 4 binomial standard deviations
-// (+16), so that a window misses about one row in 25,000 -- a row whose window
-// missed is selected over the whole row, several reads of it by its own blocks
-constexpr int kPad = 4 * 64 + 16;
+// sample positions either side of the middle ranks: 3 binomial standard deviations
+// (+16), so that a window misses about one row in 800 -- such a row is selected
+// over the whole row, a few reads of it at the rate of the whole GPU
+constexpr int kPad = 3 * 64 + 16;
 
 __global__ void __launch_bounds__(1024)
 det_sample_kernel(const float *__restrict__ cc, size_t ld, DetState *__restrict__ st, int mode,
@@ -796,12 +797,10 @@ __device__ __forceinline__ void hist_add(unsigned *h, float v, bool ok, int mode
     }
 }
 
-// One selection pass: histogram of the current digit over the elements whose
-// higher key bits equal a rank's prefix: the candidates (each thread its own
-// column, as the counting pass wrote it) or, for a row that fell back, the
-// row (mode 0 keys the values, mode 1 |x - median|; 16-byte loads strided over
-// the row's blocks, two per lane in flight per step).  Grid: (blocks per row,
-// templates), as the counting pass.
+// One selection pass over the candidates: histogram of the current digit over
+// the candidates whose higher key bits equal a rank's prefix, each thread
+// reading its own column as the counting pass wrote it.  Grid: (blocks per
+// row, templates), as the counting pass.
 __global__ void __launch_bounds__(kDetThreads)
 det_hist_kernel(const float *__restrict__ cc, size_t ld, const DetState *__restrict__ st,
                 unsigned *__restrict__ hist, const float *__restrict__ cand, long long cap, Lanes g,
@@ -810,8 +809,9 @@ det_hist_kernel(const float *__restrict__ cc, size_t ld, const DetState *__restr
     __shared__ unsigned h[2 * kDetBins];
     const int t = blockIdx.y;
     const DetState s = st[t];
-    if (s.src == kSrcDone || s.end - s.begin <= 0)
-        return;  // uniform over the block, before any barrier
+    if (s.src != kSrcCand || s.end - s.begin <= 0)
+        return;  // uniform over the block, before any barrier (rows that fell back:
+                 // det_hist_row_kernel)
     if (pass > 0 && s.top <= 11 * pass)
         return;  // the key is complete
     for (int i = threadIdx.x; i < 2 * kDetBins; i += kDetThreads)
@@ -827,7 +827,7 @@ det_hist_kernel(const float *__restrict__ cc, size_t ld, const DetState *__restr
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
     constexpr int kWarps = kDetThreads / 32;
-    if (s.src == kSrcCand) {
+    {
         const size_t col = ((size_t)t * g.S + blockIdx.x) * kDetThreads + threadIdx.x;
         const size_t region = (size_t)blockIdx.x * kWarps + warp;
         const float *kc = cand + (size_t)t * cap + region * (size_t)(g.Ck + kSpill) * 32 + lane;
@@ -842,17 +842,78 @@ det_hist_kernel(const float *__restrict__ cc, size_t ld, const DetState *__restr
             for (int j = 0; j < 4; j++)
                 hist_add(h, x[j], k + j < m, 2, med, shift, dmask, high, p0, p1, two, lane, false);
         }
-    } else {
-        // equal digits aggregated per warp in the first pass (a row's keys share their
-        // high digits)
+    }
+    __syncthreads();
+    unsigned *gh = hist + (size_t)t * 2 * kDetBins;
+    for (int i = threadIdx.x; i < (two ? 2 : 1) * kDetBins; i += kDetThreads) {
+        const unsigned c = h[i];
+        if (c)
+            atomicAdd(gh + i, c);
+    }
+}
+
+// The rows that need a pass over the whole row, compacted into list[0..*count)
+// (one block): kind 0 those selecting over the whole row, kind 1 those whose
+// peaks were not gathered by the counting pass (at least 3 lags).
+__global__ void __launch_bounds__(1024)
+det_collect_kernel(const DetState *__restrict__ st, int T, int kind, int *__restrict__ list,
+                   int *__restrict__ count)
+{
+    __shared__ int n;
+    if (threadIdx.x == 0)
+        n = 0;
+    __syncthreads();
+    for (int t = threadIdx.x; t < T; t += blockDim.x) {
+        const bool need = kind == 0 ? st[t].src == kSrcRow && st[t].end > st[t].begin
+                                    : !st[t].peaks_ready && st[t].end - st[t].begin >= 3;
+        if (need)
+            list[atomicAdd(&n, 1)] = t;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0)
+        *count = n;
+}
+
+// The same pass for the rows that fell back to selection over the whole row
+// (a sample window that missed, a column that overflowed): every block of a
+// fixed grid takes a slice of each such row in turn, so a row that fell back
+// is read at the rate of the whole GPU, not of its own few blocks.  mode 0
+// keys the values, mode 1 |x - median|; equal digits are aggregated per warp
+// in the first pass (a row's keys share their high digits).
+__global__ void __launch_bounds__(kDetThreads)
+det_hist_row_kernel(const float *__restrict__ cc, size_t ld, const DetState *__restrict__ st,
+                    const int *__restrict__ list, const int *__restrict__ count,
+                    unsigned *__restrict__ hist, int pass, int mode)
+{
+    __shared__ unsigned h[2 * kDetBins];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    constexpr int kWarps = kDetThreads / 32;
+    const int nrows = *count;
+    for (int k = 0; k < nrows; k++) {
+        const int t = list[k];
+        const DetState s = st[t];
+        const long long n = s.end - s.begin;
+        if (n <= 0)
+            continue;
+        int shift, width;
+        pass_digit(s.top, pass, shift, width);
+        if (width == 0)
+            continue;
+        const unsigned dmask = (1u << width) - 1u;
+        const unsigned high = above_mask(shift + width);
+        const unsigned p0 = s.prefix[0], p1 = s.prefix[1];
+        const bool two = p0 != p1;
         const bool agg = pass == 0;
+        for (int i = threadIdx.x; i < 2 * kDetBins; i += kDetThreads)
+            h[i] = 0u;
+        __syncthreads();
         const float *row = cc + (size_t)t * ld + s.begin;
-        const RowSplit rs = split_row(row, s.end - s.begin);
+        const RowSplit rs = split_row(row, n);
         if (blockIdx.x == 0 && warp == 0) {  // the unaligned ends, at most 3 + 3 values
             const long long i = lane < rs.head ? lane : rs.head + 4 * rs.nvec + (lane - rs.head);
             const bool ok = lane < rs.head + rs.tail;
             const float v = ok ? row[i] : 0.f;
-            hist_add(h, v, ok, mode, med, shift, dmask, high, p0, p1, two, lane, agg);
+            hist_add(h, v, ok, mode, s.med, shift, dmask, high, p0, p1, two, lane, agg);
         }
         const float4 *vrow = reinterpret_cast<const float4 *>(row + rs.head);
         const long long steps = (rs.nvec + 63) / 64;  // 64 float4s per warp step
@@ -868,19 +929,20 @@ det_hist_kernel(const float *__restrict__ cc, size_t ld, const DetState *__restr
             }
 #pragma unroll
             for (int u = 0; u < 2; u++) {
-                hist_add(h, v[u].x, ok[u], mode, med, shift, dmask, high, p0, p1, two, lane, agg);
-                hist_add(h, v[u].y, ok[u], mode, med, shift, dmask, high, p0, p1, two, lane, agg);
-                hist_add(h, v[u].z, ok[u], mode, med, shift, dmask, high, p0, p1, two, lane, agg);
-                hist_add(h, v[u].w, ok[u], mode, med, shift, dmask, high, p0, p1, two, lane, agg);
+                hist_add(h, v[u].x, ok[u], mode, s.med, shift, dmask, high, p0, p1, two, lane, agg);
+                hist_add(h, v[u].y, ok[u], mode, s.med, shift, dmask, high, p0, p1, two, lane, agg);
+                hist_add(h, v[u].z, ok[u], mode, s.med, shift, dmask, high, p0, p1, two, lane, agg);
+                hist_add(h, v[u].w, ok[u], mode, s.med, shift, dmask, high, p0, p1, two, lane, agg);
             }
         }
-    }
-    __syncthreads();
-    unsigned *gh = hist + (size_t)t * 2 * kDetBins;
-    for (int i = threadIdx.x; i < (two ? 2 : 1) * kDetBins; i += kDetThreads) {
-        const unsigned c = h[i];
-        if (c)
-            atomicAdd(gh + i, c);
+        __syncthreads();
+        unsigned *gh = hist + (size_t)t * 2 * kDetBins;
+        for (int i = threadIdx.x; i < (two ? 2 : 1) * kDetBins; i += kDetThreads) {
+            const unsigned c = h[i];
+            if (c)
+                atomicAdd(gh + i, c);
+        }
+        __syncthreads();  // h is cleared for the next row
     }
 }
 
@@ -972,44 +1034,46 @@ det_hot_kernel(const float *__restrict__ cc, size_t ld, DetState *__restrict__ s
 }
 
 // Local maxima at or above the threshold, appended (unordered) to the
-// template's candidate list, for the rows whose MAD pass did not gather them
-// (rows sorted whole by the sample, MAD windows that missed, overflowing
-// supersets).  Grid: (blocks per row, templates).  Samples are read with
-// 16-byte loads; the rare sample at or above the threshold is examined with
-// scalar loads.
+// template's candidate list, for the rows whose counting pass did not gather
+// them (rows sorted whole by the sample, windows that missed, supersets that
+// overflowed): every block of a fixed grid takes a slice of each such row in
+// turn.  Samples are read with 16-byte loads; the rare sample at or above the
+// threshold is examined with scalar loads.
 __global__ void __launch_bounds__(kDetThreads)
 det_peaks_kernel(const float *__restrict__ cc, size_t ld, DetState *__restrict__ st,
-                 int2 *__restrict__ cand, int cap)
+                 const int *__restrict__ list, const int *__restrict__ count, int2 *__restrict__ cand, int cap)
 {
-    const int t = blockIdx.y;
-    const long long b = st[t].begin, e = st[t].end;
-    const float thr = st[t].thr;
-    if (e - b < 3 || st[t].peaks_ready)
-        return;
-    const float *row = cc + (size_t)t * ld;
-    const RowSplit rs = split_row(row + b, e - b);
     const long long gtid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (gtid < rs.head + rs.tail) {
-        const long long i = b + (gtid < rs.head ? gtid : rs.head + 4 * rs.nvec + (gtid - rs.head));
-        peak_at(row, i, b, e, row[i], thr, st, cand, cap, t);
-    }
-    const float4 *vrow = reinterpret_cast<const float4 *>(row + b + rs.head);
-    const long long base = b + rs.head;
     const long long stride = (long long)gridDim.x * blockDim.x;
-    for (long long v = gtid; v < rs.nvec; v += 2 * stride) {
-        const float4 x0 = vrow[v];
-        const bool has1 = v + stride < rs.nvec;
-        const float4 x1 = has1 ? vrow[v + stride] : make_float4(0.f, 0.f, 0.f, 0.f);
-        const long long i0 = base + 4 * v, i1 = base + 4 * (v + stride);
-        peak_at(row, i0, b, e, x0.x, thr, st, cand, cap, t);
-        peak_at(row, i0 + 1, b, e, x0.y, thr, st, cand, cap, t);
-        peak_at(row, i0 + 2, b, e, x0.z, thr, st, cand, cap, t);
-        peak_at(row, i0 + 3, b, e, x0.w, thr, st, cand, cap, t);
-        if (has1) {
-            peak_at(row, i1, b, e, x1.x, thr, st, cand, cap, t);
-            peak_at(row, i1 + 1, b, e, x1.y, thr, st, cand, cap, t);
-            peak_at(row, i1 + 2, b, e, x1.z, thr, st, cand, cap, t);
-            peak_at(row, i1 + 3, b, e, x1.w, thr, st, cand, cap, t);
+    const int nrows = *count;
+#pragma unroll 1
+    for (int k = 0; k < nrows; k++) {
+        const int t = list[k];
+        const long long b = st[t].begin, e = st[t].end;
+        const float thr = st[t].thr;
+        const float *row = cc + (size_t)t * ld;
+        const RowSplit rs = split_row(row + b, e - b);
+        if (gtid < rs.head + rs.tail) {
+            const long long i = b + (gtid < rs.head ? gtid : rs.head + 4 * rs.nvec + (gtid - rs.head));
+            peak_at(row, i, b, e, row[i], thr, st, cand, cap, t);
+        }
+        const float4 *vrow = reinterpret_cast<const float4 *>(row + b + rs.head);
+        const long long base = b + rs.head;
+        for (long long v = gtid; v < rs.nvec; v += 2 * stride) {
+            const float4 x0 = vrow[v];
+            const bool has1 = v + stride < rs.nvec;
+            const float4 x1 = has1 ? vrow[v + stride] : make_float4(0.f, 0.f, 0.f, 0.f);
+            const long long i0 = base + 4 * v, i1 = base + 4 * (v + stride);
+            peak_at(row, i0, b, e, x0.x, thr, st, cand, cap, t);
+            peak_at(row, i0 + 1, b, e, x0.y, thr, st, cand, cap, t);
+            peak_at(row, i0 + 2, b, e, x0.z, thr, st, cand, cap, t);
+            peak_at(row, i0 + 3, b, e, x0.w, thr, st, cand, cap, t);
+            if (has1) {
+                peak_at(row, i1, b, e, x1.x, thr, st, cand, cap, t);
+                peak_at(row, i1 + 1, b, e, x1.y, thr, st, cand, cap, t);
+                peak_at(row, i1 + 2, b, e, x1.z, thr, st, cand, cap, t);
+                peak_at(row, i1 + 3, b, e, x1.w, thr, st, cand, cap, t);
+            }
         }
     }
 }
@@ -1174,10 +1238,10 @@ int detect_device(const float *cc, int T, int n_corr, size_t ld, const int *begi
     DetState *st;
     unsigned *hist;
     int2 *cand;
-    int *hot, *col_cnt;
+    int *hot, *col_cnt, *row_list;
     float *saved, *amb, *keys;
-    // candidates per row: a sample window holds about 3.3 % of a row; the values whose
-    // MAD class waits for the median, about 13 % of a Gaussian row
+    // candidates per row: a sample window holds about 2.5 % of a row; the values whose
+    // MAD class waits for the median, about 10 % of a Gaussian row
     // (at least 2 * kSpill rows of every thread's columns, so a row's columns always fit)
     const long long key_cap = std::max(2LL * kSpill * kDetThreads,
                                        n_corr < 65536 ? n_corr : std::max(65536LL, (long long)n_corr / 8));
@@ -1190,7 +1254,8 @@ int detect_device(const float *cc, int T, int n_corr, size_t ld, const int *begi
         (rc = ws.get(&cand, (size_t)chunk * kDetCap, "candidate peaks")) ||
         (rc = ws.get(&hot, (size_t)chunk * kDetCap, "values above the threshold bound")) ||
         (rc = ws.get(&saved, (size_t)chunk * kDetSample, "sampled values")) ||
-        (rc = ws.get(&col_cnt, 2 * ((size_t)kDetBlocks + chunk) * kDetThreads, "list column counts")))
+        (rc = ws.get(&col_cnt, 2 * ((size_t)kDetBlocks + chunk) * kDetThreads, "list column counts")) ||
+        (rc = ws.get(&row_list, (size_t)chunk + 1, "rows of whole-row passes")))
         return rc;
     cudaError_t e = cudaFuncSetAttribute(det_select_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)select_smem(kDetCap));
@@ -1230,8 +1295,12 @@ int detect_device(const float *cc, int T, int n_corr, size_t ld, const int *begi
         det_count_kernel<true><<<grid, kDetThreads, 0, s>>>(rows, ld, st, keys, key_cap, amb, amb_cap, g, hot,
                                                             kDetCap);
         det_check_kernel<<<check_blocks, 128, 0, s>>>(st, nt, 0, kDetCap, n_mad);
+        int *const rcount = row_list + chunk;
+        det_collect_kernel<<<1, 1024, 0, s>>>(st, nt, 0, row_list, rcount);
         for (int pass = 0; pass < 3; pass++) {
             det_hist_kernel<<<grid, kDetThreads, 0, s>>>(rows, ld, st, hist, keys, key_cap, g, pass, 0);
+            det_hist_row_kernel<<<kDetRowBlocks, kDetThreads, 0, s>>>(rows, ld, st, row_list, rcount, hist,
+                                                                      pass, 0);
             det_resolve_kernel<<<nt, 32, 0, s>>>(st, hist, pass, 0, n_mad);
         }
         // the MAD: the sample about the exact median, the listed values, selection
@@ -1239,17 +1308,21 @@ int detect_device(const float *cc, int T, int n_corr, size_t ld, const int *begi
         det_count_kernel<false><<<grid, kDetThreads, 0, s>>>(rows, ld, st, keys, key_cap, amb, amb_cap, g, hot,
                                                              kDetCap);
         det_check_kernel<<<check_blocks, 128, 0, s>>>(st, nt, 1, kDetCap, n_mad);
+        det_collect_kernel<<<1, 1024, 0, s>>>(st, nt, 0, row_list, rcount);
         for (int pass = 0; pass < 3; pass++) {
             det_hist_kernel<<<grid, kDetThreads, 0, s>>>(rows, ld, st, hist, keys, key_cap, g, pass, 1);
+            det_hist_row_kernel<<<kDetRowBlocks, kDetThreads, 0, s>>>(rows, ld, st, row_list, rcount, hist,
+                                                                      pass, 1);
             det_resolve_kernel<<<nt, 32, 0, s>>>(st, hist, pass, 1, n_mad);
         }
         det_hot_kernel<<<nt, kDetThreads, 0, s>>>(rows, ld, st, hot, kDetCap, cand, kDetCap);
-        det_peaks_kernel<<<grid, kDetThreads, 0, s>>>(rows, ld, st, cand, kDetCap);
+        det_collect_kernel<<<1, 1024, 0, s>>>(st, nt, 1, row_list, rcount);
+        det_peaks_kernel<<<kDetRowBlocks, kDetThreads, 0, s>>>(rows, ld, st, row_list, rcount, cand, kDetCap);
         det_select_kernel<<<nt, kDetSelectThreads, select_smem(kDetCap), s>>>(
             st, cand, kDetCap, min_sep, max_det, med_out ? med_out + t0 : nullptr,
             mad_out ? mad_out + t0 : nullptr, thr_out ? thr_out + t0 : nullptr, count_out + t0,
             lag_out + (size_t)t0 * max_det, val_out + (size_t)t0 * max_det);
-        count_launch(22);
+        count_launch(31);
         if ((rc = check_launch("detection kernels")))
             return rc;
     }
