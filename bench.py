@@ -707,7 +707,8 @@ def run_detection(cfg, dev_out, world, steps=3, warmup=1):
                          "traffic_source": "fmf_detect_500rows_day.md: DRAM bytes of one call's "
                                            "launches per row byte, scaled to these rows",
                          "peak_source": "%s hbm_gbs (copy)" % peak_kind,
-                         "kernel": "fmf_detect (det_hist x6, det_resolve x6, det_peaks, "
+                         "kernel": "fmf_detect (det_sample x2, det_count x2: one read of each "
+                                   "row; det_hist x6 over the candidates, det_resolve x6, "
                                    "det_select)"}}
 
 
