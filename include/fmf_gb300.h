@@ -247,7 +247,10 @@ FMF_API int fmf_matched_filter_variable_ex(const float *templates, const float *
  * NULL when max_detections is 0.  min_separation >= 1.  Rows must be free of
  * NaN.  Host pointers: synchronous, FMF_ERR_UNSUPPORTED when a row exceeded
  * the capacity.  FMF_FLAG_DEVICE_POINTERS: every array on the device,
- * asynchronous on `stream`; check count_out for -1.
+ * asynchronous on `stream`; check count_out for -1.  Working memory, from the
+ * stream-ordered pool: about 1.5 bytes per lag of the rows detected at once
+ * (up to 1,024 rows; lists of median candidates and of values whose MAD class
+ * waits for the median), plus about 25 MB.
  */
 #define FMF_DETECT_CAPACITY 16384
 FMF_API int fmf_detect(const float *cc, size_t n_templates, size_t n_corr, const int *lag_begin,
