@@ -38,8 +38,10 @@
 //   3. the median: if the window holds both middle ranks, a radix selection
 //      over the candidates (passes of up to 11 bits over the key bits the
 //      window's keys do not share, each a shared-memory histogram of the keys
-//      that match the bits chosen so far); if not -- heavy ties, an
-//      adversarial row -- the same selection over the whole row;
+//      that match the bits chosen so far); if not -- a window that missed
+//      (about one row in 800), heavy ties, an adversarial row -- the same
+//      selection over the whole row, by a fixed grid of blocks over the list
+//      of such rows, so that the row is read at the rate of the whole GPU;
 //   4. the MAD: the sample keyed by |x - med| narrows [a_lo, a_hi]; the listed
 //      values keyed by |x - med| are counted below the window or gathered in
 //      it, and selected as in 3.  A row whose median or MAD window missed, or
@@ -56,7 +58,6 @@
 // detection run needs no host round trip and can be captured in a graph.
 #include <algorithm>
 #include <cmath>
-#include <type_traits>
 
 #include "fmf_common.cuh"
 
@@ -681,16 +682,16 @@ det_count_kernel(const float *__restrict__ cc, size_t ld, DetState *__restrict__
             clamp();
         }
     } else {
-        // this thread's own column of undecided values, four loads in flight
+        // this thread's own column of undecided values, eight loads in flight
         const int m = min(g.cnt_a[col], g.Ca);
         const int mw = __reduce_max_sync(0xffffffffu, m);
-        for (int k = 0; k < mw; k += 4) {
-            float x[4];
+        for (int k = 0; k < mw; k += 8) {
+            float x[8];
 #pragma unroll
-            for (int j = 0; j < 4; j++)
+            for (int j = 0; j < 8; j++)
                 x[j] = k + j < m ? ac[(size_t)(k + j) * 32] : 0.0f;
 #pragma unroll
-            for (int j = 0; j < 4; j++)
+            for (int j = 0; j < 8; j++)
                 take(dev(x[j], med), k + j < m);
             clamp();
         }
@@ -802,9 +803,8 @@ __device__ __forceinline__ void hist_add(unsigned *h, float v, bool ok, int mode
 // reading its own column as the counting pass wrote it.  Grid: (blocks per
 // row, templates), as the counting pass.
 __global__ void __launch_bounds__(kDetThreads)
-det_hist_kernel(const float *__restrict__ cc, size_t ld, const DetState *__restrict__ st,
-                unsigned *__restrict__ hist, const float *__restrict__ cand, long long cap, Lanes g,
-                int pass, int mode)
+det_hist_kernel(const DetState *__restrict__ st, unsigned *__restrict__ hist,
+                const float *__restrict__ cand, long long cap, Lanes g, int pass)
 {
     __shared__ unsigned h[2 * kDetBins];
     const int t = blockIdx.y;
@@ -833,13 +833,13 @@ det_hist_kernel(const float *__restrict__ cc, size_t ld, const DetState *__restr
         const float *kc = cand + (size_t)t * cap + region * (size_t)(g.Ck + kSpill) * 32 + lane;
         const int m = g.cnt_k[col];  // <= Ck: no column overflowed
         const int mw = __reduce_max_sync(0xffffffffu, m);
-        for (int k = 0; k < mw; k += 4) {
-            float x[4];
+        for (int k = 0; k < mw; k += 8) {  // eight loads in flight
+            float x[8];
 #pragma unroll
-            for (int j = 0; j < 4; j++)
+            for (int j = 0; j < 8; j++)
                 x[j] = k + j < m ? kc[(size_t)(k + j) * 32] : 0.0f;
 #pragma unroll
-            for (int j = 0; j < 4; j++)
+            for (int j = 0; j < 8; j++)
                 hist_add(h, x[j], k + j < m, 2, med, shift, dmask, high, p0, p1, two, lane, false);
         }
     }
@@ -1298,7 +1298,7 @@ int detect_device(const float *cc, int T, int n_corr, size_t ld, const int *begi
         int *const rcount = row_list + chunk;
         det_collect_kernel<<<1, 1024, 0, s>>>(st, nt, 0, row_list, rcount);
         for (int pass = 0; pass < 3; pass++) {
-            det_hist_kernel<<<grid, kDetThreads, 0, s>>>(rows, ld, st, hist, keys, key_cap, g, pass, 0);
+            det_hist_kernel<<<grid, kDetThreads, 0, s>>>(st, hist, keys, key_cap, g, pass);
             det_hist_row_kernel<<<kDetRowBlocks, kDetThreads, 0, s>>>(rows, ld, st, row_list, rcount, hist,
                                                                       pass, 0);
             det_resolve_kernel<<<nt, 32, 0, s>>>(st, hist, pass, 0, n_mad);
@@ -1310,7 +1310,7 @@ int detect_device(const float *cc, int T, int n_corr, size_t ld, const int *begi
         det_check_kernel<<<check_blocks, 128, 0, s>>>(st, nt, 1, kDetCap, n_mad);
         det_collect_kernel<<<1, 1024, 0, s>>>(st, nt, 0, row_list, rcount);
         for (int pass = 0; pass < 3; pass++) {
-            det_hist_kernel<<<grid, kDetThreads, 0, s>>>(rows, ld, st, hist, keys, key_cap, g, pass, 1);
+            det_hist_kernel<<<grid, kDetThreads, 0, s>>>(st, hist, keys, key_cap, g, pass);
             det_hist_row_kernel<<<kDetRowBlocks, kDetThreads, 0, s>>>(rows, ld, st, row_list, rcount, hist,
                                                                       pass, 1);
             det_resolve_kernel<<<nt, 32, 0, s>>>(st, hist, pass, 1, n_mad);
