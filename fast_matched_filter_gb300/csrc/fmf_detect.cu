@@ -402,21 +402,32 @@ det_sample_kernel(const float *__restrict__ cc, size_t ld, DetState *__restrict_
     }
     // sample positions floor(i * n / m) from a fixed-point step (no 64-bit division
     // per sample); any spread of positions serves, the selection is exact
+    // (blockDim.x = 1024, P <= kDetSample: kPer slots per thread, all loads issued
+    // before the first store, so the scattered reads are in flight together)
     const unsigned long long stepq = ((unsigned long long)n << 20) / (unsigned long long)m;
-    for (int i = threadIdx.x; i < P; i += blockDim.x) {
-        unsigned key = 0xffffffffu;  // padding: ranks last
+    constexpr int kPer = kDetSample / 1024;
+    float v[kPer];
+#pragma unroll
+    for (int j = 0; j < kPer; j++) {
+        const int i = threadIdx.x + j * 1024;
+        v[j] = 0.0f;
         if (i < m) {
-            float v;
             if (mode == 0) {
                 const long long pos = (long long)(((unsigned long long)i * stepq) >> 20);
-                v = row[pos < n ? pos : n - 1];
-                sv[i] = v;
+                v[j] = row[pos < n ? pos : n - 1];
             } else {
-                v = sv[i];
+                v[j] = sv[i];
             }
-            key = order_key(mode == 0 ? v : dev(v, med));
         }
-        sk[i] = key;
+    }
+#pragma unroll
+    for (int j = 0; j < kPer; j++) {
+        const int i = threadIdx.x + j * 1024;
+        if (i < P) {
+            if (mode == 0 && i < m)
+                sv[i] = v[j];
+            sk[i] = i < m ? order_key(mode == 0 ? v[j] : dev(v[j], med)) : 0xffffffffu;  // padding ranks last
+        }
     }
     __syncthreads();
     // ranks of the window: the sample position of rank r is about r*m/n, with a
