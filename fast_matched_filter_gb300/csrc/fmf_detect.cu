@@ -26,8 +26,8 @@
 //      [klo, khi] around the two middle ranks (three binomial standard
 //      deviations wide), so the median lies in [m_lo, m_hi], the values of
 //      those keys; and from the sample's |x - m| about the window's middle, a
-//      window [a_lo, a_hi] the MAD lies in, widened by the median's own
-//      uncertainty;
+//      window [a_lo, a_hi] the MAD lies in, widened a little for the median's
+//      own uncertainty;
 //   2. one pass over the row counts the keys below klo and gathers the keys
 //      inside [klo, khi] (about 2.5 % of the row), and classifies every value
 //      for the MAD before the median is known: |x - m| < a_lo for every m in
@@ -488,7 +488,10 @@ det_sample_kernel(const float *__restrict__ cc, size_t ld, DetState *__restrict_
     s.n_lt = s.n_in = 0;
     s.n_below = 0;
     s.over_k = s.over_a = 0;
-    const float wide = fmaxf(__fsub_rn(mid, m_lo), __fsub_rn(m_hi, mid));
+    // the MAD moves with the median only at second order where the row is near
+    // symmetric about it (d MAD / d m ~ f(m + MAD) - f(m - MAD)): a quarter of the
+    // median window's half-width; a window that misses costs that row a pass over it
+    const float wide = __fmul_rn(0.25f, fmaxf(__fsub_rn(mid, m_lo), __fsub_rn(m_hi, mid)));
     const float a_lo = fmaxf(__fsub_rn(key_value(ka0), wide), 0.0f);
     const float a_hi = __fadd_rn(key_value(ka1), wide);
     s.one_read = isfinite(m_lo) && isfinite(m_hi) && isfinite(a_lo) && isfinite(a_hi);
