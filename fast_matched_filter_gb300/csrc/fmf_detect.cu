@@ -32,7 +32,7 @@
 //      inside [klo, khi] (about 2.5 % of the row), and classifies every value
 //      for the MAD before the median is known: |x - m| < a_lo for every m in
 //      [m_lo, m_hi] (counted), |x - m| > a_hi for every such m (dropped), or
-//      either (listed: about 10 % of a Gaussian row); the same read notes the
+//      either (listed: about 7 % of a Gaussian row); the same read notes the
 //      values at or above a lower bound of the threshold
 //      (m_lo + n_mad * a_lo: thr = med + n_mad * mad is monotone in both);
 //   3. the median: if the window holds both middle ranks, a radix selection
@@ -1255,7 +1255,7 @@ int detect_device(const float *cc, int T, int n_corr, size_t ld, const int *begi
     int *hot, *col_cnt, *row_list;
     float *saved, *amb, *keys;
     // candidates per row: a sample window holds about 2.5 % of a row; the values whose
-    // MAD class waits for the median, about 10 % of a Gaussian row
+    // MAD class waits for the median, about 7 % of a Gaussian row
     // (at least 2 * kSpill rows of every thread's columns, so a row's columns always fit)
     const long long key_cap = std::max(2LL * kSpill * kDetThreads,
                                        n_corr < 65536 ? n_corr : std::max(65536LL, (long long)n_corr / 8));
