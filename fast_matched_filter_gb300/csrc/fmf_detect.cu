@@ -540,7 +540,7 @@ __device__ __forceinline__ void peak_at(const float *row, long long i, long long
 }
 
 // A value of row t at window offset o at or above thr_lo, noted in the row's
-// hot list (the rare path of the MAD counting pass: one atomic, one store;
+// hot list (the rare path of the counting pass: one atomic, one store;
 // det_hot_kernel examines the neighbours later).
 __device__ __forceinline__ void note_hot(DetState *st, int t, long long o, int *hot, int cap)
 {
@@ -776,11 +776,11 @@ __global__ void det_check_kernel(DetState *__restrict__ st, int T, int mode, int
     st[t] = s;
 }
 
-// Histogram update by a whole warp: every lane calls it (lanes whose value
-// does not count pass ok = false); lanes with the same digit add once.
-// With `aggregate` (the first pass, whose keys share few digits) lanes with
-// the same digit add once; otherwise (later passes, digits spread) each lane
-// adds its own count.
+// Histogram update: every lane of the warp calls it (lanes whose value does
+// not count pass ok = false).  With `aggregate` (the first pass over a whole
+// row, whose keys share few digits) lanes with the same digit add once;
+// otherwise (candidates, later passes: digits spread) each lane adds its own
+// count.
 __device__ __forceinline__ void hist_add(unsigned *h, float v, bool ok, int mode, float med, int shift,
                                          unsigned dmask, unsigned high, unsigned p0, unsigned p1,
                                          bool two, int lane, bool aggregate)
@@ -1142,8 +1142,8 @@ det_select_kernel(const DetState *__restrict__ st, const int2 *__restrict__ cand
     while (P < m0)
         P <<= 1;
     const int2 *c = cand + (size_t)t * cap;
-    // 1. the candidates at or above thr (the MAD pass gathers a superset: those at or
-    // above a lower bound of thr), ordered by lag (lags are distinct); the others
+    // 1. the candidates at or above thr (the counting pass gathers a superset: those at
+    // or above a lower bound of thr), ordered by lag (lags are distinct); the others
     // sort last
     int kept = 0;
     for (int i0 = 0; i0 < P; i0 += blockDim.x) {
