@@ -280,8 +280,8 @@ int prepare_problem(const Args &a, Scratch &ws, cudaStream_t s, Problem *Pout, c
     if (window_stats_smem(L, full) > 227 * 1024)
         return set_error(FMF_ERR_SMEM, "template length %d too long for the window-statistics kernel", L);
 
-    int *k_lo, *k_hi;
-    float *stat_e, *mu = nullptr, *dcen = nullptr, *tcen = nullptr, *tsum = nullptr;
+    int *k_lo = nullptr, *k_hi = nullptr;
+    float *stat_e = nullptr, *mu = nullptr, *dcen = nullptr, *tcen = nullptr, *tsum = nullptr;
     if ((rc = ws.get(&k_lo, 2 * (size_t)T, "template ranges")))
         return rc;
     k_hi = k_lo + T;
@@ -300,7 +300,7 @@ int prepare_problem(const Args &a, Scratch &ws, cudaStream_t s, Problem *Pout, c
     count_launch();
     const float *sst = a.sst;
     if (!sst) {  // template energies as numpy computes them for float32 templates
-        float *e;
+        float *e = nullptr;
         if ((rc = ws.get(&e, (size_t)T * SC, "template energies")))
             return rc;
         const int rows = T * SC;
@@ -546,7 +546,7 @@ static int run_streamed(const Args &d, float *host_out, cudaStream_t s)
             if (nt > 0) {
                 if (!tcfull.empty()) {
                     std::vector<unsigned char> sub(tc_prob_size());
-                    unsigned long long *queue;
+                    unsigned long long *queue = nullptr;
                     tc_subset(reinterpret_cast<const TcProb *>(tcfull.data()), t0, nt,
                               reinterpret_cast<TcProb *>(sub.data()));
                     if (!(rc = ws.get(&queue, 1, "tile queue")))
@@ -641,7 +641,7 @@ static int run_host(const Args &a, cudaStream_t s)
     {
         Scratch io(s);  // device copies of the arguments, freed in stream order
         Args d;
-        float *out;
+        float *out = nullptr;
         cudaEvent_t ev_in0 = mark(s);
         if ((rc = copy_inputs(a, io, s, &d)) || (rc = io.get(&out, out_n, "output copy")))
             return rc;
@@ -763,7 +763,7 @@ static int detect_entry(const float *cc, size_t T, size_t n_corr, const int *beg
     // rows in chunks of at most 1 GiB of device memory
     size_t per = ((size_t)1 << 30) / (n_corr * sizeof(float));
     per = per < 1 ? 1 : (per > T ? T : per);
-    float *rows;
+    float *rows = nullptr;
     if ((rc = ws.get(&rows, per * n_corr, "cc rows")))
         return rc;
     for (size_t t0 = 0; t0 < T; t0 += per) {
@@ -820,7 +820,7 @@ static int search_detect_entry(const Args &a0, const DetectOut &o, cudaStream_t 
         dc.sst = d.sst ? d.sst + t0 * SC : nullptr;
         dc.mo = d.mo + t0 * SC;
         dc.w = d.w + t0 * SC;
-        float *cc;
+        float *cc = nullptr;
         if ((rc = wc.get(&cc, nt * a.n_corr, "cc sums")))
             return rc;
         dc.out = cc;
@@ -1012,7 +1012,7 @@ int fmf_template_energies(const float *templates, size_t n_rows, size_t n_sample
     }
     int rc;
     Scratch ws(s);
-    float *dt, *de;
+    float *dt = nullptr, *de = nullptr;
     if ((rc = ws.get(&dt, n_rows * n_samples_template, "templates")) ||
         (rc = ws.get(&de, n_rows, "energies")) ||
         (rc = cuda_status(cudaMemcpyAsync(dt, templates, n_rows * n_samples_template * 4,

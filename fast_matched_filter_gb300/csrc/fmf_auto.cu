@@ -175,7 +175,7 @@ __global__ void auto_template_kernel(const float *__restrict__ tpl, const float 
 int choose_auto_precision(const Problem &P, Scratch &ws, cudaStream_t s, int *precision)
 {
     int rc;
-    unsigned *worst;
+    unsigned *worst = nullptr;
     float *dc = nullptr;
     if ((rc = ws.get(&worst, 1, "precision estimate")))
         return rc;

@@ -103,7 +103,7 @@ static int batch_record(fmf_batch *b, cudaStream_t s)
                             grp.insert(grp.end(), probs.begin() + psz * i, probs.begin() + psz * (i + 1));
                     const size_t ng = grp.size() / psz;
                     for (size_t i0 = 0; i0 < ng && status == FMF_OK; i0 += TC_MAX_PROBS) {
-                        unsigned long long *queue;
+                        unsigned long long *queue = nullptr;
                         if ((status = ws.get(&queue, 1, "tile queue")))
                             break;
                         const int m = (int)(ng - i0 < (size_t)TC_MAX_PROBS ? ng - i0 : TC_MAX_PROBS);

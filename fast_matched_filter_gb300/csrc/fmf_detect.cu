@@ -1249,11 +1249,11 @@ int detect_device(const float *cc, int T, int n_corr, size_t ld, const int *begi
 {
     int rc;
     const int chunk = T < kDetChunk ? T : kDetChunk;
-    DetState *st;
-    unsigned *hist;
-    int2 *cand;
-    int *hot, *col_cnt, *row_list;
-    float *saved, *amb, *keys;
+    DetState *st = nullptr;
+    unsigned *hist = nullptr;
+    int2 *cand = nullptr;
+    int *hot = nullptr, *col_cnt = nullptr, *row_list = nullptr;
+    float *saved = nullptr, *amb = nullptr, *keys = nullptr;
     // candidates per row: a sample window holds about 2.5 % of a row; the values whose
     // MAD class waits for the median, about 7 % of a Gaussian row
     // (at least 2 * kSpill rows of every thread's columns, so a row's columns always fit)

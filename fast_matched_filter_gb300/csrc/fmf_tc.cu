@@ -1111,8 +1111,8 @@ int tc_prepare(const Problem &P, const float *data_for_tc, int split, int nb, in
     const size_t g_elems = (size_t)P.SC * step * TC_CB * pr.rows_total * 8;
     const size_t w_elems = (size_t)P.T * P.SC * step * g.NW * 64;
     const size_t n_meta = (size_t)P.T * P.SC * step;
-    uint16_t *g_hi, *g_lo = nullptr, *w_hi, *w_lo = nullptr;
-    int *mu, *psi;
+    uint16_t *g_hi = nullptr, *g_lo = nullptr, *w_hi = nullptr, *w_lo = nullptr;
+    int *mu = nullptr, *psi = nullptr;
     if ((rc = ws.get(&g_hi, g_elems, "bf16 data streams")) ||
         (split && (rc = ws.get(&g_lo, g_elems, "bf16 data streams (lo)"))) ||
         (rc = ws.get(&w_hi, w_elems, "bf16 template blocks")) ||
@@ -1330,7 +1330,7 @@ int launch_tc(const Problem &P, const float *data_for_tc, int precision, unsigne
     TcProb pr;
     if ((rc = tc_prepare(P, data_for_tc, split, nb, template_group, ws, s, &pr)))
         return rc;
-    unsigned long long *queue;
+    unsigned long long *queue = nullptr;
     if ((rc = ws.get(&queue, 1, "tile queue")))
         return rc;
     return tc_run(&pr, 1, split, queue, err, s);

@@ -533,11 +533,12 @@ static int variable_device(const VArgs &a, int L, cudaStream_t s, float *host_ou
     const int T = (int)a.T, SC = (int)(a.S * a.C), N = (int)a.N;
     const bool full = a.normalize == 1;
     Scratch ws(s);
-    int *k_lo;
-    float *zweight, *consts, *tmask, *tsum = nullptr, *mu = nullptr, *dcen = nullptr;
-    long long *bs2, *pre2q;
-    float2 *bs1, *pre1f = nullptr;
-    float *unit, *epart;
+    int *k_lo = nullptr;
+    float *zweight = nullptr, *consts = nullptr, *tmask = nullptr, *tsum = nullptr, *mu = nullptr,
+          *dcen = nullptr;
+    long long *bs2 = nullptr, *pre2q = nullptr;
+    float2 *bs1 = nullptr, *pre1f = nullptr;
+    float *unit = nullptr, *epart = nullptr;
     const int nblk = (N + kPrefixBlock - 1) / kPrefixBlock;
     if ((rc = ws.get(&k_lo, 2 * (size_t)T, "template ranges")) ||
         (rc = ws.get(&zweight, (size_t)T * SC, "Fisher-z weights")) ||
@@ -648,7 +649,7 @@ static int variable_device(const VArgs &a, int L, cudaStream_t s, float *host_ou
         if (nt > 0) {
             if (!tcfull.empty()) {
                 std::vector<unsigned char> sub(tc_prob_size());
-                unsigned long long *queue;
+                unsigned long long *queue = nullptr;
                 tc_subset(reinterpret_cast<const TcProb *>(tcfull.data()), t0, nt,
                           reinterpret_cast<TcProb *>(sub.data()));
                 if ((rc = ws.get(&queue, 1, "tile queue")) ||
